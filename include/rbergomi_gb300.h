@@ -1,0 +1,161 @@
+/*
+ * rbergomi_gb300.h -- C ABI of the GB300 rough Bergomi Romano-Touzi pricer.
+ *
+ * Two layers:
+ *
+ * 1. Drop-in entry points with the exact signatures, argument meaning, output
+ *    layout and error exits of the reference library's C interface
+ *    (rBergLib/cinterface.h:62-76).  A caller linked against librBergLib can
+ *    relink against librbergomi_gb300.so unchanged.
+ *
+ * 2. An extended, status-returning API (rbg_*) that exposes precision mode,
+ *    convolution backend, Philox seed, path offset and CUDA stream, and never
+ *    exits the process.
+ *
+ * Conventions shared by both layers
+ *   - ParamTot layout: output index i <-> (H, eta, rho)[i / op_size] and
+ *     (T, K)[i % op_size] (rBergLib/ParamTot.h:28-33).  H, eta, rho are aligned
+ *     arrays of length par_size (not a tensor product); T, K have length op_size.
+ *   - S0 = 1, r = 0, constant forward variance xi.
+ *   - Normals come from a counter-based Philox4x32-10 stream: key = the 64-bit
+ *     seed, counter = (step group g, path lo32, path hi32, stream), four normals
+ *     per call for steps 4g..4g+3 of stream 0 (W1) or 1 (W1perp).  Results do
+ *     not depend on batching, thread count or device.
+ */
+#ifndef RBERGOMI_GB300_H
+#define RBERGOMI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Drop-in layer                                                            */
+/* ------------------------------------------------------------------------ */
+
+/* Romano-Touzi prices, implied vols and MC standard errors over the ParamTot
+ * grid.  Replaces computeIVRT_tensor, rBergLib/cinterface.h:68-71
+ * (cinterface.cpp:49-85).  out_size must equal par_size * op_size, else the
+ * process exits with status 17 after a message on stderr; num_threads < 1
+ * exits with status 21 (cinterface.cpp:54-59, 76-81).  num_threads is
+ * otherwise ignored: one GPU does the work.  The seed words are folded into
+ * one 64-bit Philox key (seed[0] when seed_size == 1, splitmix64 chaining
+ * otherwise).  Precision: FP64 unless the environment sets
+ * RBG_PRECISION=mixed.  Any CUDA failure prints to stderr and exits with
+ * status 70. */
+void computeIVRT_tensor(double xi, double* H, double* eta, double* rho, int par_size, double* T, double* K,
+                        int op_size, int N, long M, uint64_t* seed, int seed_size, int num_threads, double* price,
+                        double* iv, double* stat, double* H_tot, double* eta_tot, double* rho_tot, double* T_tot,
+                        double* K_tot, int out_size);
+
+/* RT payoffs for caller-supplied normals.  Replaces
+ * computeIVRT_tensor_quadrature, rBergLib/cinterface.h:73-75
+ * (cinterface.cpp:102-131).  Z holds 2*N*M doubles: sample m uses
+ * Z[2mN, 2mN+N) as W1 and Z[(2m+1)N, (2m+2)N) as W1perp.  payoff receives
+ * M * par_size * op_size doubles, payoff[m*out_size + i].  Always FP64. */
+void computeIVRT_tensor_quadrature(double xi, double* H, double* eta, double* rho, int par_size, double* T,
+                                   double* K, int op_size, int N, long M, double* Z, int num_threads,
+                                   double* payoff);
+
+/* ------------------------------------------------------------------------ */
+/* Extended layer                                                           */
+/* ------------------------------------------------------------------------ */
+
+enum rbg_status {
+    RBG_OK = 0,
+    RBG_ERR_ARG = 1,      /* bad argument (sizes, null pointers, ranges) */
+    RBG_ERR_CUDA = 2,     /* a CUDA runtime call or kernel failed */
+    RBG_ERR_NOMEM = 3,    /* device allocation failed or over budget */
+    RBG_ERR_UNSUPPORTED = 4, /* option combination not available */
+    RBG_ERR_TIMEOUT = 5   /* a bounded device-side wait expired */
+};
+
+enum rbg_precision { RBG_FP64 = 0, RBG_MIXED = 1 };
+
+/* Volterra convolution backend.  AUTO picks the tcgen05 Toeplitz GEMM for
+ * N <= 512 in mixed mode and the direct sum otherwise. */
+enum rbg_conv { RBG_CONV_AUTO = 0, RBG_CONV_GEMM = 1, RBG_CONV_FFT = 2, RBG_CONV_DIRECT = 3 };
+
+/* Normal transform used by the FP64 form: its own FP64 Box-Muller (default),
+ * or the FP32 Box-Muller values of the mixed form widened to FP64, so an FP64
+ * run sees exactly the normals a mixed run with the same seed sees. */
+enum rbg_normals { RBG_NORMALS_F64 = 0, RBG_NORMALS_F32 = 1 };
+
+/* Split used by the mixed-form tensor-core convolution. */
+enum rbg_split { RBG_SPLIT_BF16X3 = 0, RBG_SPLIT_F16X3 = 1 };
+
+typedef struct rbg_params {
+    double xi;
+    const double* H;
+    const double* eta;
+    const double* rho;
+    int par_size;
+    const double* T;
+    const double* K;
+    int op_size;
+    int N;     /* time steps per path (dt = T / N for every maturity) */
+    int64_t M; /* paths */
+} rbg_params;
+
+typedef struct rbg_options {
+    int precision;       /* enum rbg_precision */
+    int conv;            /* enum rbg_conv */
+    int normals;         /* enum rbg_normals (FP64 form only) */
+    int split;           /* enum rbg_split (mixed form only) */
+    int compute_iv;      /* nonzero: fill iv[] (FP64 inversion on the GPU) */
+    uint64_t seed;       /* Philox key */
+    int64_t path_offset; /* global index of the first path (replicas/shards) */
+    void* stream;        /* cudaStream_t to run on; NULL = the library's stream */
+} rbg_options;
+
+/* Fills opts with defaults: FP64, AUTO, F64 normals, BF16x3, iv on, seed 0. */
+void rbg_default_options(rbg_options* opts);
+
+/* Prices on the Philox stream.  price, stat, iv: host arrays of
+ * par_size*op_size doubles (iv may be NULL).  Returns enum rbg_status. */
+int rbg_price_rt(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv);
+
+/* Same, with the raw sums instead of finished moments: sum[i] = sum_m x,
+ * sum2[i] = sum_m x^2 over this call's paths (for merging shards/replicas). */
+int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, double* sum2);
+
+/* Per-path payoffs for caller-supplied normals (quadrature layout).  Z and
+ * payoff are host pointers unless device_ptrs != 0, in which case both are
+ * device pointers on the current device.  FP64 only. */
+int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs);
+
+/* Writes the normals the pricer would draw for paths
+ * [path_offset, path_offset + M), N steps, streams W1 and W1perp, in the
+ * quadrature layout (M * 2 * N doubles, host pointer).  precision selects the
+ * FP64 or the FP32 transform (the latter widened exactly to double). */
+int rbg_generate_normals(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, double* Z);
+
+/* Implied vols of call prices (S0 = 1, r = 0) on the GPU; NaN where no
+ * volatility reproduces the price. */
+int rbg_implied_vol(int n, const double* price, const double* K, const double* T, double* iv);
+
+/* Message for the last failing rbg_* call on this thread. */
+const char* rbg_last_error(void);
+
+/* Number of kernels this library has launched in this process. */
+uint64_t rbg_launch_count(void);
+
+/* Waits for the library's stream on the current device. */
+int rbg_synchronize(void);
+
+/* Releases the cached device buffers and tables of the current device. */
+int rbg_release(void);
+
+/* Host-only introspection of the ParamTot plan (no GPU needed): the number
+ * of distinct Volterra passes (H values), variance groups ((H, T, eta)
+ * after the reference's trigger chain) and outputs; vgroup_of_output
+ * (length par_size*op_size, may be NULL) receives each output's group. */
+int rbg_plan_info(const rbg_params* p, int* n_vol, int* n_vgroups, int* n_out, int* vgroup_of_output);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RBERGOMI_GB300_H */

@@ -1,0 +1,249 @@
+"""rbergomi_gb300 -- GB300-native rough Bergomi Romano-Touzi pricer.
+
+A ctypes binding of ``librbergomi_gb300.so`` (C ABI in
+``include/rbergomi_gb300.h``).  The functions mirror the reference's
+interface (rBergLib/cinterface.h, rBergLib/interface.h): the same argument
+meaning, ParamTot output layout and result fields (``price``, ``iv``,
+``stat`` and the ``*_tot`` parameter echoes).
+
+There is no CPU fallback: importing works without a GPU, but every pricing
+call runs the CUDA kernels and fails loudly if the library or the GPU is
+missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "librbergomi_gb300.so")
+
+FP64, MIXED = 0, 1
+CONV_AUTO, CONV_GEMM, CONV_FFT, CONV_DIRECT = 0, 1, 2, 3
+NORMALS_F64, NORMALS_F32 = 0, 1
+SPLIT_BF16X3, SPLIT_F16X3 = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_u64p = C.POINTER(C.c_uint64)
+
+
+class RbgParams(C.Structure):
+    _fields_ = [("xi", C.c_double), ("H", _dp), ("eta", _dp), ("rho", _dp), ("par_size", C.c_int),
+                ("T", _dp), ("K", _dp), ("op_size", C.c_int), ("N", C.c_int), ("M", C.c_int64)]
+
+
+class RbgOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("conv", C.c_int), ("normals", C.c_int), ("split", C.c_int),
+                ("compute_iv", C.c_int), ("seed", C.c_uint64), ("path_offset", C.c_int64),
+                ("stream", C.c_void_p)]
+
+
+class RbgError(RuntimeError):
+    pass
+
+
+_lib = None
+
+EXPORTS = [
+    "computeIVRT_tensor", "computeIVRT_tensor_quadrature", "rbg_default_options", "rbg_price_rt",
+    "rbg_price_rt_sums", "rbg_payoffs_rt", "rbg_generate_normals", "rbg_implied_vol", "rbg_last_error",
+    "rbg_launch_count", "rbg_synchronize", "rbg_release", "rbg_plan_info",
+]
+
+
+def lib():
+    """The loaded shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RbgError(f"{LIB_PATH} is missing; build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        full = [C.c_double, _dp, _dp, _dp, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_long, _u64p, C.c_int,
+                C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int]
+        L.computeIVRT_tensor.argtypes = full
+        L.computeIVRT_tensor.restype = None
+        L.computeIVRT_tensor_quadrature.argtypes = [C.c_double, _dp, _dp, _dp, C.c_int, _dp, _dp, C.c_int,
+                                                    C.c_int, C.c_long, _dp, C.c_int, _dp]
+        L.computeIVRT_tensor_quadrature.restype = None
+        P, O = C.POINTER(RbgParams), C.POINTER(RbgOptions)
+        L.rbg_default_options.argtypes = [O]
+        L.rbg_price_rt.argtypes = [P, O, _dp, _dp, _dp]
+        L.rbg_price_rt.restype = C.c_int
+        L.rbg_price_rt_sums.argtypes = [P, O, _dp, _dp]
+        L.rbg_price_rt_sums.restype = C.c_int
+        L.rbg_payoffs_rt.argtypes = [P, O, C.c_void_p, C.c_void_p, C.c_int]
+        L.rbg_payoffs_rt.restype = C.c_int
+        L.rbg_generate_normals.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int, C.c_int, _dp]
+        L.rbg_generate_normals.restype = C.c_int
+        L.rbg_implied_vol.argtypes = [C.c_int, _dp, _dp, _dp, _dp]
+        L.rbg_implied_vol.restype = C.c_int
+        L.rbg_last_error.restype = C.c_char_p
+        L.rbg_launch_count.restype = C.c_uint64
+        L.rbg_synchronize.restype = C.c_int
+        L.rbg_release.restype = C.c_int
+        L.rbg_plan_info.argtypes = [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]
+        L.rbg_plan_info.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise RbgError(f"rbg status {rc}: {lib().rbg_last_error().decode()}")
+
+
+def _arr(x) -> np.ndarray:
+    return np.ascontiguousarray(np.atleast_1d(np.asarray(x, dtype=np.float64)))
+
+
+class _Params:
+    """Keeps the numpy arrays alive behind an RbgParams struct."""
+
+    def __init__(self, xi, H, eta, rho, T, K, N, M):
+        self.H, self.eta, self.rho = _arr(H), _arr(eta), _arr(rho)
+        self.T, self.K = _arr(T), _arr(K)
+        if not (len(self.H) == len(self.eta) == len(self.rho)):
+            raise ValueError("H, eta, rho must have the same length (par_size)")
+        if len(self.T) != len(self.K):
+            raise ValueError("T and K must have the same length (op_size)")
+        self.s = RbgParams(float(xi), self.H.ctypes.data_as(_dp), self.eta.ctypes.data_as(_dp),
+                           self.rho.ctypes.data_as(_dp), len(self.H), self.T.ctypes.data_as(_dp),
+                           self.K.ctypes.data_as(_dp), len(self.T), int(N), int(M))
+        self.out = len(self.H) * len(self.T)
+
+
+def options(precision=FP64, conv=CONV_AUTO, normals=NORMALS_F64, split=SPLIT_BF16X3, compute_iv=True, seed=0,
+            path_offset=0, stream=None) -> RbgOptions:
+    o = RbgOptions()
+    lib().rbg_default_options(C.byref(o))
+    o.precision, o.conv, o.normals, o.split = precision, conv, normals, split
+    o.compute_iv = 1 if compute_iv else 0
+    o.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    o.path_offset = int(path_offset)
+    o.stream = stream
+    return o
+
+
+@dataclass
+class ResultSimple:
+    """Same fields as the reference's ResultSimple (rBergLib/interface.h:23-36)."""
+    price: np.ndarray
+    iv: np.ndarray
+    H: np.ndarray
+    rho: np.ndarray
+    eta: np.ndarray
+    T: np.ndarray
+    K: np.ndarray
+    xi: float
+    stat: np.ndarray
+    N: int
+    M: int
+    numThreads: int
+
+
+def computeIVRT_tensor(xi, H, eta, rho, T, K, N, M, seed, num_threads=1) -> ResultSimple:
+    """Drop-in RT pricing (rBergLib/cinterface.h:68-71) through the C ABI."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    seed = np.ascontiguousarray(np.atleast_1d(np.asarray(seed, dtype=np.uint64)))
+    outs = [np.empty(p.out) for _ in range(8)]
+    lib().computeIVRT_tensor(float(xi), p.s.H, p.s.eta, p.s.rho, p.s.par_size, p.s.T, p.s.K, p.s.op_size, int(N),
+                             int(M), seed.ctypes.data_as(_u64p), len(seed), int(num_threads),
+                             *[o.ctypes.data_as(_dp) for o in outs], p.out)
+    price, iv, stat, Ht, et, rt, Tt, Kt = outs
+    return ResultSimple(price, iv, Ht, rt, et, Tt, Kt, float(xi), stat, int(N), int(M), int(num_threads))
+
+
+def computeIVRT_tensor_quadrature(xi, H, eta, rho, T, K, Z, num_threads=1) -> np.ndarray:
+    """Drop-in per-sample RT payoffs (rBergLib/cinterface.h:73-75).
+
+    Z: normals [M, 2, N] (or flat 2*N*M).  Returns payoff [M, par_size*op_size]."""
+    Z = np.ascontiguousarray(Z, dtype=np.float64)
+    M, two, N = Z.shape
+    if two != 2:
+        raise ValueError("Z must be [M, 2, N]")
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    pay = np.empty((M, p.out))
+    lib().computeIVRT_tensor_quadrature(float(xi), p.s.H, p.s.eta, p.s.rho, p.s.par_size, p.s.T, p.s.K,
+                                        p.s.op_size, int(N), int(M), Z.ctypes.data_as(_dp), int(num_threads),
+                                        pay.ctypes.data_as(_dp))
+    return pay
+
+
+def price_rt(xi, H, eta, rho, T, K, N, M, **opts):
+    """Extended API: returns (price, stat, iv) arrays."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    o = options(**opts)
+    price, stat, iv = np.empty(p.out), np.empty(p.out), np.empty(p.out)
+    _check(lib().rbg_price_rt(C.byref(p.s), C.byref(o), price.ctypes.data_as(_dp), stat.ctypes.data_as(_dp),
+                              iv.ctypes.data_as(_dp)))
+    return price, stat, iv
+
+
+def price_rt_sums(xi, H, eta, rho, T, K, N, M, **opts):
+    """Extended API: raw (sum x, sum x^2) per output over this call's paths."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    o = options(**opts)
+    s1, s2 = np.empty(p.out), np.empty(p.out)
+    _check(lib().rbg_price_rt_sums(C.byref(p.s), C.byref(o), s1.ctypes.data_as(_dp), s2.ctypes.data_as(_dp)))
+    return s1, s2
+
+
+def payoffs_rt(xi, H, eta, rho, T, K, Z, device_ptrs=False, M=None, N=None, **opts):
+    """Per-path FP64 payoffs.  Z is a host [M, 2, N] array, or (device_ptrs=True)
+    a device address with M, N given; then payoff is returned as None and the
+    caller passes ``out`` via opts['out_ptr']."""
+    out_ptr = opts.pop("out_ptr", None)
+    o = options(**opts)
+    if device_ptrs:
+        p = _Params(xi, H, eta, rho, T, K, N, M)
+        _check(lib().rbg_payoffs_rt(C.byref(p.s), C.byref(o), C.c_void_p(int(Z)), C.c_void_p(int(out_ptr)), 1))
+        return None
+    Z = np.ascontiguousarray(Z, dtype=np.float64)
+    M, two, N = Z.shape
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    pay = np.empty((M, p.out))
+    _check(lib().rbg_payoffs_rt(C.byref(p.s), C.byref(o), Z.ctypes.data, pay.ctypes.data, 0))
+    return pay
+
+
+def generate_normals(seed, M, N, precision=FP64, path_offset=0) -> np.ndarray:
+    """The normals the pricer draws: [M, 2, N] float64 (FP32 values widened
+    exactly when precision=MIXED)."""
+    Z = np.empty((M, 2, N))
+    _check(lib().rbg_generate_normals(int(seed) & 0xFFFFFFFFFFFFFFFF, int(path_offset), int(M), int(N),
+                                      int(precision), Z.ctypes.data_as(_dp)))
+    return Z
+
+
+def implied_vol(price, K, T) -> np.ndarray:
+    price, K, T = _arr(price), _arr(K), _arr(T)
+    iv = np.empty(len(price))
+    _check(lib().rbg_implied_vol(len(price), price.ctypes.data_as(_dp), K.ctypes.data_as(_dp),
+                                 T.ctypes.data_as(_dp), iv.ctypes.data_as(_dp)))
+    return iv
+
+
+def plan_info(xi, H, eta, rho, T, K, N, M=1):
+    """Host-only: (n_volterra_passes, n_variance_groups, group_of_output)."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    nv, ng, no = C.c_int(), C.c_int(), C.c_int()
+    groups = (C.c_int * p.out)()
+    _check(lib().rbg_plan_info(C.byref(p.s), C.byref(nv), C.byref(ng), C.byref(no), groups))
+    return nv.value, ng.value, np.array(list(groups), dtype=np.int64)
+
+
+def launch_count() -> int:
+    return int(lib().rbg_launch_count())
+
+
+def synchronize() -> None:
+    _check(lib().rbg_synchronize())
+
+
+def release() -> None:
+    _check(lib().rbg_release())

@@ -1,0 +1,515 @@
+// rbg_api.cpp -- host side of librbergomi_gb300: device contexts, cached
+// buffers and tables, the drop-in C ABI and the extended rbg_* API.
+//
+// The drop-in functions keep the reference's observable behaviour
+// (rBergLib/cinterface.cpp): same argument meaning and output layout, the
+// same stderr message + exit(17) on out_size != par_size * op_size and
+// exit(21) on num_threads < 1.  GPU failures, which the reference cannot
+// have, exit with status 70 after a message.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rbg_internal.hpp"
+#include "rbg_mixed.hpp"
+
+namespace rbg {
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define RBG_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess) {                                                                \
+            cudaGetLastError();                                                                 \
+            return fail(RBG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+        }                                                                                       \
+    } while (0)
+
+// Grow-only device buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    int ensure(size_t bytes)
+    {
+        if (bytes <= n) return 0;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t want = std::max(bytes, (size_t)256);
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            return -1;
+        }
+        n = want;
+        return 0;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    template <class T>
+    T* as() const { return (T*)p; }
+};
+
+struct Ctx {
+    int dev = -1;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    DevBuf z, ivb, part, acc, tabs, res, pay, mixed_ws;
+    ~Ctx() {}
+};
+
+static std::mutex g_ctx_mu;
+static std::map<int, std::unique_ptr<Ctx>> g_ctx;
+
+static int get_ctx(Ctx** out)
+{
+    int dev = 0;
+    RBG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    auto& slot = g_ctx[dev];
+    if (!slot) {
+        std::unique_ptr<Ctx> c(new Ctx());
+        c->dev = dev;
+        RBG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        slot = std::move(c);
+    }
+    *out = slot.get();
+    return RBG_OK;
+}
+
+static int ensure(DevBuf& b, size_t bytes, const char* what)
+{
+    if (b.ensure(bytes)) return fail(RBG_ERR_NOMEM, std::string("device allocation failed: ") + what);
+    return RBG_OK;
+}
+
+// ---------------------------------------------------------------- tables
+struct TableSet {
+    Fp64Tables t{};
+    const double* Tvals = nullptr;
+};
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts)
+{
+    const int nv = (int)plan.vols.size(), ng = (int)plan.vgs.size(), no = (int)plan.outs.size(), N = plan.N;
+    std::vector<VolDev> vols(nv);
+    for (int v = 0; v < nv; ++v) vols[v] = VolDev{plan.vols[v].a1, plan.vols[v].a2, plan.vols[v].vg_begin, plan.vols[v].vg_end};
+    std::vector<VGDev> vgs(ng);
+    for (int g = 0; g < ng; ++g) {
+        const VGroup& G = plan.vgs[g];
+        vgs[g] = VGDev{G.scale, G.eta, G.dt, G.sdt, plan.xi, G.nsteps, G.vol};
+    }
+    std::vector<OutDev> outs(no);
+    std::vector<double> Tv(no);
+    for (int i = 0; i < no; ++i) {
+        outs[i] = OutDev{plan.outs[i].rho, plan.outs[i].K, plan.outs[i].vg, 0};
+        Tv[i] = plan.outs[i].T;
+    }
+    size_t off_vols = 0;
+    size_t off_vgs = align_up(off_vols + sizeof(VolDev) * nv, 256);
+    size_t off_outs = align_up(off_vgs + sizeof(VGDev) * ng, 256);
+    size_t off_T = align_up(off_outs + sizeof(OutDev) * no, 256);
+    size_t off_gamma = align_up(off_T + sizeof(double) * no, 256);
+    size_t off_comp = align_up(off_gamma + sizeof(double) * plan.gamma.size(), 256);
+    size_t total = align_up(off_comp + sizeof(double) * plan.comp.size(), 256);
+    std::vector<unsigned char> host(total, 0);
+    std::memcpy(host.data() + off_vols, vols.data(), sizeof(VolDev) * nv);
+    std::memcpy(host.data() + off_vgs, vgs.data(), sizeof(VGDev) * ng);
+    std::memcpy(host.data() + off_outs, outs.data(), sizeof(OutDev) * no);
+    std::memcpy(host.data() + off_T, Tv.data(), sizeof(double) * no);
+    std::memcpy(host.data() + off_gamma, plan.gamma.data(), sizeof(double) * plan.gamma.size());
+    std::memcpy(host.data() + off_comp, plan.comp.data(), sizeof(double) * plan.comp.size());
+    int rc = ensure(c.tabs, total, "tables");
+    if (rc) return rc;
+    RBG_CUDA(cudaMemcpyAsync(c.tabs.p, host.data(), total, cudaMemcpyHostToDevice, st));
+    // the host staging vector dies at return: make the copy complete first
+    RBG_CUDA(cudaStreamSynchronize(st));
+    unsigned char* base = (unsigned char*)c.tabs.p;
+    ts.t.vols = (const VolDev*)(base + off_vols);
+    ts.t.vgs = (const VGDev*)(base + off_vgs);
+    ts.t.outs = (const OutDev*)(base + off_outs);
+    ts.t.gamma = (const double*)(base + off_gamma);
+    ts.t.comp = (const double*)(base + off_comp);
+    ts.t.n_vol = nv;
+    ts.t.n_vg = ng;
+    ts.t.n_out = no;
+    ts.t.N = N;
+    ts.t.xi = plan.xi;
+    ts.Tvals = (const double*)(base + off_T);
+    return RBG_OK;
+}
+
+// ------------------------------------------------------------ FP64 form
+static const int64_t kChunkTarget = 608;  // ~4 chunks per SM of a 152-SM part
+
+static int64_t fp64_batch(const Plan& plan, int64_t M)
+{
+    // normals (16 N B/path) within 2 GiB, variance-path sums within 1 GiB
+    int64_t by_z = ((int64_t)1 << 31) / (16 * (int64_t)plan.N);
+    int64_t by_iv = ((int64_t)1 << 30) / (16 * (int64_t)std::max<size_t>(1, plan.vgs.size()));
+    int64_t B = std::min(by_z, by_iv);
+    B = std::max<int64_t>(256, B / 256 * 256);
+    return std::min(B, M);
+}
+
+static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M, cudaStream_t st,
+                      double* host_res)
+{
+    TableSet ts;
+    int rc = upload_tables(c, plan, st, ts);
+    if (rc) return rc;
+    const int no = (int)plan.outs.size(), N = plan.N;
+    const int64_t B = fp64_batch(plan, M);
+    if ((rc = ensure(c.z, sizeof(double) * 2 * N * (size_t)B, "normals"))) return rc;
+    if ((rc = ensure(c.ivb, sizeof(double) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
+    const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+    if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
+    if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
+    if ((rc = ensure(c.res, sizeof(double) * 5 * no, "results"))) return rc;
+    RBG_CUDA(cudaMemsetAsync(c.acc.p, 0, sizeof(double) * 4 * no, st));
+    for (int64_t m0 = 0; m0 < M; m0 += B) {
+        const int64_t b = std::min(B, M - m0);
+        launch_normals(o.seed, o.path_offset + m0, b, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st);
+        launch_path_fp64(ts.t, c.z.as<double>(), b, c.ivb.as<double>(), st);
+        const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
+        launch_payoff_sums(ts.t, c.ivb.as<double>(), b, b, G, c.part.as<double>(), nchunks, st);
+        launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+        RBG_CUDA(cudaGetLastError());
+    }
+    launch_finalize(c.acc.as<double>(), no, M, ts.t.outs, ts.Tvals, o.compute_iv, c.res.as<double>(), st);
+    RBG_CUDA(cudaGetLastError());
+    RBG_CUDA(cudaMemcpyAsync(host_res, c.res.p, sizeof(double) * 5 * no, cudaMemcpyDeviceToHost, st));
+    RBG_CUDA(cudaStreamSynchronize(st));
+    return RBG_OK;
+}
+
+// Mixed form: tcgen05 fused path kernel writes FP32 (Ivdt, IsvdW) per
+// (variance group, path); the FP64 payoff/sum kernels finish.
+static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M, cudaStream_t st,
+                       double* host_res)
+{
+    TableSet ts;
+    int rc = upload_tables(c, plan, st, ts);
+    if (rc) return rc;
+    const int no = (int)plan.outs.size();
+    MixedJob job{};
+    if ((rc = mixed_prepare(plan, o, M, job, g_err))) return rc;
+    const int64_t B = job.batch;
+    if ((rc = ensure(c.ivb, sizeof(double) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
+    const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
+    const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+    if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
+    if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
+    if ((rc = ensure(c.res, sizeof(double) * 5 * no, "results"))) return rc;
+    if ((rc = mixed_upload(job, c.mixed_ws.p, st, g_err))) return rc;
+    RBG_CUDA(cudaMemsetAsync(c.acc.p, 0, sizeof(double) * 4 * no, st));
+    for (int64_t m0 = 0; m0 < M; m0 += B) {
+        const int64_t b = std::min(B, M - m0);
+        if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, c.ivb.as<double>(), st, g_err)))
+            return rc;
+        const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
+        launch_payoff_sums(ts.t, c.ivb.as<double>(), b, b, G, c.part.as<double>(), nchunks, st);
+        launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+        RBG_CUDA(cudaGetLastError());
+    }
+    if ((rc = mixed_check(job, c.mixed_ws.p, st, g_err))) return rc;
+    launch_finalize(c.acc.as<double>(), no, M, ts.t.outs, ts.Tvals, o.compute_iv, c.res.as<double>(), st);
+    RBG_CUDA(cudaGetLastError());
+    RBG_CUDA(cudaMemcpyAsync(host_res, c.res.p, sizeof(double) * 5 * no, cudaMemcpyDeviceToHost, st));
+    RBG_CUDA(cudaStreamSynchronize(st));
+    return RBG_OK;
+}
+
+static int price_any(const rbg_params* p, const rbg_options* o, std::vector<double>& res)
+{
+    if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
+    res.assign(5 * plan.outs.size(), 0.0);
+    if (o->precision == RBG_FP64) {
+        if (o->conv == RBG_CONV_GEMM || o->conv == RBG_CONV_FFT)
+            return fail(RBG_ERR_UNSUPPORTED, "FP64 form uses the direct Volterra sum");
+        return price_fp64(*c, plan, *o, p->M, st, res.data());
+    }
+    if (o->precision == RBG_MIXED) return price_mixed(*c, plan, *o, p->M, st, res.data());
+    return fail(RBG_ERR_ARG, "unknown precision");
+}
+
+static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payoff, int device_ptrs,
+                              cudaStream_t user_stream)
+{
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
+    if (!Z || !payoff) return fail(RBG_ERR_ARG, "null Z/payoff");
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaStream_t st = user_stream ? user_stream : c->stream;
+    TableSet ts;
+    if ((rc = upload_tables(*c, plan, st, ts))) return rc;
+    const int no = (int)plan.outs.size(), N = plan.N;
+    const int64_t M = p->M;
+    int64_t B = fp64_batch(plan, M);
+    // payoffs of a batch within 1 GiB too
+    B = std::min<int64_t>(B, std::max<int64_t>(256, ((int64_t)1 << 30) / (8 * (int64_t)no)));
+    if ((rc = ensure(c->ivb, sizeof(double) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    if (!device_ptrs) {
+        if ((rc = ensure(c->z, sizeof(double) * 2 * N * (size_t)B, "normals"))) return rc;
+        if ((rc = ensure(c->pay, sizeof(double) * no * (size_t)B, "payoffs"))) return rc;
+    }
+    for (int64_t m0 = 0; m0 < M; m0 += B) {
+        const int64_t b = std::min(B, M - m0);
+        const double* Zd;
+        double* Pd;
+        if (device_ptrs) {
+            Zd = Z + m0 * 2 * N;
+            Pd = payoff + m0 * no;
+        } else {
+            RBG_CUDA(cudaMemcpyAsync(c->z.p, Z + m0 * 2 * N, sizeof(double) * 2 * N * b, cudaMemcpyHostToDevice, st));
+            Zd = c->z.as<double>();
+            Pd = c->pay.as<double>();
+        }
+        launch_path_fp64(ts.t, Zd, b, c->ivb.as<double>(), st);
+        launch_payoff_store(ts.t, c->ivb.as<double>(), b, b, Pd, st);
+        RBG_CUDA(cudaGetLastError());
+        if (!device_ptrs)
+            RBG_CUDA(cudaMemcpyAsync(payoff + m0 * no, Pd, sizeof(double) * no * b, cudaMemcpyDeviceToHost, st));
+    }
+    RBG_CUDA(cudaStreamSynchronize(st));
+    return RBG_OK;
+}
+
+}  // namespace rbg
+
+using namespace rbg;
+
+// ===================================================================== ABI
+extern "C" {
+
+void rbg_default_options(rbg_options* o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precision = RBG_FP64;
+    o->conv = RBG_CONV_AUTO;
+    o->normals = RBG_NORMALS_F64;
+    o->split = RBG_SPLIT_BF16X3;
+    o->compute_iv = 1;
+}
+
+const char* rbg_last_error(void) { return g_err.c_str(); }
+
+uint64_t rbg_launch_count(void) { return g_launches.load(); }
+
+int rbg_price_rt(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv)
+{
+    std::vector<double> res;
+    int rc = price_any(p, o, res);
+    if (rc) return rc;
+    const size_t no = res.size() / 5;
+    if (price) std::memcpy(price, res.data(), no * sizeof(double));
+    if (stat) std::memcpy(stat, res.data() + no, no * sizeof(double));
+    if (iv) std::memcpy(iv, res.data() + 2 * no, no * sizeof(double));
+    return RBG_OK;
+}
+
+int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, double* sum2)
+{
+    std::vector<double> res;
+    int rc = price_any(p, o, res);
+    if (rc) return rc;
+    const size_t no = res.size() / 5;
+    if (sum) std::memcpy(sum, res.data() + 3 * no, no * sizeof(double));
+    if (sum2) std::memcpy(sum2, res.data() + 4 * no, no * sizeof(double));
+    return RBG_OK;
+}
+
+int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs)
+{
+    if (!p) return fail(RBG_ERR_ARG, "null params");
+    if (o && o->precision != RBG_FP64) return fail(RBG_ERR_UNSUPPORTED, "per-path payoffs are FP64 only");
+    return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr);
+}
+
+int rbg_generate_normals(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, double* Z)
+{
+    if (M < 1 || N < 1 || !Z) return fail(RBG_ERR_ARG, "bad sizes");
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const int64_t B = std::max<int64_t>(1, std::min<int64_t>(M, ((int64_t)1 << 30) / (16 * (int64_t)N)));
+    if ((rc = ensure(c->z, sizeof(double) * 2 * N * (size_t)B, "normals"))) return rc;
+    for (int64_t m0 = 0; m0 < M; m0 += B) {
+        const int64_t b = std::min(B, M - m0);
+        launch_normals(seed, path_offset + m0, b, N, precision == RBG_MIXED, c->z.as<double>(), c->stream);
+        RBG_CUDA(cudaGetLastError());
+        RBG_CUDA(cudaMemcpyAsync(Z + m0 * 2 * N, c->z.p, sizeof(double) * 2 * N * b, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    }
+    RBG_CUDA(cudaStreamSynchronize(c->stream));
+    return RBG_OK;
+}
+
+int rbg_implied_vol(int n, const double* price, const double* K, const double* T, double* iv)
+{
+    if (n < 0 || (n > 0 && (!price || !K || !T || !iv))) return fail(RBG_ERR_ARG, "bad arguments");
+    if (n == 0) return RBG_OK;
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if ((rc = ensure(c->res, sizeof(double) * 4 * (size_t)n, "iv buffers"))) return rc;
+    double* d = c->res.as<double>();
+    RBG_CUDA(cudaMemcpyAsync(d, price, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    RBG_CUDA(cudaMemcpyAsync(d + n, K, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    RBG_CUDA(cudaMemcpyAsync(d + 2 * n, T, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    launch_implied_vol(n, d, d + n, d + 2 * n, d + 3 * n, c->stream);
+    RBG_CUDA(cudaGetLastError());
+    RBG_CUDA(cudaMemcpyAsync(iv, d + 3 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    RBG_CUDA(cudaStreamSynchronize(c->stream));
+    return RBG_OK;
+}
+
+int rbg_synchronize(void)
+{
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    RBG_CUDA(cudaStreamSynchronize(c->stream));
+    return RBG_OK;
+}
+
+int rbg_release(void)
+{
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    RBG_CUDA(cudaStreamSynchronize(c->stream));
+    for (DevBuf* b : {&c->z, &c->ivb, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws}) b->release();
+    mixed_release_cache();
+    return RBG_OK;
+}
+
+int rbg_plan_info(const rbg_params* p, int* n_vol, int* n_vgroups, int* n_out, int* vgroup_of_output)
+{
+    if (!p) return fail(RBG_ERR_ARG, "null params");
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
+    if (n_vol) *n_vol = (int)plan.vols.size();
+    if (n_vgroups) *n_vgroups = (int)plan.vgs.size();
+    if (n_out) *n_out = (int)plan.outs.size();
+    if (vgroup_of_output)
+        for (size_t i = 0; i < plan.outs.size(); ++i) vgroup_of_output[i] = plan.outs[i].vg;
+    return RBG_OK;
+}
+
+// ------------------------------------------------------------- drop-in
+static void die_on(int rc)
+{
+    if (rc == RBG_OK) return;
+    std::cerr << "rbergomi_gb300: " << rbg_last_error() << "\n";
+    std::exit(70);
+}
+
+static void fill_tot(double* H, double* eta, double* rho, int par_size, double* T, double* K, int op_size,
+                     double* H_tot, double* eta_tot, double* rho_tot, double* T_tot, double* K_tot)
+{
+    const long out = (long)par_size * op_size;
+    for (long i = 0; i < out; ++i) {
+        H_tot[i] = H[i / op_size];
+        eta_tot[i] = eta[i / op_size];
+        rho_tot[i] = rho[i / op_size];
+        T_tot[i] = T[i % op_size];
+        K_tot[i] = K[i % op_size];
+    }
+}
+
+static uint64_t fold_seed(const uint64_t* seed, int seed_size)
+{
+    if (!seed || seed_size <= 0) return 0;
+    uint64_t h = seed[0];
+    for (int i = 1; i < seed_size; ++i) {
+        uint64_t x = h + seed[i];
+        x += 0x9E3779B97F4A7C15ull;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        h = x ^ (x >> 31);
+    }
+    return h;
+}
+
+void computeIVRT_tensor(double xi, double* H, double* eta, double* rho, int par_size, double* T, double* K,
+                        int op_size, int N, long M, uint64_t* seed, int seed_size, int num_threads, double* price,
+                        double* iv, double* stat, double* H_tot, double* eta_tot, double* rho_tot, double* T_tot,
+                        double* K_tot, int out_size)
+{
+    if (out_size != par_size * op_size) {
+        std::cerr << "Output arrays have wrong size:\n"
+                  << "par_size * op_size = " << par_size * op_size << " != out_size.\n";
+        std::exit(17);
+    }
+    if (num_threads < 1) {
+        std::cerr << "Number of threads has to be a positive integer,\n"
+                  << "obtained num_threads = " << num_threads << ".\n";
+        std::exit(21);
+    }
+    rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
+    rbg_options o;
+    rbg_default_options(&o);
+    const char* prec = std::getenv("RBG_PRECISION");
+    if (prec && std::strcmp(prec, "mixed") == 0) o.precision = RBG_MIXED;
+    o.seed = fold_seed(seed, seed_size);
+    die_on(rbg_price_rt(&p, &o, price, stat, iv));
+    fill_tot(H, eta, rho, par_size, T, K, op_size, H_tot, eta_tot, rho_tot, T_tot, K_tot);
+}
+
+void computeIVRT_tensor_quadrature(double xi, double* H, double* eta, double* rho, int par_size, double* T,
+                                   double* K, int op_size, int N, long M, double* Z, int num_threads,
+                                   double* payoff)
+{
+    (void)num_threads;
+    if (M <= 0) return;
+    rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
+    die_on(rbg_payoffs_rt(&p, nullptr, Z, payoff, 0));
+}
+
+}  // extern "C"

@@ -1,0 +1,337 @@
+// rbg_fp64.cu -- the plain FP64 form of the RT pricer on the GPU.
+//
+// Kernels (one pass over a batch of paths):
+//   k_normals      Philox4x32-10 -> FP64 normals, quadrature layout [B][2][N]
+//   k_path_fp64    per path: Volterra sum Y2 = (W1 * Gamma)[0..N) as a direct
+//                  causal FP64 sum, X = Y2 + a1 W1 + a2 W1perp, then for every
+//                  variance group v, Ivdt = dt sum v, IsvdW = sum sqrt(v) sdt W1
+//                  (rBergLib/rBergomiMT.cpp:73-109, 163-167, 427-436)
+//   k_payoff_sums  conditional BS per (path, output) and compensated per-chunk
+//                  sums of x and x^2 (rBergomiMT.cpp:598-602, 404-409)
+//   k_accumulate   fixed-order Neumaier merge of chunk sums (deterministic)
+//   k_finalize     price, stat (reference formula), implied vol
+//   k_payoff_store per-path payoffs for the quadrature entry point
+// GB300's FP64 pipe (~2 DFMA/clk/SM) bounds every kernel here except the
+// normal writer; this form exists for 1e-12 parity, not speed.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+#include "rbg_device.cuh"
+#include "rbg_internal.hpp"
+
+namespace rbg {
+
+// ------------------------------------------------------------------ normals
+template <int F32>
+__global__ void k_normals(uint64_t seed, int64_t path0, int64_t B, int N, double* __restrict__ Z)
+{
+    const int ng = (N + 3) >> 2;
+    const int64_t total = B * 2 * ng;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int g = (int)(t % ng);
+        const int64_t r = t / ng;
+        const int s = (int)(r & 1);
+        const int64_t m = r >> 1;
+        const uint4 x = philox_group(seed, (uint64_t)(path0 + m), (uint32_t)g, (uint32_t)s);
+        double z[4];
+        if (F32) {
+            float f0, f1, f2, f3;
+            box_muller_f32(x.x, x.y, f0, f1);
+            box_muller_f32(x.z, x.w, f2, f3);
+            z[0] = f0; z[1] = f1; z[2] = f2; z[3] = f3;
+        } else {
+            box_muller_f64(x.x, x.y, z[0], z[1]);
+            box_muller_f64(x.z, x.w, z[2], z[3]);
+        }
+        double* o = Z + (m * 2 + s) * (int64_t)N + 4 * g;
+        const int left = N - 4 * g;
+        if (left >= 4) {
+            o[0] = z[0]; o[1] = z[1]; o[2] = z[2]; o[3] = z[3];
+        } else {
+            for (int q = 0; q < left; ++q) o[q] = z[q];
+        }
+    }
+}
+
+void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream)
+{
+    const int64_t total = B * 2 * ((N + 3) / 4);
+    const int threads = 256;
+    int64_t blocks = (total + threads - 1) / threads;
+    if (blocks > (1 << 20)) blocks = 1 << 20;
+    if (f32) k_normals<1><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(seed, path0, B, N, Z);
+    else k_normals<0><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(seed, path0, B, N, Z);
+    count_launch();
+}
+
+// --------------------------------------------------------------- path pass
+// One warp per path.  Shared memory: Gamma of the current pass (N doubles),
+// then per warp W1 (N) and X (N).
+__global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t B, double2* __restrict__ ivb)
+{
+    extern __shared__ double sm[];
+    const int N = t.N;
+    const int warps = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* G = sm;
+    double* W1s = sm + N + (size_t)w * 2 * N;
+    double* X = W1s + N;
+    const int64_t m = (int64_t)blockIdx.x * warps + w;
+    const bool active = m < B;
+    const double* W1 = Z + m * 2 * (int64_t)N;
+    const double* W1p = W1 + N;
+    if (active)
+        for (int j = lane; j < N; j += 32) W1s[j] = W1[j];
+
+    for (int v = 0; v < t.n_vol; ++v) {
+        __syncthreads();
+        for (int j = threadIdx.x; j < N; j += blockDim.x) G[j] = t.gamma[(size_t)v * N + j];
+        __syncthreads();
+        if (!active) continue;
+        const VolDev vol = t.vols[v];
+        // Y2[j] = sum_{k<j} W1[k] Gamma[j-k]   (Gamma[0] = 0)
+        for (int j = lane; j < N; j += 32) {
+            double acc = 0.0;
+            for (int k = 0; k < j; ++k) acc = fma(W1s[k], G[j - k], acc);
+            X[j] = acc + (vol.a1 * W1s[j] + vol.a2 * W1p[j]);
+        }
+        __syncwarp();
+        for (int g = vol.vg_begin; g < vol.vg_end; ++g) {
+            const VGDev vg = t.vgs[g];
+            const double* comp = t.comp + (size_t)g * N;
+            double sv = 0.0, sw = 0.0;
+            for (int j = lane; j < vg.nsteps; j += 32) {
+                const double vj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * X[j - 1]) - comp[j - 1]);
+                sv += vj;
+                sw += sqrt(vj) * vg.sdt * W1s[j];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sv += __shfl_xor_sync(0xffffffffu, sv, o);
+                sw += __shfl_xor_sync(0xffffffffu, sw, o);
+            }
+            if (lane == 0) ivb[(size_t)g * B + m] = make_double2(vg.dt * sv, sw);
+        }
+        __syncwarp();
+    }
+}
+
+int path_fp64_warps(int N)
+{
+    const size_t budget = 200 * 1024;
+    size_t per = 16 * (size_t)N;
+    size_t w = (budget - 8 * (size_t)N) / per;
+    if (w > 8) w = 8;
+    if (w < 1) w = 1;
+    return (int)w;
+}
+
+size_t path_fp64_smem(int N, int warps) { return 8 * (size_t)N + (size_t)warps * 16 * N; }
+
+void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream)
+{
+    const int warps = path_fp64_warps(t.N);
+    const size_t smem = path_fp64_smem(t.N, warps);
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaFuncSetAttribute(k_path_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = smem;
+    }
+    const int64_t blocks = (B + warps - 1) / warps;
+    k_path_fp64<<<(unsigned)blocks, warps * 32, smem, (cudaStream_t)stream>>>(t, Z, B, (double2*)ivb);
+    count_launch();
+}
+
+// ------------------------------------------------------------ payoff sums
+constexpr int kOPB = 8;  // outputs per block
+
+// grid (nchunks, ceil(n_out / kOPB)), 256 threads; chunk c covers paths
+// [c G 256, (c+1) G 256) of the batch; part[(c * n_out + i) * 4 + {0,1,2,3}] =
+// (sum, comp, sum2, comp2).
+__global__ void __launch_bounds__(256) k_payoff_sums(Fp64Tables t, const double2* __restrict__ ivb, int64_t B,
+                                                     int64_t stride, int G, double* __restrict__ part)
+{
+    __shared__ double red[8][kOPB][2];
+    const int c = blockIdx.x;
+    const int o0 = blockIdx.y * kOPB;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double S = 0, CS = 0, S2 = 0, CS2 = 0;  // meaningful in threads q < kOPB
+    OutDev od[kOPB];
+#pragma unroll
+    for (int q = 0; q < kOPB; ++q) {
+        const int i = o0 + q;
+        od[q] = (i < t.n_out) ? t.outs[i] : OutDev{0.0, 1.0, -1, 0};
+    }
+    for (int sub = 0; sub < G; ++sub) {
+        const int64_t m = ((int64_t)c * G + sub) * 256 + threadIdx.x;
+#pragma unroll
+        for (int q = 0; q < kOPB; ++q) {
+            double x = 0.0;
+            if (m < B && od[q].vg >= 0) {
+                const double2 iv = ivb[(size_t)od[q].vg * stride + m];
+                x = rt_payoff(iv.x, iv.y, od[q].rho, od[q].K);
+            }
+            double x2 = x * x;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+                x2 += __shfl_xor_sync(0xffffffffu, x2, o);
+            }
+            if (lane == 0) { red[w][q][0] = x; red[w][q][1] = x2; }
+        }
+        __syncthreads();
+        if (threadIdx.x < kOPB) {
+            const int q = threadIdx.x;
+            double a = 0, a2 = 0;
+            for (int k = 0; k < 8; ++k) { a += red[k][q][0]; a2 += red[k][q][1]; }
+            neumaier_add(S, CS, a);
+            neumaier_add(S2, CS2, a2);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < kOPB && o0 + (int)threadIdx.x < t.n_out) {
+        double* p = part + ((size_t)c * t.n_out + o0 + threadIdx.x) * 4;
+        p[0] = S; p[1] = CS; p[2] = S2; p[3] = CS2;
+    }
+}
+
+void launch_payoff_sums(const Fp64Tables& t, const double* ivb, int64_t B, int64_t stride, int G, double* part,
+                        int nchunks, void* stream)
+{
+    dim3 grid(nchunks, (t.n_out + kOPB - 1) / kOPB);
+    k_payoff_sums<<<grid, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride, G, part);
+    count_launch();
+}
+
+// acc[i * 4 + {0..3}] += chunk sums, in chunk order
+__global__ void k_accumulate(const double* __restrict__ part, int nchunks, int n_out, double* __restrict__ acc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_out) return;
+    double S = acc[i * 4 + 0], C = acc[i * 4 + 1], S2 = acc[i * 4 + 2], C2 = acc[i * 4 + 3];
+    for (int c = 0; c < nchunks; ++c) {
+        const double* p = part + ((size_t)c * n_out + i) * 4;
+        neumaier_add(S, C, p[0]);
+        neumaier_add(S, C, p[1]);
+        neumaier_add(S2, C2, p[2]);
+        neumaier_add(S2, C2, p[3]);
+    }
+    acc[i * 4 + 0] = S; acc[i * 4 + 1] = C; acc[i * 4 + 2] = S2; acc[i * 4 + 3] = C2;
+}
+
+void launch_accumulate(const double* part, int nchunks, int n_out, double* acc, void* stream)
+{
+    k_accumulate<<<(n_out + 127) / 128, 128, 0, (cudaStream_t)stream>>>(part, nchunks, n_out, acc);
+    count_launch();
+}
+
+// ------------------------------------------------------------- IV (FP64)
+__device__ double bs_gen(double K, double T, double s, int put)
+{
+    const double sq = sqrt(T);
+    const double d1 = (log(1.0 / K) + 0.5 * s * s * T) / (s * sq);
+    const double d2 = d1 - s * sq;
+    return put ? (-phi_cdf(-d1) + phi_cdf(-d2) * K) : (phi_cdf(d1) - phi_cdf(d2) * K);
+}
+
+// Inverts on the out-of-the-money side (put-call parity for K < 1, as
+// rBergLib/BlackScholes.cpp:38-41 does): bracket by doubling, Newton steps on
+// log(price) safeguarded by bisection, to ~1e-15 relative.
+__device__ double implied_vol_call(double price, double K, double T)
+{
+    const int put = 1.0 > K;
+    const double target = put ? price - 1.0 + K : price;
+    const double upper = put ? K : 1.0;
+    if (!(target > 0.0) || !(target < upper) || !(T > 0.0)) return __longlong_as_double(0x7ff8000000000000ll);
+    double lo = 0.0, hi = 0.5;
+    for (int it = 0; it < 60; ++it) {
+        if (bs_gen(K, T, hi, put) >= target) break;
+        lo = hi;
+        hi *= 2.0;
+    }
+    const double lt = log(target);
+    double s = 0.5 * (lo + hi);
+    for (int it = 0; it < 200; ++it) {
+        const double p = bs_gen(K, T, s, put);
+        if (p > target) hi = s; else lo = s;
+        double sn;
+        if (p > 0.0) {
+            const double d1 = (log(1.0 / K) + 0.5 * s * s * T) / (s * sqrt(T));
+            const double vega = exp(-0.5 * d1 * d1) * 0.39894228040143267794 * sqrt(T);
+            sn = s - (log(p) - lt) * p / vega;
+        } else {
+            sn = 0.5 * (lo + hi);
+        }
+        if (!(sn > lo && sn < hi)) sn = 0.5 * (lo + hi);
+        if (fabs(sn - s) <= 1e-15 * s || hi - lo <= 1e-15 * hi) { s = sn; break; }
+        s = sn;
+    }
+    return s;
+}
+
+// res: [0,n) price, [n,2n) stat, [2n,3n) iv, [3n,4n) sum, [4n,5n) sum2
+__global__ void k_finalize(const double* __restrict__ acc, int n_out, int64_t M, const OutDev* __restrict__ outs,
+                           const double* __restrict__ Tv, int compute_iv, double* __restrict__ res)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_out) return;
+    const double S = acc[i * 4 + 0] + acc[i * 4 + 1];
+    const double S2 = acc[i * 4 + 2] + acc[i * 4 + 3];
+    // rBergLib/rBergomiMT.cpp:404-409
+    const double price = S * (1.0 / (double)M);
+    const double var = 1.0 * (S2 * (1.0 / (double)M)) + -1.0 * (price * price);
+    const double stat = sqrt(var) * (1.0 / sqrt((double)M));
+    res[i] = price;
+    res[n_out + i] = stat;
+    res[2 * n_out + i] = compute_iv ? implied_vol_call(price, outs[i].K, Tv[i]) : 0.0;
+    res[3 * n_out + i] = S;
+    res[4 * n_out + i] = S2;
+}
+
+void launch_finalize(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,
+                     int compute_iv, double* res, void* stream)
+{
+    k_finalize<<<(n_out + 127) / 128, 128, 0, (cudaStream_t)stream>>>(acc, n_out, M, outs, Tvals, compute_iv, res);
+    count_launch();
+}
+
+__global__ void k_implied_vol(int n, const double* price, const double* K, const double* T, double* iv)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) iv[i] = implied_vol_call(price[i], K[i], T[i]);
+}
+
+void launch_implied_vol(int n, const double* price, const double* K, const double* T, double* iv, void* stream)
+{
+    k_implied_vol<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(n, price, K, T, iv);
+    count_launch();
+}
+
+// ------------------------------------------------------------ quadrature
+__global__ void k_payoff_store(Fp64Tables t, const double2* __restrict__ ivb, int64_t B, int64_t stride,
+                               double* __restrict__ payoff)
+{
+    const int64_t total = B * t.n_out;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t m = idx / t.n_out;
+        const int i = (int)(idx - m * t.n_out);
+        const OutDev od = t.outs[i];
+        const double2 iv = ivb[(size_t)od.vg * stride + m];
+        payoff[idx] = rt_payoff(iv.x, iv.y, od.rho, od.K);
+    }
+}
+
+void launch_payoff_store(const Fp64Tables& t, const double* ivb, int64_t B, int64_t stride, double* payoff,
+                         void* stream)
+{
+    const int64_t total = B * t.n_out;
+    int64_t blocks = (total + 255) / 256;
+    if (blocks > (1 << 20)) blocks = 1 << 20;
+    k_payoff_store<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride, payoff);
+    count_launch();
+}
+
+}  // namespace rbg

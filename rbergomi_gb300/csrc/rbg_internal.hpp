@@ -1,0 +1,97 @@
+// rbg_internal.hpp -- types shared by the host planner, the launchers and the
+// kernels of librbergomi_gb300.  Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "rbergomi_gb300.h"
+
+namespace rbg {
+
+// One Volterra pass: a distinct H at which the reference's HTrigger fired.
+// X_j = Y2_j + a1 W1_j + a2 W1perp_j with Y2 = (W1 * Gamma_H)[0..N) is shared
+// by every variance group of this pass (rBergLib/rBergomiMT.cpp:83-109).
+struct VolGroup {
+    double H;
+    double c;       // sqrt(2H) * N^-H          (rBergomiMT.cpp:107-108)
+    double a1, a2;  // rhoH / s2H, sqrt(1 - rhoH^2) / s2H  (rBergomiMT.cpp:87-89)
+    int vg_begin, vg_end;  // its variance groups, contiguous after sorting
+};
+
+// One variance path: the state after the reference's H/T/eta trigger chain
+// (rBergomiMT.cpp:493-507).  WS_j = scale * X_j with scale = c * T_s^H_s;
+// v_0 = xi, v_j = xi exp(eta WS_{j-1} - comp[j-1]) with
+// comp[j] = 0.5 eta eta (j dt)^{2 H_v} (rBergomiMT.cpp:73-80).
+struct VGroup {
+    int vol;
+    double Hs, Ts;  // H and T at the last H-or-T trigger (scaleWtilde)
+    double Hv, eta; // H and eta at the last H-or-T-or-eta trigger (updateV)
+    double scale, dt, sdt;
+    int nsteps;
+};
+
+struct OutMap {
+    int vg;
+    double rho, K, T;
+};
+
+struct Plan {
+    double xi = 0;
+    int N = 0;
+    std::vector<VolGroup> vols;
+    std::vector<VGroup> vgs;
+    std::vector<OutMap> outs;
+    std::vector<double> gamma;  // [n_vol][N] (rBergomiMT.cpp:143-149)
+    std::vector<double> comp;   // [n_vg][N], comp[N-1] unused
+};
+
+// Builds the plan with the reference's ParamTot trigger semantics
+// (rBergLib/ParamTot.h:28-43, eps 1e-10 at ParamTot.cpp:27).  Volterra passes
+// are deduplicated by exact H value, variance groups by exact tuple.
+// Returns false and sets err on invalid input.
+bool build_plan(const rbg_params& p, Plan& plan, std::string& err);
+
+// ---- device-side views -------------------------------------------------
+struct VolDev {
+    double a1, a2;
+    int vg_begin, vg_end;
+};
+struct VGDev {
+    double scale, eta, dt, sdt, xi;
+    int nsteps, vol;
+};
+struct OutDev {
+    double rho, K;
+    int vg, pad;
+};
+
+// ---- launchers (rbg_fp64.cu) -------------------------------------------
+struct Fp64Tables {
+    const VolDev* vols;
+    const VGDev* vgs;
+    const OutDev* outs;
+    const double* gamma;
+    const double* comp;
+    int n_vol, n_vg, n_out, N;
+    double xi;
+};
+
+void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream);
+int path_fp64_warps(int N);
+size_t path_fp64_smem(int N, int warps);
+void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream);
+void launch_payoff_sums(const Fp64Tables& t, const double* ivb, int64_t B, int64_t ivb_stride, int G,
+                        double* part, int nchunks, void* stream);
+void launch_accumulate(const double* part, int nchunks, int n_out, double* acc, void* stream);
+void launch_finalize(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,
+                     int compute_iv, double* res, void* stream);
+void launch_payoff_store(const Fp64Tables& t, const double* ivb, int64_t B, int64_t ivb_stride, double* payoff,
+                         void* stream);
+void launch_implied_vol(int n, const double* price, const double* K, const double* T, double* iv, void* stream);
+
+// Kernel-launch counter shared by all launchers.
+void count_launch(int n = 1);
+
+}  // namespace rbg

@@ -1,0 +1,103 @@
+"""C-ABI library checks that need no GPU: exports, host planner, exit codes."""
+import ctypes as C
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "rbergomi_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def R():
+    import rbergomi_gb300 as R
+    if not os.path.exists(R.LIB_PATH):
+        from rbergomi_gb300 import build
+        build.build()
+    R.lib()
+    return R
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:void|int|const char\s*\*|uint64_t)\s*\**\s*(\w+)\s*\(", src, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol(R):
+    names = declared_functions()
+    assert "computeIVRT_tensor" in names and "computeIVRT_tensor_quadrature" in names
+    L = C.CDLL(R.LIB_PATH)
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) <= set(R.EXPORTS) | set(names)
+
+
+def oracle_groups(H, eta, rho, T, K, N):
+    """The reference trigger chain (rBergLib/rBergomiMT.cpp:490-507) replayed
+    in Python: the (H_vol, H_s, T_s, H_v, eta) state each output sees."""
+    O = len(T)
+    eps = 1e-10
+    states = []
+    vol = Hs = Ts = None
+    for i in range(len(H) * O):
+        h, e, t = H[i // O], eta[i // O], T[i % O]
+        ph = H[(i - 1) // O] if i else None
+        upd = i == 0 or abs(h - ph) > eps
+        if upd:
+            vol = h
+        upd = upd or abs(t - T[(i - 1) % O]) > eps
+        if upd:
+            Hs, Ts = h, t
+        upd = upd or abs(e - eta[(i - 1) // O]) > eps
+        if upd:
+            cur = (vol, Hs, Ts, h, e)
+        states.append(cur)
+    return states
+
+
+@pytest.mark.parametrize("case", [
+    ([0.1], [1.5], [-0.7], [1.0] * 3, [0.9, 1.0, 1.1]),
+    ([0.05, 0.1, 0.1, 0.3, 0.1], [1.0, 1.5, 1.5, 2.5, 1.5], [-0.95, -0.7, -0.5, -0.7, -0.3],
+     [0.25, 0.25, 0.5, 1.0, 1.0, 2.0], [0.9, 1.1, 1.0, 0.8, 1.3, 2.0]),
+    # near-duplicates within the 1e-10 trigger tolerance keep the earlier state
+    ([0.1, 0.1 + 5e-11, 0.2], [1.0, 1.0 + 5e-11, 1.0], [-0.5, -0.5, -0.5], [1.0, 1.0 + 5e-11], [1.0, 1.1]),
+])
+def test_plan_matches_trigger_chain(R, case):
+    H, eta, rho, T, K = case
+    nv, ng, groups = R.plan_info(0.04, H, eta, rho, T, K, 64)
+    states = oracle_groups(H, eta, rho, T, K, 64)
+    # outputs share a variance group iff the reference reaches them in the same state
+    for a in range(len(states)):
+        for b in range(len(states)):
+            assert (groups[a] == groups[b]) == (states[a] == states[b])
+    assert nv == len({s[0] for s in states})
+    assert ng == len(set(states))
+
+
+def test_plan_rejects_bad_input(R):
+    with pytest.raises(R.RbgError):
+        R.plan_info(0.04, [0.0], [1.0], [-0.5], [1.0], [1.0], 64)
+    with pytest.raises(R.RbgError):
+        R.plan_info(0.04, [0.1], [1.0], [-0.5], [1.0], [1.0], 0)
+
+
+def _run(code):
+    return subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=120)
+
+
+def test_dropin_exit_codes():
+    """Size mismatch -> exit 17, num_threads < 1 -> exit 21, before any GPU work
+    (rBergLib/cinterface.cpp:54-59, 76-81)."""
+    pre = ("import ctypes as C, numpy as np, rbergomi_gb300 as R\n"
+           "L=R.lib(); d=lambda n: (C.c_double*n)(); s=(C.c_uint64*1)(1)\n")
+    call = ("L.computeIVRT_tensor(0.04, d(1), d(1), d(1), 1, d(2), d(2), 2, 8, 16, s, 1, {nt}, "
+            "d(2), d(2), d(2), d(2), d(2), d(2), d(2), d(2), {out})\n")
+    r = _run(pre + call.format(nt=1, out=3))
+    assert r.returncode == 17 and "wrong size" in r.stderr
+    r = _run(pre + call.format(nt=0, out=2))
+    assert r.returncode == 21 and "positive integer" in r.stderr
