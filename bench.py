@@ -1,0 +1,324 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 rough Bergomi RT pricer.
+
+Default workload (the configuration the headline metric is quoted on):
+mixed precision, H = 0.1, eta = 1.9, rho = -0.9, xi = 0.235^2, T = 1,
+21 strikes on [0.6, 1.4], N = 512 steps, M = 2^22 paths, Philox seed 11.
+One step = one full pricing call over all M paths.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints ONE JSON line.  `value` is path-steps/s (path x step x distinct H) of
+the mixed form timed with CUDA events on the launching stream, L2 flushed
+(256 MiB write) before every timed step.  `e2e` is the same metric through
+the drop-in C-ABI call computeIVRT_tensor with host buffers.  The FP64 form
+is timed on the same workload, and the mixed prices are compared with the
+FP64 form on identical normals.  `--impl reference` times the CPU oracle
+(the C restatement of the reference's OpenMP path) on a bounded sample of
+the same workload on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "mixed-n512-m4m-21k": dict(xi=0.235 ** 2, H=[0.1], eta=[1.9], rho=[-0.9], T=[1.0] * 21,
+                               K=[round(float(k), 10) for k in np.linspace(0.6, 1.4, 21)], N=512, M=1 << 22,
+                               seed=11),
+    "fp64-n100-m64k-5k": dict(xi=0.235 ** 2, H=[0.07], eta=[1.9], rho=[-0.9], T=[1.0] * 5,
+                              K=[0.8, 0.9, 1.0, 1.1, 1.2], N=100, M=1 << 16, seed=42),
+}
+DEFAULT = "mixed-n512-m4m-21k"
+METRIC = "path-steps/s"
+
+
+def path_steps(w) -> float:
+    return float(w["M"]) * w["N"] * len(set(w["H"]))
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# --------------------------------------------------------------- CPU arm
+def cpu_sample(w, paths: int, threads: int):
+    """Times the oracle's C restatement of the reference RT path (OpenMP over
+    paths, FP64, direct causal Volterra sum) on `paths` paths of workload w."""
+    from oracle import oracle as O
+    O.lib()
+    t0 = time.perf_counter()
+    O.price_rt_philox(w["xi"], w["H"], w["eta"], w["rho"], w["T"], w["K"], w["N"], paths, w["seed"], threads)
+    dt = time.perf_counter() - t0
+    return paths * w["N"] * len(set(w["H"])) / dt, dt
+
+
+def run_reference(args, w):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.lib()
+    threads = O.max_threads()
+    paths = args.cpu_paths
+    for _ in range(args.warmup):
+        cpu_sample(w, paths, threads)
+    vals = []
+    t_all = 0.0
+    for _ in range(args.steps):
+        v, dt = cpu_sample(w, paths, threads)
+        vals.append(v)
+        t_all += dt
+    value = args.steps * paths * w["N"] * len(set(w["H"])) / t_all
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "path-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "N": w["N"], "M_sample_per_step": paths, "strikes": len(w["K"]),
+                   "note": "CPU oracle: C restatement of rBergLib's RT path (direct causal sum in place of FFTW)"},
+        "cpu_baseline": {"value": value, "unit": "path-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{paths} paths x N={w['N']} per step"},
+        "e2e": {"value": value, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# --------------------------------------------------------------- GPU arm
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[4:8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        active = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        loaded = [r for r in rows if r[2] > 200.0] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": active, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel: str, w):
+    """DRAM bytes per launch from the committed ncu summary, scaled by paths."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            d = json.load(f)[kernel]
+        return d["bytes"] * (w["M"] / d["paths"]) if d.get("scale_with_paths", True) else d["bytes"]
+    except (OSError, KeyError, ValueError, TypeError):
+        return None
+
+
+def run_gpu(args, w):
+    import torch
+
+    import rbergomi_gb300 as R
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    R.lib()
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    prec = R.MIXED if args.precision == "mixed" else R.FP64
+    # weak scaling: every rank prices its own M paths (disjoint Philox paths)
+    offset = rank * w["M"]
+    kw = dict(seed=w["seed"], precision=prec, split=args.split, path_offset=offset, stream=sptr)
+    flush = torch.empty((256 << 20) // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        return R.price_rt(w["xi"], w["H"], w["eta"], w["rho"], w["T"], w["K"], w["N"], w["M"], **kw)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    R.profile_reset()
+    R.profile_enable(True)
+    n0 = R.launch_count()
+    times = []
+    with ClockSampler(local) as clk:
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            price, stat, iv = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        if ws > 1:
+            torch.distributed.barrier()
+    R.profile_enable(False)
+    launches = R.launch_count() - n0
+    total_ms = float(sum(times))
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = ws * path_steps(w) / (ms_step / 1e3)
+    if rank != 0:
+        return
+    stage = R.STAGE_MIXED if prec == R.MIXED else R.STAGE_PATH_FP64
+    kms, kn = R.profile_read(stage)
+    avg_kernel_ms = kms / max(kn, 1)
+    bf16_peak, hbm_peak, peak_src = peaks()
+    algo_flops = w["M"] * w["N"] * (w["N"] - 1) * len(set(w["H"])) / max(1, kn // args.steps)
+    achieved_tf = algo_flops / (avg_kernel_ms / 1e3) / 1e12
+    Np = (w["N"] + 31) // 32 * 32
+    nc = Np // 32
+    exec_flops = 6.0 * 32 * 32 * nc * (nc + 1) / 2 * w["M"] / max(1, kn // args.steps)
+    roof = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": achieved_tf / bf16_peak, "traffic": traffic_per_launch("k_mixed_gemm", w),
+            "kernel": "k_mixed_gemm" if prec == R.MIXED else "k_path_fp64",
+            "kernel_ms": avg_kernel_ms, "peak_source": f"{peak_src} bf16 burst",
+            "algorithmic_flops_per_launch": algo_flops,
+            "executed_tensor_tflops": exec_flops / (avg_kernel_ms / 1e3) / 1e12 if prec == R.MIXED else None}
+
+    # plain FP64 form on the same workload, and the error vs FP64 on identical normals
+    extra = {}
+    if prec == R.MIXED and not args.skip_fp64:
+        kf = dict(seed=w["seed"], path_offset=offset, stream=sptr)
+        R.price_rt(w["xi"], w["H"], w["eta"], w["rho"], w["T"], w["K"], w["N"], min(w["M"], 1 << 16), **kf)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        R.price_rt(w["xi"], w["H"], w["eta"], w["rho"], w["T"], w["K"], w["N"], w["M"], **kf)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fp64_ms = e0.elapsed_time(e1)
+        fp, fs, _ = R.price_rt(w["xi"], w["H"], w["eta"], w["rho"], w["T"], w["K"], w["N"], w["M"],
+                               normals=R.NORMALS_F32, **kf)
+        err = np.abs(price - fp)
+        extra = {"fp64_value": path_steps(w) / (fp64_ms / 1e3), "fp64_ms_per_step": fp64_ms,
+                 "speedup_vs_fp64": (path_steps(w) / (ms_step / 1e3)) / (path_steps(w) / (fp64_ms / 1e3)),
+                 "max_rel_err_vs_fp64": float(np.max(err / fp)),
+                 "max_err_over_se": float(np.max(err / fs)),
+                 "prices": [float(x) for x in price], "stat": [float(x) for x in stat]}
+
+    # e2e through the drop-in C ABI with host buffers
+    os.environ["RBG_PRECISION"] = "mixed" if prec == R.MIXED else "fp64"
+    seed_words = [w["seed"]]
+    for _ in range(max(1, args.warmup // 2)):
+        R.computeIVRT_tensor(w["xi"], w["H"], w["eta"], w["rho"], w["T"], w["K"], w["N"], w["M"], seed_words)
+    t_e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        R.computeIVRT_tensor(w["xi"], w["H"], w["eta"], w["rho"], w["T"], w["K"], w["N"], w["M"], seed_words)
+        t_e2e.append(time.perf_counter() - t0)
+    h2d, d2h = R.last_transfer_bytes()
+    e2e = {"value": path_steps(w) / statistics.mean(t_e2e), "unit": "path-steps/s",
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "ms_per_step": 1e3 * statistics.mean(t_e2e), "api": "computeIVRT_tensor (C ABI, host buffers)"}
+
+    cpu = None
+    if not args.skip_cpu:
+        from oracle import oracle as O
+        thr = O.max_threads()
+        v, dt = cpu_sample(w, args.cpu_paths, thr)
+        cpu = {"value": v, "unit": "path-steps/s", "cores": thr, "kind": "port",
+               "sample": f"{args.cpu_paths} paths of this workload, FP64 C restatement, {dt:.1f} s wall"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "path-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": ("bf16x3" if args.split == 0 else "f16x3") + "+f32+f64" if prec == R.MIXED else "f64",
+        "data": "synthetic (Philox4x32-10 normals generated on device)",
+        "config": {"workload": args.workload, "N": w["N"], "M": w["M"], "strikes": len(w["K"]),
+                   "H": w["H"], "eta": w["eta"], "rho": w["rho"], "xi": w["xi"], "T": w["T"][0],
+                   "seed": w["seed"], "precision": args.precision, "l2": "flushed (256 MiB write) before each step",
+                   "prices_per_step": len(w["H"]) * len(w["K"])},
+        "prices_per_s": ws * len(w["H"]) * len(w["K"]) / (ms_step / 1e3),
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(), "gpu_launches": launches,
+    }
+    line.update(extra)
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
+    ap.add_argument("--split", type=int, default=0, help="0 = BF16x3, 1 = FP16x3")
+    ap.add_argument("--cpu-paths", type=int, default=1 << 17)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.precision is None:
+        args.precision = "mixed" if args.workload.startswith("mixed") else "fp64"
+    if args.impl == "reference":
+        run_reference(args, w)
+    else:
+        run_gpu(args, w)
+
+
+if __name__ == "__main__":
+    main()

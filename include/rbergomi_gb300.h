@@ -154,6 +154,25 @@ int rbg_release(void);
  * (length par_size*op_size, may be NULL) receives each output's group. */
 int rbg_plan_info(const rbg_params* p, int* n_vol, int* n_vgroups, int* n_out, int* vgroup_of_output);
 
+/* Stage timing: when enabled, CUDA events bracket each stage on the stream
+ * that launches it (stage 0 normals, 1 FP64 path pass, 2 mixed tcgen05 path
+ * kernel, 3 payoff sums, 4 chunk merge); rbg_profile_read returns the summed
+ * milliseconds and kernel launches since the last reset. */
+void rbg_profile_enable(int on);
+void rbg_profile_reset(void);
+int rbg_profile_read(int stage, double* total_ms, uint64_t* launches);
+
+/* Host<->device bytes copied by this thread's last rbg_price_rt* call. */
+void rbg_last_transfer_bytes(uint64_t* h2d, uint64_t* d2h);
+
+/* Diagnostic run of the mixed-form path kernel on at most 2^20 paths with
+ * the same arguments as rbg_price_rt: copies out the FP32 normals it drew
+ * (normals: M * 2 * Np floats, Np = N rounded up to 32, [path][W1|W1perp][step]),
+ * its X = Y2 + a1 W1 + a2 W1perp per step (x: M * Np) and its (Ivdt, IsvdW)
+ * per variance group and path (ivb: 2 * n_vgroups * M, [group][path][2]).
+ * Any output pointer may be NULL. */
+int rbg_debug_mixed_paths(const rbg_params* p, const rbg_options* o, float* normals, float* x, float* ivb);
+
 #ifdef __cplusplus
 }
 #endif

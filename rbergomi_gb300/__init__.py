@@ -50,8 +50,11 @@ _lib = None
 EXPORTS = [
     "computeIVRT_tensor", "computeIVRT_tensor_quadrature", "rbg_default_options", "rbg_price_rt",
     "rbg_price_rt_sums", "rbg_payoffs_rt", "rbg_generate_normals", "rbg_implied_vol", "rbg_last_error",
-    "rbg_launch_count", "rbg_synchronize", "rbg_release", "rbg_plan_info",
+    "rbg_launch_count", "rbg_synchronize", "rbg_release", "rbg_plan_info", "rbg_profile_enable",
+    "rbg_profile_reset", "rbg_profile_read", "rbg_last_transfer_bytes", "rbg_debug_mixed_paths",
 ]
+
+STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4
 
 
 def lib():
@@ -88,6 +91,16 @@ def lib():
         L.rbg_plan_info.argtypes = [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                     C.POINTER(C.c_int)]
         L.rbg_plan_info.restype = C.c_int
+        L.rbg_profile_enable.argtypes = [C.c_int]
+        L.rbg_profile_enable.restype = None
+        L.rbg_profile_reset.restype = None
+        L.rbg_profile_read.argtypes = [C.c_int, _dp, C.POINTER(C.c_uint64)]
+        L.rbg_profile_read.restype = C.c_int
+        L.rbg_last_transfer_bytes.argtypes = [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.rbg_last_transfer_bytes.restype = None
+        _fp = C.POINTER(C.c_float)
+        L.rbg_debug_mixed_paths.argtypes = [P, O, _fp, _fp, _fp]
+        L.rbg_debug_mixed_paths.restype = C.c_int
         _lib = L
     return _lib
 
@@ -247,3 +260,41 @@ def synchronize() -> None:
 
 def release() -> None:
     _check(lib().rbg_release())
+
+
+def profile_enable(on=True) -> None:
+    lib().rbg_profile_enable(1 if on else 0)
+
+
+def profile_reset() -> None:
+    lib().rbg_profile_reset()
+
+
+def profile_read(stage: int):
+    """(total milliseconds, kernel launches) recorded for a stage."""
+    ms, n = C.c_double(), C.c_uint64()
+    _check(lib().rbg_profile_read(int(stage), C.byref(ms), C.byref(n)))
+    return ms.value, int(n.value)
+
+
+def last_transfer_bytes():
+    """(host->device, device->host) bytes of this thread's last pricing call."""
+    a, b = C.c_uint64(), C.c_uint64()
+    lib().rbg_last_transfer_bytes(C.byref(a), C.byref(b))
+    return int(a.value), int(b.value)
+
+
+def debug_mixed_paths(xi, H, eta, rho, T, K, N, M, **opts):
+    """Diagnostic run of the mixed path kernel: (normals [M, 2, Np],
+    X [M, Np], ivb [n_groups, M, 2]) as float32, Np = N rounded up to 32."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    o = options(precision=MIXED, **opts)
+    _, ng, _ = plan_info(xi, H, eta, rho, T, K, N, M)
+    Np = (int(N) + 31) // 32 * 32
+    w = np.empty((M, 2, Np), np.float32)
+    x = np.empty((M, Np), np.float32)
+    iv = np.empty((ng, M, 2), np.float32)
+    fp = C.POINTER(C.c_float)
+    _check(lib().rbg_debug_mixed_paths(C.byref(p.s), C.byref(o), w.ctypes.data_as(fp), x.ctypes.data_as(fp),
+                                       iv.ctypes.data_as(fp)))
+    return w, x, iv

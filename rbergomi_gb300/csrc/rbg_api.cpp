@@ -19,6 +19,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "rbg_internal.hpp"
@@ -30,6 +31,63 @@ static std::atomic<uint64_t> g_launches{0};
 void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
 static thread_local std::string g_err;
+// ------------------------------------------------------------- profiling
+// When enabled, CUDA events are recorded on the launching stream around each
+// stage; durations are folded in after the call's final synchronisation.
+enum { kStageNormals = 0, kStagePathFp64 = 1, kStageMixed = 2, kStagePayoff = 3, kStageReduce = 4, kStages = 5 };
+struct Prof {
+    std::mutex mu;
+    bool on = false;
+    double ms[kStages] = {0};
+    uint64_t n[kStages] = {0};
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t, int>> pending;
+};
+static Prof g_prof;
+
+struct ProfScope {
+    int stage, count;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(int stage_, cudaStream_t st_, int count_ = 1) : stage(stage_), count(count_), st(st_)
+    {
+        std::lock_guard<std::mutex> lk(g_prof.mu);
+        if (!g_prof.on) return;
+        for (cudaEvent_t* e : {&a, &b}) {
+            if (!g_prof.pool.empty()) { *e = g_prof.pool.back(); g_prof.pool.pop_back(); }
+            else cudaEventCreate(e);
+        }
+        cudaEventRecord(a, st);
+    }
+    ~ProfScope()
+    {
+        if (!a) return;
+        cudaEventRecord(b, st);
+        std::lock_guard<std::mutex> lk(g_prof.mu);
+        g_prof.pending.emplace_back(stage, a, b, count);
+    }
+};
+
+// called after the stream that carried the pending events has synchronised
+static void prof_collect()
+{
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    for (auto& t : g_prof.pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, std::get<1>(t), std::get<2>(t)) == cudaSuccess) {
+            g_prof.ms[std::get<0>(t)] += ms;
+            g_prof.n[std::get<0>(t)] += (uint64_t)std::get<3>(t);
+        }
+        cudaGetLastError();
+        g_prof.pool.push_back(std::get<1>(t));
+        g_prof.pool.push_back(std::get<2>(t));
+    }
+    g_prof.pending.clear();
+}
+
+// bytes moved between host and device by the last completed call
+static thread_local uint64_t g_h2d = 0, g_d2h = 0;
+
 
 static int fail(int code, const std::string& msg)
 {
@@ -148,6 +206,7 @@ static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts
     int rc = ensure(c.tabs, total, "tables");
     if (rc) return rc;
     RBG_CUDA(cudaMemcpyAsync(c.tabs.p, host.data(), total, cudaMemcpyHostToDevice, st));
+    g_h2d += total;
     // the host staging vector dies at return: make the copy complete first
     RBG_CUDA(cudaStreamSynchronize(st));
     unsigned char* base = (unsigned char*)c.tabs.p;
@@ -196,17 +255,31 @@ static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M,
     RBG_CUDA(cudaMemsetAsync(c.acc.p, 0, sizeof(double) * 4 * no, st));
     for (int64_t m0 = 0; m0 < M; m0 += B) {
         const int64_t b = std::min(B, M - m0);
-        launch_normals(o.seed, o.path_offset + m0, b, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st);
-        launch_path_fp64(ts.t, c.z.as<double>(), b, c.ivb.as<double>(), st);
+        {
+            ProfScope ps(kStageNormals, st);
+            launch_normals(o.seed, o.path_offset + m0, b, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st);
+        }
+        {
+            ProfScope ps(kStagePathFp64, st);
+            launch_path_fp64(ts.t, c.z.as<double>(), b, c.ivb.as<double>(), st);
+        }
         const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
-        launch_payoff_sums(ts.t, c.ivb.as<double>(), b, b, G, c.part.as<double>(), nchunks, st);
-        launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+        {
+            ProfScope ps(kStagePayoff, st);
+            launch_payoff_sums(ts.t, c.ivb.as<double>(), b, b, G, c.part.as<double>(), nchunks, st);
+        }
+        {
+            ProfScope ps(kStageReduce, st);
+            launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+        }
         RBG_CUDA(cudaGetLastError());
     }
     launch_finalize(c.acc.as<double>(), no, M, ts.t.outs, ts.Tvals, o.compute_iv, c.res.as<double>(), st);
     RBG_CUDA(cudaGetLastError());
     RBG_CUDA(cudaMemcpyAsync(host_res, c.res.p, sizeof(double) * 5 * no, cudaMemcpyDeviceToHost, st));
     RBG_CUDA(cudaStreamSynchronize(st));
+    g_d2h += sizeof(double) * 5 * no;
+    prof_collect();
     return RBG_OK;
 }
 
@@ -219,10 +292,10 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
     int rc = upload_tables(c, plan, st, ts);
     if (rc) return rc;
     const int no = (int)plan.outs.size();
-    MixedJob job{};
+    MixedJob job;
     if ((rc = mixed_prepare(plan, o, M, job, g_err))) return rc;
     const int64_t B = job.batch;
-    if ((rc = ensure(c.ivb, sizeof(double) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    if ((rc = ensure(c.ivb, sizeof(float) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
     if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
     const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
     const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
@@ -230,27 +303,40 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
     if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
     if ((rc = ensure(c.res, sizeof(double) * 5 * no, "results"))) return rc;
     if ((rc = mixed_upload(job, c.mixed_ws.p, st, g_err))) return rc;
+    g_h2d += job.host_ws.size();
     RBG_CUDA(cudaMemsetAsync(c.acc.p, 0, sizeof(double) * 4 * no, st));
     for (int64_t m0 = 0; m0 < M; m0 += B) {
         const int64_t b = std::min(B, M - m0);
-        if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, c.ivb.as<double>(), st, g_err)))
-            return rc;
+        {
+            ProfScope ps(kStageMixed, st, (int)job.launches.size());
+            if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, c.ivb.p, st, g_err))) return rc;
+        }
         const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
-        launch_payoff_sums(ts.t, c.ivb.as<double>(), b, b, G, c.part.as<double>(), nchunks, st);
-        launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+        {
+            ProfScope ps(kStagePayoff, st);
+            launch_payoff_sums_f32(ts.t.outs, no, c.ivb.p, b, G, c.part.as<double>(), nchunks, st);
+        }
+        {
+            ProfScope ps(kStageReduce, st);
+            launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+        }
         RBG_CUDA(cudaGetLastError());
     }
     if ((rc = mixed_check(job, c.mixed_ws.p, st, g_err))) return rc;
+    g_d2h += 4;
     launch_finalize(c.acc.as<double>(), no, M, ts.t.outs, ts.Tvals, o.compute_iv, c.res.as<double>(), st);
     RBG_CUDA(cudaGetLastError());
     RBG_CUDA(cudaMemcpyAsync(host_res, c.res.p, sizeof(double) * 5 * no, cudaMemcpyDeviceToHost, st));
     RBG_CUDA(cudaStreamSynchronize(st));
+    g_d2h += sizeof(double) * 5 * no;
+    prof_collect();
     return RBG_OK;
 }
 
 static int price_any(const rbg_params* p, const rbg_options* o, std::vector<double>& res)
 {
     if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
+    g_h2d = g_d2h = 0;
     Plan plan;
     std::string err;
     if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
@@ -424,8 +510,74 @@ int rbg_release(void)
     std::lock_guard<std::mutex> lk(c->mu);
     RBG_CUDA(cudaStreamSynchronize(c->stream));
     for (DevBuf* b : {&c->z, &c->ivb, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws}) b->release();
-    mixed_release_cache();
     return RBG_OK;
+}
+
+int rbg_debug_mixed_paths(const rbg_params* p, const rbg_options* o, float* normals, float* x, float* ivb)
+{
+    if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
+    if (p->M > (1 << 20)) return fail(RBG_ERR_ARG, "diagnostic runs are limited to 2^20 paths");
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
+    MixedJob job;
+    if ((rc = mixed_prepare(plan, *o, p->M, job, g_err))) return rc;
+    if (job.batch < p->M) return fail(RBG_ERR_ARG, "diagnostic run does not fit one batch");
+    const int Np = (plan.N + 31) / 32 * 32;
+    const size_t M = (size_t)p->M, nvg = plan.vgs.size();
+    if ((rc = ensure(c->mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
+    DevBuf dbg;
+    if (dbg.ensure(sizeof(float) * (M * 2 * Np + M * Np + 2 * nvg * M))) return fail(RBG_ERR_NOMEM, "debug buffers");
+    float* dw = dbg.as<float>();
+    float* dx = dw + M * 2 * Np;
+    float* div = dx + M * Np;
+    if ((rc = mixed_upload(job, c->mixed_ws.p, st, g_err))) { dbg.release(); return rc; }
+    rc = mixed_launch(job, c->mixed_ws.p, o->seed, o->path_offset, p->M, div, st, g_err, dw, dx);
+    if (!rc) rc = mixed_check(job, c->mixed_ws.p, st, g_err);
+    if (!rc) {
+        cudaError_t e = cudaSuccess;
+        if (normals) e = cudaMemcpy(normals, dw, sizeof(float) * M * 2 * Np, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && x) e = cudaMemcpy(x, dx, sizeof(float) * M * Np, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && ivb) e = cudaMemcpy(ivb, div, sizeof(float) * 2 * nvg * M, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            rc = fail(RBG_ERR_CUDA, std::string("debug copy: ") + cudaGetErrorString(e));
+        }
+    }
+    dbg.release();
+    return rc;
+}
+
+void rbg_profile_enable(int on)
+{
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    g_prof.on = on != 0;
+}
+
+void rbg_profile_reset(void)
+{
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    for (int i = 0; i < kStages; ++i) { g_prof.ms[i] = 0; g_prof.n[i] = 0; }
+}
+
+int rbg_profile_read(int stage, double* total_ms, uint64_t* launches)
+{
+    if (stage < 0 || stage >= kStages) return fail(RBG_ERR_ARG, "bad stage");
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    if (total_ms) *total_ms = g_prof.ms[stage];
+    if (launches) *launches = g_prof.n[stage];
+    return RBG_OK;
+}
+
+void rbg_last_transfer_bytes(uint64_t* h2d, uint64_t* d2h)
+{
+    if (h2d) *h2d = g_h2d;
+    if (d2h) *d2h = g_d2h;
 }
 
 int rbg_plan_info(const rbg_params* p, int* n_vol, int* n_vgroups, int* n_out, int* vgroup_of_output)

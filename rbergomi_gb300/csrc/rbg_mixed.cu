@@ -1,19 +1,767 @@
-// rbg_mixed.cu -- mixed-precision form (placeholder until the tcgen05 kernel lands).
+// rbg_mixed.cu -- the mixed-precision form of the RT pricer on sm_103a.
+//
+// One persistent kernel per Volterra pass (distinct H) fuses
+//   Philox4x32-10 normals (FP32 Box-Muller) for W1 and W1perp,
+//   the hybrid-scheme convolution Y2[p][j] = sum_{k<j} W1[p][k] Gamma[j-k]
+//     as a block-lower-triangular Toeplitz GEMM on the tcgen05 tensor cores
+//     (BF16x3 or FP16x3 split products, FP32 accumulation in TMEM),
+//   the variance path v and the Romano-Touzi integrals
+//     Ivdt = dt sum v, IsvdW = sum sqrt(v) sdt W1   (FP32, per variance group)
+// and writes one float2 per (variance group, path).  A second kernel prices
+// every (rho, K) output in FP32 and reduces across paths in FP64.
+//
+// Arithmetic restated from rBergLib/rBergomiMT.cpp:73-109 (updateV,
+// updateWtilde), :163-167 (scaleWtilde), :427-436 (intVdt, intRootVdW) and
+// :598-602 (the conditional BS payoff).
+//
+// Toeplitz structure.  Time steps are cut into K-chunks of 32.  Chunk c
+// multiplies the A tile W1[:, 32c, 32c+32) into output columns [32c, Np):
+//   D[:, 32c + j'] += sum_{k'<32} A_c[:, k'] * S[j'][k'],  S[j'][k'] = Gamma[j' - k'],
+// and S does not depend on c.  So one 32 x Np strip S (hi and lo halves,
+// 64 KB at N = 512) stays resident in shared memory for the whole kernel,
+// loaded once by a bulk async copy; only A tiles stream.  After chunk c's
+// MMAs, columns [32c, 32c+32) are final and the epilogue reads them.
+//
+// Warp roles (416 threads, one CTA per SM, persistent over 128-path tiles):
+//   warps 0-7   producers: Philox -> FP32 normals; W1 split into hi/lo
+//               16-bit A tiles (SW64 K-major layout); FP32 W1, W1perp kept
+//               for the epilogue
+//   warps 8-11  epilogue: tcgen05.ld of 32 accumulator columns per chunk,
+//               X = Y2 + a1 W1 + a2 W1perp, v and the two integrals
+//   warp 12     TMEM allocation and the single-thread tcgen05.mma issuer
+// Every mbarrier wait is bounded (%globaltimer); on expiry the kernel records
+// an error word, drains its MMAs, frees TMEM and returns.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "rbg_device.cuh"
 #include "rbg_mixed.hpp"
 
 namespace rbg {
 
-int mixed_prepare(const Plan&, const rbg_options&, int64_t, MixedJob&, std::string& err)
+constexpr int kTileM = 128;
+constexpr int kChunk = 32;
+constexpr int kMaxG = kMixedMaxGroups;
+constexpr int kProdWarps = 8;
+constexpr int kEpiWarps = 4;
+constexpr int kEpiWarp0 = kProdWarps;               // warps 8..11: TMEM lane quadrants 0..3
+constexpr int kMmaWarp = kProdWarps + kEpiWarps;    // warp 12
+constexpr int kThreads = (kMmaWarp + 1) * 32;       // 416
+constexpr int kMaxNp = 512;                         // TMEM: 128 lanes x 512 FP32 columns
+constexpr uint64_t kWaitNs = 2000000000ull;         // 2 s per wait
+
+// shared-memory layout (offsets from a 1024-aligned base):
+//   [strip hi | strip lo]            2 * Np * 64 B, SW64 K-major
+//   A tiles, per stage [hi | lo]     16 KB per stage (1024-aligned)
+//   FP32 tiles, per stage            w1 [32][128], w1perp [32][128], w1next [128]
+//   per-thread group sums            kMaxG * 2 * 128 floats
+//   mbarriers + TMEM address
+constexpr int kTileBytes = kTileM * kChunk * 2;                          // one 16-bit 128 x 32 tile, 8 KB
+constexpr int kStageA = 2 * kTileBytes;                                  // hi + lo
+constexpr int kStageF = 2 * kChunk * kTileM * 4 + kTileM * 4;            // w1, w1perp, w1next
+
+struct SmemLayout {
+    int strip, a0, f0, stages, acc, bars, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int Np, int stages)
 {
-    err = "mixed precision form not built yet";
-    return RBG_ERR_UNSUPPORTED;
+    SmemLayout L;
+    L.strip = 0;
+    L.a0 = ((2 * Np * 64) + 1023) / 1024 * 1024;
+    L.stages = stages;
+    L.f0 = L.a0 + stages * kStageA;
+    L.acc = L.f0 + stages * kStageF;
+    L.bars = L.acc + kMaxG * 2 * kTileM * 4;
+    L.total = L.bars + 128 + 1024;  // barriers + alignment slack for the dynamic base
+    return L;
 }
-int mixed_upload(MixedJob&, void*, cudaStream_t, std::string&) { return RBG_ERR_UNSUPPORTED; }
-int mixed_launch(const MixedJob&, void*, uint64_t, int64_t, int64_t, double*, cudaStream_t, std::string&)
+
+// ------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer()
 {
-    return RBG_ERR_UNSUPPORTED;
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
-int mixed_check(const MixedJob&, void*, cudaStream_t, std::string&) { return RBG_ERR_UNSUPPORTED; }
-void mixed_release_cache() {}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase of the given parity; false on timeout or when
+// another role already failed (then the caller winds down).
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site)
+{
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = globaltimer();
+    while (true) {
+        if (mbar_try(bar, parity)) return true;
+        if (*(volatile unsigned int*)err != 0u) return false;
+        if (globaltimer() - t0 > kWaitNs) {
+            atomicCAS(err, 0u, site);
+            return false;
+        }
+    }
+}
+
+// the same wait, made warp-uniform so .sync.aligned tcgen05 ops stay converged
+__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site)
+{
+    const bool ok = mbar_wait(bar, parity, err, site);
+    return __all_sync(0xffffffffu, ok);
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// SW64 K-major shared-memory matrix descriptor (tcgen05 format): start
+// address >> 4, LBO (unused for swizzled K-major) = 1, SBO = 8 rows x 64 B,
+// version bit 46, layout type SWIZZLE_64B (4) in bits 61-63.
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t addr)
+{
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16 (1) or F16 (0),
+// both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__device__ __forceinline__ uint32_t idesc_f16(int n, int ab_bf16)
+{
+    const uint32_t fmt = ab_bf16 ? 1u : 0u;
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 16-bit split x = hi + lo (+ O(2^-16 |x|) for BF16, O(2^-22 |x|) for FP16)
+template <int BF16>
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_t& lo)
+{
+    if (BF16) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+        float2 hf = __bfloat1622float2(h);
+        __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+        hi = *reinterpret_cast<uint32_t*>(&h);
+        lo = *reinterpret_cast<uint32_t*>(&l);
+    } else {
+        __half2 h = __floats2half2_rn(x0, x1);
+        float2 hf = __half22float2(h);
+        __half2 l = __floats2half2_rn(x0 - hf.x, x1 - hf.y);
+        hi = *reinterpret_cast<uint32_t*>(&h);
+        lo = *reinterpret_cast<uint32_t*>(&l);
+    }
+}
+
+// --------------------------------------------------------------- the kernel
+template <int BF16>
+__global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
+{
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    const SmemLayout L = smem_layout(a.Np, a.stages);
+    unsigned char* strip = base + L.strip;
+    float* acc_s = (float*)(base + L.acc);
+    uint64_t* bars = (uint64_t*)(base + L.bars);
+    // barrier slots
+    const int S = a.stages;
+    uint64_t* full = bars;           // [S]
+    uint64_t* empty = bars + 3;      // [S]
+    uint64_t* accf = bars + 6;       // [S]
+    uint64_t* tmem_empty = bars + 9;
+    uint64_t* strip_bar = bars + 10;
+    uint64_t* final_bar = bars + 11;
+    uint32_t* tmem_holder = (uint32_t*)(bars + 12);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int Np = a.Np, nc = a.nc;
+    const int64_t ntiles = (a.B + kTileM - 1) / kTileM;
+    const uint32_t strip_bytes = (uint32_t)(2 * Np * 64);
+
+    if (threadIdx.x == kMmaWarp * 32) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(smem_u32(full + s), kProdWarps);
+            mbar_init(smem_u32(empty + s), 1 + kEpiWarps);
+            mbar_init(smem_u32(accf + s), 1);
+        }
+        mbar_init(smem_u32(tmem_empty), kEpiWarps);
+        mbar_init(smem_u32(strip_bar), 1);
+        mbar_init(smem_u32(final_bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_expect_tx(smem_u32(strip_bar), strip_bytes);
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(strip)),
+            "l"(a.strip), "r"(strip_bytes), "r"(smem_u32(strip_bar))
+            : "memory");
+    }
+    if (warp == kMmaWarp) {
+        __syncwarp();
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                     "r"(a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    if (warp < kProdWarps) {
+        // ------------------------------------------------------- producers
+        const int p = threadIdx.x & (kTileM - 1);
+        const int h = threadIdx.x >> 7;  // which 16 steps of the chunk
+        int64_t lt = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
+            const int64_t m = tile * kTileM + p;
+            const bool valid = m < a.B;
+            const uint64_t gpath = (uint64_t)(a.path0 + m);
+            for (int c = 0; c < nc; ++c) {
+                const int64_t gc = lt * nc + c;
+                const int s = (int)(gc % S);
+                const uint32_t ph = (uint32_t)((gc / S) & 1);
+                if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1)) goto done;
+                unsigned char* st = base + L.a0 + s * kStageA;
+                float* w1s = (float*)(base + L.f0 + s * kStageF);
+                float* w1ps = w1s + kChunk * kTileM;
+                float* w1next = w1ps + kChunk * kTileM;
+                const int step0 = kChunk * c + 16 * h;
+                float w[16], wp[16];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t g = (uint32_t)((step0 >> 2) + q);
+                    const uint4 x0 = philox_group(a.seed, gpath, g, 0);
+                    const uint4 x1 = philox_group(a.seed, gpath, g, 1);
+                    box_muller_f32(x0.x, x0.y, w[4 * q], w[4 * q + 1]);
+                    box_muller_f32(x0.z, x0.w, w[4 * q + 2], w[4 * q + 3]);
+                    box_muller_f32(x1.x, x1.y, wp[4 * q], wp[4 * q + 1]);
+                    box_muller_f32(x1.z, x1.w, wp[4 * q + 2], wp[4 * q + 3]);
+                }
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    if (!valid || step0 + q >= a.N) { w[q] = 0.f; wp[q] = 0.f; }
+                }
+                // A tile: row p, logical 16-byte chunks 2h and 2h+1, SW64 swizzle
+                uint32_t hi[8], lo[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) split2<BF16>(w[2 * q], w[2 * q + 1], hi[q], lo[q]);
+                const int sw = (p >> 1) & 3;
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int off = p * 64 + (((2 * h + e) ^ sw) << 4);
+                    *(uint4*)(st + off) = make_uint4(hi[4 * e], hi[4 * e + 1], hi[4 * e + 2], hi[4 * e + 3]);
+                    *(uint4*)(st + kTileBytes + off) =
+                        make_uint4(lo[4 * e], lo[4 * e + 1], lo[4 * e + 2], lo[4 * e + 3]);
+                }
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    w1s[(16 * h + q) * kTileM + p] = w[q];
+                    w1ps[(16 * h + q) * kTileM + p] = wp[q];
+                }
+                if (h == 1) {
+                    // W1 at step 32c + 32 pairs with the chunk's last column
+                    const int sn = kChunk * (c + 1);
+                    float z0 = 0.f, z1;
+                    if (valid && sn < a.N) {
+                        const uint4 x = philox_group(a.seed, gpath, (uint32_t)(sn >> 2), 0);
+                        box_muller_f32(x.x, x.y, z0, z1);
+                    }
+                    w1next[p] = z0;
+                }
+                if (a.dbg_w && valid) {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        a.dbg_w[(m * 2 + 0) * Np + step0 + q] = w[q];
+                        a.dbg_w[(m * 2 + 1) * Np + step0 + q] = wp[q];
+                    }
+                }
+                fence_proxy_async();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(full + s));
+            }
+        }
+    } else if (warp < kMmaWarp) {
+        // -------------------------------------------------------- epilogue
+        const int ew = warp - kEpiWarp0;  // == warp % 4, the TMEM lane quadrant
+        const int p = ew * 32 + lane;
+        const uint32_t tlane = tmem + ((uint32_t)(ew * 32) << 16);
+        int64_t lt = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
+            const int64_t m = tile * kTileM + p;
+            const bool valid = m < a.B;
+            for (int g = 0; g < a.n_g; ++g) {
+                acc_s[(2 * g) * kTileM + p] = 0.f;
+                acc_s[(2 * g + 1) * kTileM + p] = 0.f;
+            }
+            float w1_0 = 0.f;
+            for (int c = 0; c < nc; ++c) {
+                const int64_t gc = lt * nc + c;
+                const int s = (int)(gc % S);
+                const uint32_t ph = (uint32_t)((gc / S) & 1);
+                // the producers' FP32 tiles of this stage, then the MMA results
+                if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7)) goto done;
+                if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2)) goto done;
+                tc_fence_after();
+                float x[32];
+                tmem_ld32(tlane + (uint32_t)(kChunk * c), x);
+                if (c == nc - 1) {
+                    // accumulator of this tile fully read: the MMA may start the next tile
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(smem_u32(tmem_empty));
+                }
+                const float* w1s = (const float*)(base + L.f0 + s * kStageF);
+                const float* w1ps = w1s + kChunk * kTileM;
+                const float* w1next = w1ps + kChunk * kTileM;
+                float wn[32];
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) {
+                    const float w1 = w1s[jj * kTileM + p];
+                    x[jj] = x[jj] + a.a1 * w1 + a.a2 * w1ps[jj * kTileM + p];
+                    if (jj > 0) wn[jj - 1] = w1;
+                    if (jj == 0 && c == 0) w1_0 = w1;
+                }
+                wn[31] = w1next[p];
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(empty + s));
+                if (a.dbg_x && valid) {
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) a.dbg_x[m * Np + kChunk * c + jj] = x[jj];
+                }
+                for (int g = 0; g < a.n_g; ++g) {
+                    const float al = a.alpha[g];
+                    const float* bt = a.beta + (size_t)g * Np + kChunk * c;
+                    const int lim = a.nsteps[g] - 1 - kChunk * c;
+                    float sv = 0.f, swv = 0.f;
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) {
+                        if (jj < lim) {
+                            const float arg = fmaf(al, x[jj], -__ldg(bt + jj));
+                            sv += exp2f(arg);
+                            swv = fmaf(exp2f(0.5f * arg), wn[jj], swv);
+                        }
+                    }
+                    acc_s[(2 * g) * kTileM + p] += sv;
+                    acc_s[(2 * g + 1) * kTileM + p] += swv;
+                }
+            }
+            if (valid) {
+                for (int g = 0; g < a.n_g; ++g) {
+                    const float Ivdt = a.dt[g] * (a.xi + acc_s[(2 * g) * kTileM + p]);
+                    const float IsvdW = a.sdt[g] * fmaf(a.sqrt_xi, w1_0, acc_s[(2 * g + 1) * kTileM + p]);
+                    a.ivb[(size_t)(a.g0 + g) * a.B + m] = make_float2(Ivdt, IsvdW);
+                }
+            }
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------------ MMA issuer
+        const uint32_t strip_hi = smem_u32(strip);
+        const uint32_t strip_lo = strip_hi + (uint32_t)(Np * 64);
+        if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3)) {
+            int64_t lt = 0;
+            for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
+                if (lt > 0 && !mbar_wait(smem_u32(tmem_empty), (uint32_t)((lt - 1) & 1), a.err, 4)) break;
+                tc_fence_after();
+                bool ok = true;
+                for (int c = 0; c < nc && ok; ++c) {
+                    const int64_t gc = lt * nc + c;
+                    const int s = (int)(gc % S);
+                    const uint32_t ph = (uint32_t)((gc / S) & 1);
+                    if (!mbar_wait(smem_u32(full + s), ph, a.err, 5)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
+                    const uint32_t alo = ahi + kTileBytes;
+                    for (int col0 = kChunk * c; col0 < Np; col0 += 256) {
+                        const int n = (Np - col0 < 256) ? (Np - col0) : 256;
+                        const uint32_t id = idesc_f16(n, BF16);
+                        const uint32_t jrow = (uint32_t)(col0 - kChunk * c);
+#pragma unroll
+                        for (int ks = 0; ks < 2; ++ks) {
+                            const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
+                            const uint64_t dbh = sdesc_sw64(strip_hi + jrow * 64 + 32 * ks);
+                            const uint64_t dbl = sdesc_sw64(strip_lo + jrow * 64 + 32 * ks);
+                            const uint32_t d = tmem + (uint32_t)col0;
+                            umma_f16(d, dah, dbh, id, (c > 0 || ks > 0) ? 1u : 0u);
+                            umma_f16(d, dah, dbl, id, 1u);
+                            umma_f16(d, dal, dbh, id, 1u);
+                        }
+                    }
+                    umma_commit(smem_u32(empty + s));
+                    umma_commit(smem_u32(accf + s));
+                }
+                if (!ok) break;
+            }
+        }
+        // drain every issued MMA before TMEM is released
+        umma_commit(smem_u32(final_bar));
+        mbar_wait(smem_u32(final_bar), 0, a.err, 6);
+    }
+done:
+    tc_fence_before();
+    __syncthreads();
+    if (warp == kMmaWarp) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols)
+                     : "memory");
+    }
+}
+
+// ----------------------------------------------- FP32 payoffs, FP64 sums
+// Conditional BS call (tau = 1, r = 0) from (Ivdt, IsvdW) in FP32.  Tails use
+// erfc so both ITM (via put-call parity) and OTM stay accurate.
+__device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rho, float K, float lnK)
+{
+    const float vol = sqrtf((1.0f - rho * rho) * Ivdt);
+    const float lnS = -0.5f * rho * rho * Ivdt + rho * IsvdW;
+    const float spot = __expf(lnS);
+    if (!(vol > 0.0f)) return fmaxf(spot - K, 0.0f);
+    const float d1 = (lnS - lnK) / vol + 0.5f * vol;
+    const float d2 = d1 - vol;
+    const float r2 = 0.70710678118654752f;
+    if (spot > K) return (spot - K) + (0.5f * K * erfcf(d2 * r2) - 0.5f * spot * erfcf(d1 * r2));
+    return 0.5f * spot * erfcf(-d1 * r2) - 0.5f * K * erfcf(-d2 * r2);
+}
+
+constexpr int kOPB32 = 8;
+
+__global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restrict__ outs, int n_out,
+                                                         const float2* __restrict__ ivb, int64_t B, int G,
+                                                         double* __restrict__ part)
+{
+    __shared__ double red[8][kOPB32][2];
+    const int c = blockIdx.x;
+    const int o0 = blockIdx.y * kOPB32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float rho[kOPB32], K[kOPB32], lnK[kOPB32];
+    int vg[kOPB32];
+#pragma unroll
+    for (int q = 0; q < kOPB32; ++q) {
+        const int i = o0 + q;
+        const OutDev od = (i < n_out) ? outs[i] : OutDev{0.0, 1.0, -1, 0};
+        rho[q] = (float)od.rho; K[q] = (float)od.K; lnK[q] = logf((float)od.K); vg[q] = od.vg;
+    }
+    double S = 0, CS = 0, S2 = 0, CS2 = 0;
+    for (int sub = 0; sub < G; ++sub) {
+        const int64_t m = ((int64_t)c * G + sub) * 256 + threadIdx.x;
+#pragma unroll
+        for (int q = 0; q < kOPB32; ++q) {
+            float x = 0.f;
+            if (m < B && vg[q] >= 0) {
+                const float2 iv = ivb[(size_t)vg[q] * B + m];
+                x = rt_payoff_f32(iv.x, iv.y, rho[q], K[q], lnK[q]);
+            }
+            float x2 = x * x;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+                x2 += __shfl_xor_sync(0xffffffffu, x2, o);
+            }
+            if (lane == 0) { red[w][q][0] = x; red[w][q][1] = x2; }
+        }
+        __syncthreads();
+        if (threadIdx.x < kOPB32) {
+            const int q = threadIdx.x;
+            double s1 = 0, s2 = 0;
+            for (int k = 0; k < 8; ++k) { s1 += red[k][q][0]; s2 += red[k][q][1]; }
+            neumaier_add(S, CS, s1);
+            neumaier_add(S2, CS2, s2);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < kOPB32 && o0 + (int)threadIdx.x < n_out) {
+        double* pp = part + ((size_t)c * n_out + o0 + threadIdx.x) * 4;
+        pp[0] = S; pp[1] = CS; pp[2] = S2; pp[3] = CS2;
+    }
+}
+
+void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int64_t B, int G, double* part,
+                            int nchunks, cudaStream_t st)
+{
+    dim3 grid(nchunks, (n_out + kOPB32 - 1) / kOPB32);
+    k_payoff_sums_f32<<<grid, 256, 0, st>>>(outs, n_out, (const float2*)ivb, B, G, part);
+    count_launch();
+}
+
+// ------------------------------------------------------------------- host
+namespace {
+
+uint16_t to_bf16(float f)
+{
+    __nv_bfloat16 h = __float2bfloat16_rn(f);
+    uint16_t u;
+    std::memcpy(&u, &h, 2);
+    return u;
+}
+float from_bf16(uint16_t u)
+{
+    __nv_bfloat16 h;
+    std::memcpy(&h, &u, 2);
+    return __bfloat162float(h);
+}
+uint16_t to_f16(float f)
+{
+    __half h = __float2half_rn(f);
+    uint16_t u;
+    std::memcpy(&u, &h, 2);
+    return u;
+}
+float from_f16(uint16_t u)
+{
+    __half h;
+    std::memcpy(&h, &u, 2);
+    return __half2float(h);
+}
+
+// S[j'][k'] = Gamma[j' - k'] (j' >= k'), hi/lo 16-bit halves in the SW64
+// K-major image the MMA descriptors expect: row j' at j' * 64 bytes, 16-byte
+// chunk (k' / 8) XOR ((j' / 2) mod 4).
+void build_strip(const double* gamma, int N, int Np, int bf16, unsigned char* img)
+{
+    std::memset(img, 0, (size_t)2 * Np * 64);
+    for (int j = 0; j < Np; ++j)
+        for (int k = 0; k < kChunk; ++k) {
+            const int d = j - k;
+            const double gv = (d >= 0 && d < N) ? gamma[d] : 0.0;
+            uint16_t hi, lo;
+            if (bf16) {
+                hi = to_bf16((float)gv);
+                lo = to_bf16((float)(gv - (double)from_bf16(hi)));
+            } else {
+                hi = to_f16((float)gv);
+                lo = to_f16((float)(gv - (double)from_f16(hi)));
+            }
+            const size_t off = (size_t)j * 64 + ((((k >> 3) ^ ((j >> 1) & 3))) << 4) + (k & 7) * 2;
+            std::memcpy(img + off, &hi, 2);
+            std::memcpy(img + (size_t)Np * 64 + off, &lo, 2);
+        }
+}
+
+}  // namespace
+
+int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        cudaGetLastError();
+        err = "cudaGetDeviceProperties failed";
+        return RBG_ERR_CUDA;
+    }
+    if (prop.major != 10) {
+        err = "mixed form needs a Blackwell (sm_10x) GPU with tcgen05";
+        return RBG_ERR_UNSUPPORTED;
+    }
+    if (o.conv == RBG_CONV_FFT || o.conv == RBG_CONV_DIRECT) {
+        err = "mixed form: only the tensor-core GEMM convolution is built";
+        return RBG_ERR_UNSUPPORTED;
+    }
+    const int N = plan.N;
+    const int Np = (N + kChunk - 1) / kChunk * kChunk;
+    if (Np > kMaxNp) {
+        err = "mixed GEMM form supports N <= 512 (TMEM holds 128 x 512 FP32)";
+        return RBG_ERR_UNSUPPORTED;
+    }
+    job = MixedJob();
+    job.N = N;
+    job.n_vol = (int)plan.vols.size();
+    job.n_vg = (int)plan.vgs.size();
+    job.split = o.split;
+    job.sms = prop.multiProcessorCount;
+    const int bf16 = (o.split == RBG_SPLIT_BF16X3) ? 1 : 0;
+    int stages = 3;
+    if (smem_layout(Np, 3).total > (int)prop.sharedMemPerBlockOptin) stages = 2;
+    if (smem_layout(Np, stages).total > (int)prop.sharedMemPerBlockOptin) {
+        err = "mixed kernel shared memory does not fit";
+        return RBG_ERR_UNSUPPORTED;
+    }
+    int tcols = 32;
+    while (tcols < Np) tcols <<= 1;
+
+    size_t off = 256;  // the error word lives at offset 0
+    job.off_err = 0;
+    const double log2e = 1.4426950408889634;
+    for (int v = 0; v < job.n_vol; ++v) {
+        const VolGroup& vol = plan.vols[v];
+        for (int g0 = vol.vg_begin; g0 < vol.vg_end; g0 += kMaxG) {
+            const int ng = std::min(kMaxG, vol.vg_end - g0);
+            MixedLaunch r;
+            std::memset(&r.args, 0, sizeof(r.args));
+            MixedArgs& A = r.args;
+            A.N = N;
+            A.Np = Np;
+            A.nc = Np / kChunk;
+            A.n_g = ng;
+            A.g0 = g0;
+            A.tmem_cols = tcols;
+            A.stages = stages;
+            A.a1 = (float)vol.a1;
+            A.a2 = (float)vol.a2;
+            A.xi = (float)plan.xi;
+            A.sqrt_xi = (float)std::sqrt(plan.xi);
+            for (int g = 0; g < ng; ++g) {
+                const VGroup& G = plan.vgs[g0 + g];
+                A.alpha[g] = (float)(G.eta * G.scale * log2e);
+                A.dt[g] = (float)G.dt;
+                A.sdt[g] = (float)G.sdt;
+                A.nsteps[g] = G.nsteps;
+            }
+            r.off_strip = off;
+            off += (size_t)2 * Np * 64;
+            off = (off + 255) / 256 * 256;
+            r.off_beta = off;
+            off += (size_t)ng * Np * 4;
+            off = (off + 255) / 256 * 256;
+            job.launches.push_back(r);
+        }
+    }
+    std::vector<unsigned char>& ws = job.host_ws;
+    ws.assign(off, 0);
+    const double lnxi = std::log(plan.xi);
+    for (const MixedLaunch& r : job.launches) {
+        const MixedArgs& A = r.args;
+        const int vol = plan.vgs[A.g0].vol;
+        build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, bf16, ws.data() + r.off_strip);
+        float* beta = (float*)(ws.data() + r.off_beta);
+        for (int g = 0; g < A.n_g; ++g)
+            for (int j = 0; j < Np; ++j) {
+                const double cj = (j < N) ? plan.comp[(size_t)(A.g0 + g) * N + j] : 0.0;
+                beta[(size_t)g * Np + j] = (float)((cj - lnxi) * log2e);
+            }
+    }
+    job.workspace_bytes = off;
+    // batch: float2 per (variance group, path) within 1 GiB
+    int64_t cap = ((int64_t)1 << 30) / (8 * (int64_t)std::max(1, job.n_vg));
+    cap = std::max<int64_t>(kTileM, cap / kTileM * kTileM);
+    job.batch = std::min<int64_t>(M, cap);
+    return RBG_OK;
+}
+
+int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& err)
+{
+    if (cudaMemcpyAsync(ws, job.host_ws.data(), job.host_ws.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        err = "mixed workspace upload failed";
+        return RBG_ERR_CUDA;
+    }
+    return RBG_OK;
+}
+
+int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
+                 cudaStream_t st, std::string& err, float* dbg_w, float* dbg_x)
+{
+    unsigned char* base = (unsigned char*)ws;
+    for (const MixedLaunch& r : job.launches) {
+        MixedArgs A = r.args;
+        A.strip = base + r.off_strip;
+        A.beta = (const float*)(base + r.off_beta);
+        A.ivb = (float2*)ivb;
+        A.err = (unsigned int*)(base + job.off_err);
+        A.dbg_w = dbg_w;
+        A.dbg_x = dbg_x;
+        A.seed = seed;
+        A.path0 = path0;
+        A.B = B;
+        const int smem = smem_layout(A.Np, A.stages).total;
+        const int64_t ntiles = (B + kTileM - 1) / kTileM;
+        const int grid = (int)std::min<int64_t>(ntiles, job.sms);
+        cudaError_t e;
+        if (job.split == RBG_SPLIT_BF16X3) {
+            e = cudaFuncSetAttribute(k_mixed_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e == cudaSuccess) k_mixed_gemm<1><<<grid, kThreads, smem, st>>>(A);
+        } else {
+            e = cudaFuncSetAttribute(k_mixed_gemm<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e == cudaSuccess) k_mixed_gemm<0><<<grid, kThreads, smem, st>>>(A);
+        }
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            err = std::string("mixed kernel launch: ") + cudaGetErrorString(e);
+            return RBG_ERR_CUDA;
+        }
+        count_launch();
+    }
+    return RBG_OK;
+}
+
+int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err)
+{
+    unsigned int word = 0;
+    cudaError_t e = cudaMemcpyAsync(&word, (unsigned char*)ws + job.off_err, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("mixed kernel failed: ") + cudaGetErrorString(e);
+        return RBG_ERR_CUDA;
+    }
+    if (word != 0) {
+        err = "mixed kernel: a bounded pipeline wait expired (site " + std::to_string(word) + ")";
+        return RBG_ERR_TIMEOUT;
+    }
+    return RBG_OK;
+}
+
+
 
 }  // namespace rbg

@@ -1,5 +1,6 @@
 // rbg_mixed.hpp -- the mixed-precision form: tcgen05 Toeplitz-GEMM path
-// kernel fused with Philox generation and the variance-path epilogue.
+// kernel fused with Philox generation and the variance-path epilogue, plus
+// the FP32 payoff / FP64 reduction kernel.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -12,19 +13,44 @@
 
 namespace rbg {
 
+constexpr int kMixedMaxGroups = 16;  // variance groups handled by one launch
+
+// Kernel arguments (passed by value as a __grid_constant__).
+struct MixedArgs {
+    const unsigned char* strip;  // [hi | lo], each Np*64 bytes, SW64 K-major image
+    const float* beta;           // [n_g][Np] log2 compensator minus log2 xi
+    float2* ivb;                 // [n_vg_total][B] (Ivdt, IsvdW)
+    unsigned int* err;           // 0, or the id of the wait that expired
+    float* dbg_w;                // optional [B][2][Np] normals the producers drew
+    float* dbg_x;                // optional [B][Np] X = Y2 + a1 W1 + a2 W1perp
+    uint64_t seed;
+    int64_t path0, B;
+    int N, Np, nc, n_g, g0, tmem_cols, stages;
+    float a1, a2, xi, sqrt_xi;
+    float alpha[kMixedMaxGroups], dt[kMixedMaxGroups], sdt[kMixedMaxGroups];
+    int nsteps[kMixedMaxGroups];
+};
+
+struct MixedLaunch {
+    MixedArgs args;  // device pointers filled at launch time
+    size_t off_strip = 0, off_beta = 0;
+};
+
 struct MixedJob {
     int64_t batch = 0;           // paths per launch
-    size_t workspace_bytes = 0;  // device workspace for tables and the error word
-    int N = 0, n_vol = 0, n_vg = 0, split = 0;
-    std::vector<unsigned char> host_ws;  // image uploaded by mixed_upload
+    size_t workspace_bytes = 0;  // error word + strips + beta tables
     size_t off_err = 0;
+    int N = 0, n_vol = 0, n_vg = 0, split = 0, sms = 0;
+    std::vector<MixedLaunch> launches;   // one per (Volterra pass, <= 16 groups)
+    std::vector<unsigned char> host_ws;  // image uploaded by mixed_upload
 };
 
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err);
-int mixed_upload(MixedJob& job, void* ws, cudaStream_t st, std::string& err);
-int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, double* ivb,
-                 cudaStream_t st, std::string& err);
+int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
+int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
+                 cudaStream_t st, std::string& err, float* dbg_w = nullptr, float* dbg_x = nullptr);
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
-void mixed_release_cache();
+void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int64_t B, int G, double* part,
+                            int nchunks, cudaStream_t st);
 
 }  // namespace rbg

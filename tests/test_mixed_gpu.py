@@ -1,0 +1,119 @@
+"""GPU checks of the mixed-precision form (tcgen05 split GEMM, FP32 path
+state, FP32 payoffs, FP64 cross-path sums).
+
+Stage by stage on identical inputs:
+  normals   the fused kernel's Philox/Box-Muller output equals the exported
+            FP32 stream bit for bit;
+  GEMM      X = Y2 + a1 W1 + a2 W1perp against an FP64 convolution of those
+            normals: BF16x3 error <= 4e-5 of the term magnitude, FP16x3 <= 1e-6;
+  epilogue  (Ivdt, IsvdW) against FP64 on the same normals;
+  prices    against the FP64 form fed the same FP32 normals: at most 1e-4
+            relative and below 0.2 Monte Carlo standard errors.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def R():
+    import rbergomi_gb300 as R
+    R.lib()
+    return R
+
+
+CFG2 = dict(xi=0.235 ** 2, H=[0.1], eta=[1.9], rho=[-0.9], T=[1.0] * 21, K=list(np.linspace(0.6, 1.4, 21)))
+GRID = dict(xi=0.04, H=[0.05, 0.1, 0.1, 0.3, 0.1], eta=[1.0, 1.5, 1.5, 2.5, 1.5],
+            rho=[-0.95, -0.7, -0.5, -0.7, -0.3], T=[0.25, 0.25, 0.5, 1.0, 1.0, 2.0], K=[0.9, 1.1, 1.0, 0.8, 1.3, 2.0])
+
+
+def fp64_x(W1, W1p, H, N):
+    """X_j = sum_{k<j} W1_k Gamma_{j-k} + a1 W1_j + a2 W1perp_j in FP64 and
+    the magnitude sum_{k<j} |W1_k Gamma_{j-k}| (rBergLib/rBergomiMT.cpp:83-109)."""
+    from oracle import oracle as O
+    G = O.gamma(H, N)
+    s2H = np.sqrt(2 * H)
+    rhoH = s2H / (H + 0.5)
+    a1, a2 = rhoH / s2H, np.sqrt(1 - rhoH ** 2) / s2H
+    M = W1.shape[0]
+    Y = np.zeros((M, N))
+    A = np.zeros((M, N))
+    for k in range(N):
+        Y[:, k + 1:] += W1[:, k:k + 1] * G[None, 1:N - k]
+        A[:, k + 1:] += np.abs(W1[:, k:k + 1] * G[None, 1:N - k])
+    return Y + a1 * W1[:, :N] + a2 * W1p[:, :N], A
+
+
+@pytest.mark.parametrize("N,M", [(100, 300), (512, 256), (33, 129)])
+def test_fused_normals_are_the_exported_stream(R, N, M):
+    w, _, _ = R.debug_mixed_paths(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], N, M, seed=11, path_offset=7)
+    Z = R.generate_normals(11, M, N, precision=R.MIXED, path_offset=7)
+    np.testing.assert_array_equal(w[:, :, :N].astype(np.float64), Z)
+    assert np.all(w[:, :, N:] == 0)
+
+
+@pytest.mark.parametrize("split,tol", [(0, 4e-5), (1, 1e-6)])
+@pytest.mark.parametrize("N", [64, 100, 512])
+def test_toeplitz_gemm_columns(R, split, tol, N):
+    H = 0.1
+    M = 256
+    w, x, _ = R.debug_mixed_paths(0.04, [H], [1.5], [-0.7], [1.0], [1.0], N, M, seed=3, split=split)
+    Xf, A = fp64_x(w[:, 0, :].astype(np.float64), w[:, 1, :].astype(np.float64), H, N)
+    err = np.abs(x[:, :N].astype(np.float64) - Xf)
+    assert np.max(err / (A + 1.0)) < tol
+
+
+def test_epilogue_integrals(R, oracle):
+    g = GRID
+    N, M = 64, 384
+    w, _, iv = R.debug_mixed_paths(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, seed=9, split=1)
+    Z = w[:, :, :N].astype(np.float64)
+    # FP64 reference of (Ivdt, IsvdW) per output through the oracle's payoff
+    # machinery: recover them from the FP64 form's per-group sums instead of
+    # re-deriving, by pricing each output with both and comparing payoffs.
+    pay64 = oracle.payoffs_rt(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], Z)
+    _, _, groups = R.plan_info(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N)
+    O = len(g["T"])
+    for i in range(pay64.shape[1]):
+        rho, K = g["rho"][i // O], g["K"][i % O]
+        Iv, Iw = iv[groups[i], :, 0].astype(np.float64), iv[groups[i], :, 1].astype(np.float64)
+        vol = np.sqrt((1 - rho * rho) * Iv)
+        spot = np.exp(-0.5 * rho * rho * Iv + rho * Iw)
+        from scipy.special import erfc
+        d1 = (np.log(spot / K) + 0.5 * vol * vol) / vol
+        pay = 0.5 * erfc(-d1 / np.sqrt(2)) * spot - 0.5 * erfc(-(d1 - vol) / np.sqrt(2)) * K
+        assert np.max(np.abs(pay - pay64[:, i])) < 2e-5 * max(1.0, np.abs(pay64[:, i]).max())
+
+
+@pytest.mark.parametrize("split", [0, 1])
+def test_mixed_prices_vs_fp64_identical_normals(R, split):
+    """Workload-2 shape (N = 512, 21 strikes) at reduced M: error vs the FP64
+    form on the same FP32 normals <= 1e-4 relative and < 0.2 standard errors."""
+    c = CFG2
+    N, M = 512, 1 << 16
+    mp, ms, miv = R.price_rt(c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], N, M, seed=11,
+                             precision=R.MIXED, split=split)
+    fp, fs, fiv = R.price_rt(c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], N, M, seed=11,
+                             normals=R.NORMALS_F32)
+    err = np.abs(mp - fp)
+    assert np.all(err <= 1e-4 * fp)
+    assert np.all(err < 0.2 * fs)
+    assert np.all(np.abs(ms / fs - 1) < 1e-3)
+
+
+def test_mixed_grid_multi_pass(R):
+    g = GRID
+    N, M = 64, 1 << 14
+    mp, ms, _ = R.price_rt(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, seed=21,
+                           precision=R.MIXED, split=1)
+    fp, fs, _ = R.price_rt(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, seed=21,
+                           normals=R.NORMALS_F32)
+    big = fp > 1e-4
+    assert np.all(np.abs(mp - fp)[big] <= 1e-4 * fp[big])
+    assert np.all(np.abs(mp - fp) < 0.2 * np.maximum(fs, 1e-12) + 1e-9)
+
+
+def test_mixed_rejects_long_horizon_without_fft(R):
+    with pytest.raises(R.RbgError):
+        R.price_rt(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 1024, 256, precision=R.MIXED, conv=R.CONV_GEMM)
