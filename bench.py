@@ -308,10 +308,13 @@ def main():
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
     ap.add_argument("--split", type=int, default=0, help="0 = BF16x3, 1 = FP16x3")
     ap.add_argument("--cpu-paths", type=int, default=1 << 17)
+    ap.add_argument("--paths", type=int, default=None, help="override M (small cases for ncu captures)")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     args = ap.parse_args()
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.paths:
+        w["M"] = int(args.paths)
     if args.precision is None:
         args.precision = "mixed" if args.workload.startswith("mixed") else "fp64"
     if args.impl == "reference":
