@@ -9,26 +9,73 @@
 namespace rbg {
 
 // Philox4x32-10: ten rounds of two 32x32->64 multiplies and a Feistel-like
-// permutation, Weyl key schedule between rounds.
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
+// permutation, Weyl key schedule between rounds.  The round keys depend only
+// on the seed, so callers that draw many blocks precompute them once.
+struct PhiloxKeys {
+    uint32_t a[10], b[10];
+};
+
+__device__ __forceinline__ PhiloxKeys philox_keys(uint64_t seed)
+{
+    PhiloxKeys k;
+    uint32_t x = (uint32_t)seed, y = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        k.a[r] = x;
+        k.b[r] = y;
+        x += 0x9E3779B9u;
+        y += 0xBB67AE85u;
+    }
+    return k;
+}
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, const PhiloxKeys& k)
 {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
-        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
-        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
-        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-        k.x += 0x9E3779B9u;
-        k.y += 0xBB67AE85u;
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+        c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ k.a[r], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k.b[r],
+                       (uint32_t)p0);
     }
     return c;
 }
 
 // Counter layout of the project's normal stream: steps 4g..4g+3 of stream s
 // (0 = W1, 1 = W1perp, 2 = Wperp) of global path p.
+__device__ __forceinline__ uint4 philox_group(const PhiloxKeys& k, uint64_t p, uint32_t g, uint32_t s)
+{
+    return philox4x32_10(make_uint4(g, (uint32_t)p, (uint32_t)(p >> 32), s), k);
+}
+
 __device__ __forceinline__ uint4 philox_group(uint64_t seed, uint64_t p, uint32_t g, uint32_t s)
 {
-    return philox4x32_10(make_uint4(g, (uint32_t)p, (uint32_t)(p >> 32), s),
-                         make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+    return philox_group(philox_keys(seed), p, g, s);
+}
+
+// Hardware approximations (PTX .approx instructions on the MUFU pipe).
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lg2_approx(float x)
+{
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ void sincos_approx(float x, float& s, float& c)
+{
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"(x));
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(c) : "f"(x));
 }
 
 // FP64 Box-Muller on uniforms (x + 1/2) 2^-32.
@@ -43,14 +90,17 @@ __device__ __forceinline__ void box_muller_f64(uint32_t a, uint32_t b, double& z
     z1 = r * s;
 }
 
-// FP32 Box-Muller on the same uniforms (mixed form).
+// FP32 Box-Muller on the same uniforms (mixed form), on the MUFU pipe:
+// r = sqrt(-2 ln 2 log2 u0) and the angle 2 pi u1 folded into (-pi, pi] so
+// sin/cos.approx stay in their accurate range (same sin and cos values).
 __device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float& z0, float& z1)
 {
     const float u0 = fmaf((float)a, 2.3283064e-10f, 1.1641532e-10f);
     const float u1 = fmaf((float)b, 2.3283064e-10f, 1.1641532e-10f);
-    const float r = sqrtf(-2.0f * logf(u0));
+    const float r = sqrt_approx(-1.3862944f * lg2_approx(u0));
+    const float th = 6.2831853f * (u1 > 0.5f ? u1 - 1.0f : u1);
     float s, c;
-    sincospif(2.0f * u1, &s, &c);
+    sincos_approx(th, s, c);
     z0 = r * c;
     z1 = r * s;
 }

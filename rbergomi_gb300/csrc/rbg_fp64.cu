@@ -205,25 +205,50 @@ void launch_payoff_sums(const Fp64Tables& t, const double* ivb, int64_t B, int64
     count_launch();
 }
 
-// acc[i * 4 + {0..3}] += chunk sums, in chunk order
-__global__ void k_accumulate(const double* __restrict__ part, int nchunks, int n_out, double* __restrict__ acc)
+// acc[i * 4 + {0..3}] += the batch's chunk sums.  One block per output:
+// strided Neumaier sums per thread, then a fixed-shape tree, so the result
+// does not depend on scheduling.
+__global__ void __launch_bounds__(256) k_accumulate(const double* __restrict__ part, int nchunks, int n_out,
+                                                    double* __restrict__ acc)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_out) return;
-    double S = acc[i * 4 + 0], C = acc[i * 4 + 1], S2 = acc[i * 4 + 2], C2 = acc[i * 4 + 3];
-    for (int c = 0; c < nchunks; ++c) {
+    __shared__ double sh[4][256];
+    const int i = blockIdx.x;
+    double S = 0, C = 0, S2 = 0, C2 = 0;
+    for (int c = threadIdx.x; c < nchunks; c += blockDim.x) {
         const double* p = part + ((size_t)c * n_out + i) * 4;
         neumaier_add(S, C, p[0]);
         neumaier_add(S, C, p[1]);
         neumaier_add(S2, C2, p[2]);
         neumaier_add(S2, C2, p[3]);
     }
-    acc[i * 4 + 0] = S; acc[i * 4 + 1] = C; acc[i * 4 + 2] = S2; acc[i * 4 + 3] = C2;
+    sh[0][threadIdx.x] = S; sh[1][threadIdx.x] = C; sh[2][threadIdx.x] = S2; sh[3][threadIdx.x] = C2;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            const int j = threadIdx.x + h;
+            double a = sh[0][threadIdx.x], ac = sh[1][threadIdx.x];
+            neumaier_add(a, ac, sh[0][j]);
+            neumaier_add(a, ac, sh[1][j]);
+            double b = sh[2][threadIdx.x], bc = sh[3][threadIdx.x];
+            neumaier_add(b, bc, sh[2][j]);
+            neumaier_add(b, bc, sh[3][j]);
+            sh[0][threadIdx.x] = a; sh[1][threadIdx.x] = ac; sh[2][threadIdx.x] = b; sh[3][threadIdx.x] = bc;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double a = acc[i * 4 + 0], ac = acc[i * 4 + 1], b = acc[i * 4 + 2], bc = acc[i * 4 + 3];
+        neumaier_add(a, ac, sh[0][0]);
+        neumaier_add(a, ac, sh[1][0]);
+        neumaier_add(b, bc, sh[2][0]);
+        neumaier_add(b, bc, sh[3][0]);
+        acc[i * 4 + 0] = a; acc[i * 4 + 1] = ac; acc[i * 4 + 2] = b; acc[i * 4 + 3] = bc;
+    }
 }
 
 void launch_accumulate(const double* part, int nchunks, int n_out, double* acc, void* stream)
 {
-    k_accumulate<<<(n_out + 127) / 128, 128, 0, (cudaStream_t)stream>>>(part, nchunks, n_out, acc);
+    k_accumulate<<<n_out, 256, 0, (cudaStream_t)stream>>>(part, nchunks, n_out, acc);
     count_launch();
 }
 
@@ -236,76 +261,83 @@ __device__ double bs_gen(double K, double T, double s, int put)
     return put ? (-phi_cdf(-d1) + phi_cdf(-d2) * K) : (phi_cdf(d1) - phi_cdf(d2) * K);
 }
 
-// Inverts on the out-of-the-money side (put-call parity for K < 1, as
-// rBergLib/BlackScholes.cpp:38-41 does): bracket by doubling, Newton steps on
-// log(price) safeguarded by bisection, to ~1e-15 relative.
-__device__ double implied_vol_call(double price, double K, double T)
+// Implied vol by a warp: inverts on the out-of-the-money side (put-call
+// parity for K < 1, as rBergLib/BlackScholes.cpp:38-41 does).  The 32 lanes
+// price 32 volatilities at once: first a geometric grid 1e-3 * 2^(l/2) to
+// bracket the root, then repeated 33-section of the bracket (the price is
+// increasing in sigma), shrinking it ~33x per round to ~1e-15 relative.
+// All lanes return the same value; NaN when no volatility fits.
+__device__ double implied_vol_warp(double price, double K, double T)
 {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     const int put = 1.0 > K;
     const double target = put ? price - 1.0 + K : price;
     const double upper = put ? K : 1.0;
-    if (!(target > 0.0) || !(target < upper) || !(T > 0.0)) return __longlong_as_double(0x7ff8000000000000ll);
-    double lo = 0.0, hi = 0.5;
-    for (int it = 0; it < 60; ++it) {
-        if (bs_gen(K, T, hi, put) >= target) break;
-        lo = hi;
-        hi *= 2.0;
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    if (!(target > 0.0) || !(target < upper) || !(T > 0.0)) return nan;
+    double sig = 1e-3 * exp2(0.5 * lane);
+    unsigned b = __ballot_sync(FULL, bs_gen(K, T, sig, put) >= target);
+    if (b == 0u) return nan;
+    int f = __ffs(b) - 1;
+    double lo = (f > 0) ? 1e-3 * exp2(0.5 * (f - 1)) : 0.0;
+    double hi = 1e-3 * exp2(0.5 * f);
+    for (int it = 0; it < 14 && hi - lo > 1e-15 * hi; ++it) {
+        const double s = lo + (hi - lo) * (double)(lane + 1) / 33.0;
+        b = __ballot_sync(FULL, bs_gen(K, T, s, put) >= target);
+        f = b ? __ffs(b) - 1 : 32;
+        const double nlo = __shfl_sync(FULL, s, f > 0 ? f - 1 : 0);
+        const double nhi = __shfl_sync(FULL, s, f < 32 ? f : 31);
+        if (f > 0) lo = nlo;
+        if (f < 32) hi = nhi;
     }
-    const double lt = log(target);
-    double s = 0.5 * (lo + hi);
-    for (int it = 0; it < 200; ++it) {
-        const double p = bs_gen(K, T, s, put);
-        if (p > target) hi = s; else lo = s;
-        double sn;
-        if (p > 0.0) {
-            const double d1 = (log(1.0 / K) + 0.5 * s * s * T) / (s * sqrt(T));
-            const double vega = exp(-0.5 * d1 * d1) * 0.39894228040143267794 * sqrt(T);
-            sn = s - (log(p) - lt) * p / vega;
-        } else {
-            sn = 0.5 * (lo + hi);
-        }
-        if (!(sn > lo && sn < hi)) sn = 0.5 * (lo + hi);
-        if (fabs(sn - s) <= 1e-15 * s || hi - lo <= 1e-15 * hi) { s = sn; break; }
-        s = sn;
-    }
-    return s;
+    return 0.5 * (lo + hi);
 }
 
-// res: [0,n) price, [n,2n) stat, [2n,3n) iv, [3n,4n) sum, [4n,5n) sum2
+// res: [0,n) price, [n,2n) stat, [2n,3n) iv, [3n,4n) sum, [4n,5n) sum2.
+// One warp per output.
 __global__ void k_finalize(const double* __restrict__ acc, int n_out, int64_t M, const OutDev* __restrict__ outs,
                            const double* __restrict__ Tv, int compute_iv, double* __restrict__ res)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_out) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n_out) return;  // whole warps leave together
     const double S = acc[i * 4 + 0] + acc[i * 4 + 1];
     const double S2 = acc[i * 4 + 2] + acc[i * 4 + 3];
     // rBergLib/rBergomiMT.cpp:404-409
     const double price = S * (1.0 / (double)M);
     const double var = 1.0 * (S2 * (1.0 / (double)M)) + -1.0 * (price * price);
     const double stat = sqrt(var) * (1.0 / sqrt((double)M));
-    res[i] = price;
-    res[n_out + i] = stat;
-    res[2 * n_out + i] = compute_iv ? implied_vol_call(price, outs[i].K, Tv[i]) : 0.0;
-    res[3 * n_out + i] = S;
-    res[4 * n_out + i] = S2;
+    const double iv = compute_iv ? implied_vol_warp(price, outs[i].K, Tv[i]) : 0.0;
+    if ((threadIdx.x & 31) == 0) {
+        res[i] = price;
+        res[n_out + i] = stat;
+        res[2 * n_out + i] = iv;
+        res[3 * n_out + i] = S;
+        res[4 * n_out + i] = S2;
+    }
 }
 
 void launch_finalize(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,
                      int compute_iv, double* res, void* stream)
 {
-    k_finalize<<<(n_out + 127) / 128, 128, 0, (cudaStream_t)stream>>>(acc, n_out, M, outs, Tvals, compute_iv, res);
+    const int threads = 128;
+    const int blocks = (int)(((int64_t)n_out * 32 + threads - 1) / threads);
+    k_finalize<<<blocks, threads, 0, (cudaStream_t)stream>>>(acc, n_out, M, outs, Tvals, compute_iv, res);
     count_launch();
 }
 
 __global__ void k_implied_vol(int n, const double* price, const double* K, const double* T, double* iv)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) iv[i] = implied_vol_call(price[i], K[i], T[i]);
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    const double v = implied_vol_warp(price[i], K[i], T[i]);
+    if ((threadIdx.x & 31) == 0) iv[i] = v;
 }
 
 void launch_implied_vol(int n, const double* price, const double* K, const double* T, double* iv, void* stream)
 {
-    k_implied_vol<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(n, price, K, T, iv);
+    const int blocks = (int)(((int64_t)n * 32 + 127) / 128);
+    k_implied_vol<<<blocks, 128, 0, (cudaStream_t)stream>>>(n, price, K, T, iv);
     count_launch();
 }
 

@@ -65,10 +65,10 @@ constexpr int kStageA = 2 * kTileBytes;                                  // hi +
 constexpr int kStageF = 2 * kChunk * kTileM * 4 + kTileM * 4;            // w1, w1perp, w1next
 
 struct SmemLayout {
-    int strip, a0, f0, stages, acc, bars, total;
+    int strip, a0, f0, stages, acc, beta, bars, total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int Np, int stages)
+__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g)
 {
     SmemLayout L;
     L.strip = 0;
@@ -76,7 +76,8 @@ __host__ __device__ inline SmemLayout smem_layout(int Np, int stages)
     L.stages = stages;
     L.f0 = L.a0 + stages * kStageA;
     L.acc = L.f0 + stages * kStageF;
-    L.bars = L.acc + kMaxG * 2 * kTileM * 4;
+    L.beta = L.acc + n_g * 2 * kTileM * 4;
+    L.bars = L.beta + n_g * Np * 4;
     L.total = L.bars + 128 + 1024;  // barriers + alignment slack for the dynamic base
     return L;
 }
@@ -219,9 +220,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    const SmemLayout L = smem_layout(a.Np, a.stages);
+    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g);
     unsigned char* strip = base + L.strip;
     float* acc_s = (float*)(base + L.acc);
+    float* beta_s = (float*)(base + L.beta);
     uint64_t* bars = (uint64_t*)(base + L.bars);
     // barrier slots
     const int S = a.stages;
@@ -262,6 +264,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    for (int i = threadIdx.x; i < a.n_g * a.Np; i += blockDim.x) beta_s[i] = a.beta[i];
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -271,6 +274,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         // ------------------------------------------------------- producers
         const int p = threadIdx.x & (kTileM - 1);
         const int h = threadIdx.x >> 7;  // which 16 steps of the chunk
+        const PhiloxKeys keys = philox_keys(a.seed);
         int64_t lt = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
             const int64_t m = tile * kTileM + p;
@@ -290,8 +294,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const uint32_t g = (uint32_t)((step0 >> 2) + q);
-                    const uint4 x0 = philox_group(a.seed, gpath, g, 0);
-                    const uint4 x1 = philox_group(a.seed, gpath, g, 1);
+                    const uint4 x0 = philox_group(keys, gpath, g, 0);
+                    const uint4 x1 = philox_group(keys, gpath, g, 1);
                     box_muller_f32(x0.x, x0.y, w[4 * q], w[4 * q + 1]);
                     box_muller_f32(x0.z, x0.w, w[4 * q + 2], w[4 * q + 3]);
                     box_muller_f32(x1.x, x1.y, wp[4 * q], wp[4 * q + 1]);
@@ -323,7 +327,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     const int sn = kChunk * (c + 1);
                     float z0 = 0.f, z1;
                     if (valid && sn < a.N) {
-                        const uint4 x = philox_group(a.seed, gpath, (uint32_t)(sn >> 2), 0);
+                        const uint4 x = philox_group(keys, gpath, (uint32_t)(sn >> 2), 0);
                         box_muller_f32(x.x, x.y, z0, z1);
                     }
                     w1next[p] = z0;
@@ -388,17 +392,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
 #pragma unroll
                     for (int jj = 0; jj < 32; ++jj) a.dbg_x[m * Np + kChunk * c + jj] = x[jj];
                 }
+                // v_{j+1} = xi exp(eta WS_j - comp_j): su = sqrt(v) = 2^(alpha/2 X - beta/2),
+                // one MUFU ex2 per element and group, v = su * su
                 for (int g = 0; g < a.n_g; ++g) {
-                    const float al = a.alpha[g];
-                    const float* bt = a.beta + (size_t)g * Np + kChunk * c;
+                    const float ah = a.alpha[g];
+                    const float* bt = beta_s + g * Np + kChunk * c;
                     const int lim = a.nsteps[g] - 1 - kChunk * c;
                     float sv = 0.f, swv = 0.f;
+                    if (lim >= 32) {
 #pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) {
-                        if (jj < lim) {
-                            const float arg = fmaf(al, x[jj], -__ldg(bt + jj));
-                            sv += exp2f(arg);
-                            swv = fmaf(exp2f(0.5f * arg), wn[jj], swv);
+                        for (int jj = 0; jj < 32; ++jj) {
+                            const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
+                            sv = fmaf(su, su, sv);
+                            swv = fmaf(su, wn[jj], swv);
+                        }
+                    } else {
+#pragma unroll
+                        for (int jj = 0; jj < 32; ++jj) {
+                            if (jj < lim) {
+                                const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
+                                sv = fmaf(su, su, sv);
+                                swv = fmaf(su, wn[jj], swv);
+                            }
                         }
                     }
                     acc_s[(2 * g) * kTileM + p] += sv;
@@ -500,36 +515,43 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
         const OutDev od = (i < n_out) ? outs[i] : OutDev{0.0, 1.0, -1, 0};
         rho[q] = (float)od.rho; K[q] = (float)od.K; lnK[q] = logf((float)od.K); vg[q] = od.vg;
     }
-    double S = 0, CS = 0, S2 = 0, CS2 = 0;
+    // each thread sums its own G paths in FP32 (G <= a few dozen), FP64 from the warp level up
+    float s1[kOPB32], s2[kOPB32];
+#pragma unroll
+    for (int q = 0; q < kOPB32; ++q) { s1[q] = 0.f; s2[q] = 0.f; }
     for (int sub = 0; sub < G; ++sub) {
         const int64_t m = ((int64_t)c * G + sub) * 256 + threadIdx.x;
+        if (m >= B) break;
+        int cur = -1;
+        float2 iv = make_float2(0.f, 0.f);
 #pragma unroll
         for (int q = 0; q < kOPB32; ++q) {
-            float x = 0.f;
-            if (m < B && vg[q] >= 0) {
-                const float2 iv = ivb[(size_t)vg[q] * B + m];
-                x = rt_payoff_f32(iv.x, iv.y, rho[q], K[q], lnK[q]);
-            }
-            float x2 = x * x;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                x += __shfl_xor_sync(0xffffffffu, x, o);
-                x2 += __shfl_xor_sync(0xffffffffu, x2, o);
-            }
-            if (lane == 0) { red[w][q][0] = x; red[w][q][1] = x2; }
+            if (vg[q] < 0) continue;
+            if (vg[q] != cur) { cur = vg[q]; iv = ivb[(size_t)cur * B + m]; }
+            const float x = rt_payoff_f32(iv.x, iv.y, rho[q], K[q], lnK[q]);
+            s1[q] += x;
+            s2[q] = fmaf(x, x, s2[q]);
         }
-        __syncthreads();
-        if (threadIdx.x < kOPB32) {
-            const int q = threadIdx.x;
-            double s1 = 0, s2 = 0;
-            for (int k = 0; k < 8; ++k) { s1 += red[k][q][0]; s2 += red[k][q][1]; }
-            neumaier_add(S, CS, s1);
-            neumaier_add(S2, CS2, s2);
-        }
-        __syncthreads();
     }
+#pragma unroll
+    for (int q = 0; q < kOPB32; ++q) {
+        double a = s1[q], b = s2[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        if (lane == 0) { red[w][q][0] = a; red[w][q][1] = b; }
+    }
+    __syncthreads();
     if (threadIdx.x < kOPB32 && o0 + (int)threadIdx.x < n_out) {
-        double* pp = part + ((size_t)c * n_out + o0 + threadIdx.x) * 4;
+        const int q = threadIdx.x;
+        double S = 0, CS = 0, S2 = 0, CS2 = 0;
+        for (int k = 0; k < 8; ++k) {
+            neumaier_add(S, CS, red[k][q][0]);
+            neumaier_add(S2, CS2, red[k][q][1]);
+        }
+        double* pp = part + ((size_t)c * n_out + o0 + q) * 4;
         pp[0] = S; pp[1] = CS; pp[2] = S2; pp[3] = CS2;
     }
 }
@@ -629,12 +651,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     job.split = o.split;
     job.sms = prop.multiProcessorCount;
     const int bf16 = (o.split == RBG_SPLIT_BF16X3) ? 1 : 0;
-    int stages = 3;
-    if (smem_layout(Np, 3).total > (int)prop.sharedMemPerBlockOptin) stages = 2;
-    if (smem_layout(Np, stages).total > (int)prop.sharedMemPerBlockOptin) {
-        err = "mixed kernel shared memory does not fit";
-        return RBG_ERR_UNSUPPORTED;
-    }
+    const int optin = (int)prop.sharedMemPerBlockOptin;
     int tcols = 32;
     while (tcols < Np) tcols <<= 1;
 
@@ -654,14 +671,18 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             A.n_g = ng;
             A.g0 = g0;
             A.tmem_cols = tcols;
-            A.stages = stages;
+            A.stages = (smem_layout(Np, 3, ng).total <= optin) ? 3 : 2;
+            if (smem_layout(Np, A.stages, ng).total > optin) {
+                err = "mixed kernel shared memory does not fit";
+                return RBG_ERR_UNSUPPORTED;
+            }
             A.a1 = (float)vol.a1;
             A.a2 = (float)vol.a2;
             A.xi = (float)plan.xi;
             A.sqrt_xi = (float)std::sqrt(plan.xi);
             for (int g = 0; g < ng; ++g) {
                 const VGroup& G = plan.vgs[g0 + g];
-                A.alpha[g] = (float)(G.eta * G.scale * log2e);
+                A.alpha[g] = (float)(0.5 * G.eta * G.scale * log2e);  // halved: the epilogue forms sqrt(v)
                 A.dt[g] = (float)G.dt;
                 A.sdt[g] = (float)G.sdt;
                 A.nsteps[g] = G.nsteps;
@@ -686,7 +707,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         for (int g = 0; g < A.n_g; ++g)
             for (int j = 0; j < Np; ++j) {
                 const double cj = (j < N) ? plan.comp[(size_t)(A.g0 + g) * N + j] : 0.0;
-                beta[(size_t)g * Np + j] = (float)((cj - lnxi) * log2e);
+                beta[(size_t)g * Np + j] = (float)(0.5 * (cj - lnxi) * log2e);
             }
     }
     job.workspace_bytes = off;
@@ -723,7 +744,7 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         A.seed = seed;
         A.path0 = path0;
         A.B = B;
-        const int smem = smem_layout(A.Np, A.stages).total;
+        const int smem = smem_layout(A.Np, A.stages, A.n_g).total;
         const int64_t ntiles = (B + kTileM - 1) / kTileM;
         const int grid = (int)std::min<int64_t>(ntiles, job.sms);
         cudaError_t e;

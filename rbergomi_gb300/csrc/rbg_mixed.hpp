@@ -18,7 +18,7 @@ constexpr int kMixedMaxGroups = 16;  // variance groups handled by one launch
 // Kernel arguments (passed by value as a __grid_constant__).
 struct MixedArgs {
     const unsigned char* strip;  // [hi | lo], each Np*64 bytes, SW64 K-major image
-    const float* beta;           // [n_g][Np] log2 compensator minus log2 xi
+    const float* beta;           // [n_g][Np] (log2 compensator - log2 xi) / 2
     float2* ivb;                 // [n_vg_total][B] (Ivdt, IsvdW)
     unsigned int* err;           // 0, or the id of the wait that expired
     float* dbg_w;                // optional [B][2][Np] normals the producers drew
@@ -27,7 +27,8 @@ struct MixedArgs {
     int64_t path0, B;
     int N, Np, nc, n_g, g0, tmem_cols, stages;
     float a1, a2, xi, sqrt_xi;
-    float alpha[kMixedMaxGroups], dt[kMixedMaxGroups], sdt[kMixedMaxGroups];
+    float alpha[kMixedMaxGroups];  // eta * scale * log2(e) / 2
+    float dt[kMixedMaxGroups], sdt[kMixedMaxGroups];
     int nsteps[kMixedMaxGroups];
 };
 

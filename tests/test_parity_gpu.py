@@ -27,7 +27,11 @@ def test_normals_match_oracle(R, oracle):
     assert np.max(np.abs(Z - Zo)) < 1e-13
     Z32 = R.generate_normals(42, 300, 37, precision=R.MIXED, path_offset=12345)
     assert np.all(Z32.astype(np.float32).astype(np.float64) == Z32)
-    assert np.max(np.abs(Z32 - Zo)) < 1e-4
+    # the FP32 transform runs on hardware approximations (lg2/sqrt/sin/cos
+    # .approx): ~1e-6 relative except near r = 0, where log2(u) ~ 0 loses bits
+    d = np.abs(Z32 - Zo)
+    assert np.max(d) < 1e-3
+    assert np.mean(d < 1e-5 * (1 + np.abs(Zo))) > 0.999
 
 
 @pytest.mark.parametrize("name", QUAD_CASES)
