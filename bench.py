@@ -181,7 +181,9 @@ def run_gpu(args, w):
     prec = R.MIXED if args.precision == "mixed" else R.FP64
     # weak scaling: every rank prices its own M paths (disjoint Philox paths)
     offset = rank * w["M"]
-    kw = dict(seed=w["seed"], precision=prec, split=args.split, path_offset=offset, stream=sptr)
+    conv = {"auto": R.CONV_AUTO, "gemm": R.CONV_GEMM, "fft": R.CONV_FFT}[args.conv]
+    kw = dict(seed=w["seed"], precision=prec, split=args.split, path_offset=offset, stream=sptr,
+              conv=conv if prec == R.MIXED else R.CONV_AUTO)
     flush = torch.empty((256 << 20) // 4, dtype=torch.float32, device="cuda")
 
     def step():
@@ -231,7 +233,8 @@ def run_gpu(args, w):
     exec_flops = 6.0 * 32 * 32 * nc * (nc + 1) / 2 * w["M"] / max(1, kn // args.steps)
     roof = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
             "frac": achieved_tf / bf16_peak, "traffic": traffic_per_launch("k_mixed_gemm", w),
-            "kernel": "k_mixed_gemm" if prec == R.MIXED else "k_path_fp64",
+            "kernel": ("k_mixed_fft" if (args.conv == "fft" or (args.conv == "auto" and w["N"] > 512))
+                       else "k_mixed_gemm") if prec == R.MIXED else "k_path_fp64",
             "kernel_ms": avg_kernel_ms, "peak_source": f"{peak_src} bf16 burst",
             "algorithmic_flops_per_launch": algo_flops,
             "executed_tensor_tflops": exec_flops / (avg_kernel_ms / 1e3) / 1e12 if prec == R.MIXED else None}
@@ -289,7 +292,8 @@ def run_gpu(args, w):
         "data": "synthetic (Philox4x32-10 normals generated on device)",
         "config": {"workload": args.workload, "N": w["N"], "M": w["M"], "strikes": len(w["K"]),
                    "H": w["H"], "eta": w["eta"], "rho": w["rho"], "xi": w["xi"], "T": w["T"][0],
-                   "seed": w["seed"], "precision": args.precision, "l2": "flushed (256 MiB write) before each step",
+                   "seed": w["seed"], "precision": args.precision, "conv": args.conv,
+                   "l2": "flushed (256 MiB write) before each step",
                    "prices_per_step": len(w["H"]) * len(w["K"])},
         "prices_per_s": ws * len(w["H"]) * len(w["K"]) / (ms_step / 1e3),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(), "gpu_launches": launches,
@@ -309,12 +313,16 @@ def main():
     ap.add_argument("--split", type=int, default=0, help="0 = BF16x3, 1 = FP16x3")
     ap.add_argument("--cpu-paths", type=int, default=1 << 17)
     ap.add_argument("--paths", type=int, default=None, help="override M (small cases for ncu captures)")
+    ap.add_argument("--steps-per-path", type=int, default=None, help="override N (crossover sweeps)")
+    ap.add_argument("--conv", default="auto", choices=["auto", "gemm", "fft"], help="mixed-form Volterra backend")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.paths:
         w["M"] = int(args.paths)
+    if args.steps_per_path:
+        w["N"] = int(args.steps_per_path)
     if args.precision is None:
         args.precision = "mixed" if args.workload.startswith("mixed") else "fp64"
     if args.impl == "reference":

@@ -634,17 +634,24 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         err = "mixed form needs a Blackwell (sm_10x) GPU with tcgen05";
         return RBG_ERR_UNSUPPORTED;
     }
-    if (o.conv == RBG_CONV_FFT || o.conv == RBG_CONV_DIRECT) {
-        err = "mixed form: only the tensor-core GEMM convolution is built";
+    if (o.conv == RBG_CONV_DIRECT) {
+        err = "mixed form: the direct Volterra sum is FP64-only; use GEMM or FFT";
         return RBG_ERR_UNSUPPORTED;
     }
     const int N = plan.N;
     const int Np = (N + kChunk - 1) / kChunk * kChunk;
-    if (Np > kMaxNp) {
-        err = "mixed GEMM form supports N <= 512 (TMEM holds 128 x 512 FP32)";
+    int backend = o.conv;
+    if (backend == RBG_CONV_AUTO) backend = (Np <= kMaxNp) ? RBG_CONV_GEMM : RBG_CONV_FFT;
+    if (backend == RBG_CONV_GEMM && Np > kMaxNp) {
+        err = "mixed GEMM form supports N <= 512 (TMEM holds 128 x 512 FP32); use the FFT backend";
+        return RBG_ERR_UNSUPPORTED;
+    }
+    if (backend == RBG_CONV_FFT && N > 4096) {
+        err = "mixed FFT backend supports N <= 4096 (two 8192-point buffers in shared memory)";
         return RBG_ERR_UNSUPPORTED;
     }
     job = MixedJob();
+    job.backend = backend;
     job.N = N;
     job.n_vol = (int)plan.vols.size();
     job.n_vg = (int)plan.vgs.size();
@@ -672,7 +679,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             A.g0 = g0;
             A.tmem_cols = tcols;
             A.stages = (smem_layout(Np, 3, ng).total <= optin) ? 3 : 2;
-            if (smem_layout(Np, A.stages, ng).total > optin) {
+            if (backend == RBG_CONV_GEMM && smem_layout(Np, A.stages, ng).total > optin) {
                 err = "mixed kernel shared memory does not fit";
                 return RBG_ERR_UNSUPPORTED;
             }
@@ -687,14 +694,31 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
                 A.sdt[g] = (float)G.sdt;
                 A.nsteps[g] = G.nsteps;
             }
-            r.off_strip = off;
-            off += (size_t)2 * Np * 64;
-            off = (off + 255) / 256 * 256;
+            if (backend == RBG_CONV_GEMM) {
+                r.off_strip = off;
+                off += (size_t)2 * Np * 64;
+                off = (off + 255) / 256 * 256;
+            } else {
+                A.logL = fft_log2_len(N);
+                A.L = 1 << A.logL;
+                if (fft_smem_bytes(N, ng) > (size_t)optin) {
+                    err = "mixed FFT kernel shared memory does not fit";
+                    return RBG_ERR_UNSUPPORTED;
+                }
+                r.off_spec = off;
+                off += (size_t)A.L * 8;
+                off = (off + 255) / 256 * 256;
+            }
             r.off_beta = off;
             off += (size_t)ng * Np * 4;
             off = (off + 255) / 256 * 256;
             job.launches.push_back(r);
         }
+    }
+    if (backend == RBG_CONV_FFT) {
+        job.off_tw = off;
+        off += (size_t)(1 << fft_log2_len(N)) * 8;
+        off = (off + 255) / 256 * 256;
     }
     std::vector<unsigned char>& ws = job.host_ws;
     ws.assign(off, 0);
@@ -702,7 +726,11 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     for (const MixedLaunch& r : job.launches) {
         const MixedArgs& A = r.args;
         const int vol = plan.vgs[A.g0].vol;
-        build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, bf16, ws.data() + r.off_strip);
+        if (backend == RBG_CONV_GEMM)
+            build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, bf16, ws.data() + r.off_strip);
+        else
+            fft_tables(plan.gamma.data() + (size_t)vol * N, N, A.logL, (float*)(ws.data() + r.off_spec),
+                       (float*)(ws.data() + job.off_tw));
         float* beta = (float*)(ws.data() + r.off_beta);
         for (int g = 0; g < A.n_g; ++g)
             for (int j = 0; j < Np; ++j) {
@@ -737,6 +765,8 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         MixedArgs A = r.args;
         A.strip = base + r.off_strip;
         A.beta = (const float*)(base + r.off_beta);
+        A.spec = (const float2*)(base + r.off_spec);
+        A.tw = (const float2*)(base + job.off_tw);
         A.ivb = (float2*)ivb;
         A.err = (unsigned int*)(base + job.off_err);
         A.dbg_w = dbg_w;
@@ -748,7 +778,9 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         const int64_t ntiles = (B + kTileM - 1) / kTileM;
         const int grid = (int)std::min<int64_t>(ntiles, job.sms);
         cudaError_t e;
-        if (job.split == RBG_SPLIT_BF16X3) {
+        if (job.backend == RBG_CONV_FFT) {
+            e = launch_mixed_fft(A, job.sms, st);
+        } else if (job.split == RBG_SPLIT_BF16X3) {
             e = cudaFuncSetAttribute(k_mixed_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e == cudaSuccess) k_mixed_gemm<1><<<grid, kThreads, smem, st>>>(A);
         } else {

@@ -23,9 +23,12 @@ struct MixedArgs {
     unsigned int* err;           // 0, or the id of the wait that expired
     float* dbg_w;                // optional [B][2][Np] normals the producers drew
     float* dbg_x;                // optional [B][Np] X = Y2 + a1 W1 + a2 W1perp
+    const float2* spec;          // FFT backend: FFT(Gamma)/L, L points
+    const float2* tw;            // FFT backend: exp(-2 pi i t / L), L points
     uint64_t seed;
     int64_t path0, B;
     int N, Np, nc, n_g, g0, tmem_cols, stages;
+    int L, logL;  // FFT backend transform length
     float a1, a2, xi, sqrt_xi;
     float alpha[kMixedMaxGroups];  // eta * scale * log2(e) / 2
     float dt[kMixedMaxGroups], sdt[kMixedMaxGroups];
@@ -34,7 +37,7 @@ struct MixedArgs {
 
 struct MixedLaunch {
     MixedArgs args;  // device pointers filled at launch time
-    size_t off_strip = 0, off_beta = 0;
+    size_t off_strip = 0, off_beta = 0, off_spec = 0;
 };
 
 struct MixedJob {
@@ -42,6 +45,8 @@ struct MixedJob {
     size_t workspace_bytes = 0;  // error word + strips + beta tables
     size_t off_err = 0;
     int N = 0, n_vol = 0, n_vg = 0, split = 0, sms = 0;
+    int backend = RBG_CONV_GEMM;  // RBG_CONV_GEMM or RBG_CONV_FFT
+    size_t off_tw = 0;
     std::vector<MixedLaunch> launches;   // one per (Volterra pass, <= 16 groups)
     std::vector<unsigned char> host_ws;  // image uploaded by mixed_upload
 };
@@ -51,6 +56,12 @@ int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& er
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
                  cudaStream_t st, std::string& err, float* dbg_w = nullptr, float* dbg_x = nullptr);
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
+// FFT backend (rbg_fft.cu)
+int fft_log2_len(int N);
+size_t fft_smem_bytes(int N, int n_g);
+void fft_tables(const double* gamma, int N, int logL, float* spec, float* tw);
+cudaError_t launch_mixed_fft(const MixedArgs& A, int sms, cudaStream_t st);
+
 void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int64_t B, int G, double* part,
                             int nchunks, cudaStream_t st);
 

@@ -114,6 +114,42 @@ def test_mixed_grid_multi_pass(R):
     assert np.all(np.abs(mp - fp) < 0.2 * np.maximum(fs, 1e-12) + 1e-9)
 
 
-def test_mixed_rejects_long_horizon_without_fft(R):
+def test_gemm_backend_rejects_long_horizon(R):
     with pytest.raises(R.RbgError):
         R.price_rt(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 1024, 256, precision=R.MIXED, conv=R.CONV_GEMM)
+
+
+# ------------------------------------------------------------ FFT backend
+@pytest.mark.parametrize("N,M", [(64, 130), (100, 64), (700, 96), (1024, 64), (4096, 8)])
+def test_fft_backend_columns(R, N, M):
+    """Batched FFT convolution (two paths per complex transform, radix-4/2
+    Stockham, FP32): X within 1e-5 of the FP64 convolution's term magnitude."""
+    H = 0.07
+    w, x, _ = R.debug_mixed_paths(0.04, [H], [1.5], [-0.7], [1.0], [1.0], N, M, seed=4, conv=R.CONV_FFT)
+    Z = R.generate_normals(4, M, N, precision=R.MIXED)
+    np.testing.assert_array_equal(w[:, :, :N].astype(np.float64), Z)
+    Xf, A = fp64_x(Z[:, 0, :], Z[:, 1, :], H, N)
+    err = np.abs(x[:, :N].astype(np.float64) - Xf)
+    assert np.max(err / (A + 1.0)) < 1e-5
+
+
+def test_fft_and_gemm_backends_agree(R):
+    c = CFG2
+    N, M = 512, 1 << 14
+    pg, sg, _ = R.price_rt(c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], N, M, seed=5, precision=R.MIXED,
+                           conv=R.CONV_GEMM, split=1)
+    pf, sf, _ = R.price_rt(c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], N, M, seed=5, precision=R.MIXED,
+                           conv=R.CONV_FFT)
+    assert np.all(np.abs(pg - pf) <= 2e-5 * pg)
+
+
+@pytest.mark.parametrize("N", [1024, 2048])
+def test_fft_prices_vs_fp64_identical_normals(R, N):
+    H, eta, rho, xi, T = [0.1], [1.5], [-0.7], 0.04, 2.0
+    K = list(np.linspace(0.5, 1.5, 11))
+    M = 1 << 12
+    mp, ms, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=3, precision=R.MIXED)
+    fp, fs, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=3, normals=R.NORMALS_F32)
+    err = np.abs(mp - fp)
+    assert np.all(err <= 1e-4 * fp)
+    assert np.all(err < 0.2 * fs)
