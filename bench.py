@@ -36,6 +36,10 @@ WORKLOADS = {
     "mixed-n512-m4m-21k": dict(xi=0.235 ** 2, H=[0.1], eta=[1.9], rho=[-0.9], T=[1.0] * 21,
                                K=[round(float(k), 10) for k in np.linspace(0.6, 1.4, 21)], N=512, M=1 << 22,
                                seed=11),
+    # long-horizon crossover sweep shape: three H, T = 2, 11 strikes on [0.5, 1.5], M = 2^20, seed 3
+    "mixed-crossover-m1m-11k": dict(xi=0.04, H=[0.03, 0.1, 0.4], eta=[1.5] * 3, rho=[-0.7] * 3, T=[2.0] * 11,
+                                    K=[round(float(k), 10) for k in np.linspace(0.5, 1.5, 11)], N=1024,
+                                    M=1 << 20, seed=3),
     "fp64-n100-m64k-5k": dict(xi=0.235 ** 2, H=[0.07], eta=[1.9], rho=[-0.9], T=[1.0] * 5,
                               K=[0.8, 0.9, 1.0, 1.1, 1.2], N=100, M=1 << 16, seed=42),
 }
