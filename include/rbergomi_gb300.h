@@ -25,6 +25,7 @@
 #ifndef RBERGOMI_GB300_H
 #define RBERGOMI_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -172,6 +173,25 @@ void rbg_last_transfer_bytes(uint64_t* h2d, uint64_t* d2h);
  * per variance group and path (ivb: 2 * n_vgroups * M, [group][path][2]).
  * Any output pointer may be NULL. */
 int rbg_debug_mixed_paths(const rbg_params* p, const rbg_options* o, float* normals, float* x, float* ivb);
+
+/* Allocation-free pricing.  No counterpart in the reference (it has no GPU).
+ * For callers that cannot call cudaMalloc -- a host that reserved all device
+ * memory for its own pool at start-up, or a latency-critical loop that cannot
+ * take cudaMalloc's device-wide synchronisation.  Same arguments, kernels and
+ * results as rbg_price_rt, mixed precision only (RBG_ERR_UNSUPPORTED
+ * otherwise), but every scratch buffer lives in one 16 MiB file-scope device
+ * array (rbg_static_scratch_bytes()) that each GPU loading the library holds
+ * until exit; no device memory is allocated or freed.  Limits: at most 4096
+ * outputs, and the job's tables must fit the array (RBG_ERR_ARG with a
+ * message from rbg_static_last_error() otherwise); M is unbounded (paths are
+ * processed in batches that fit).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and should come before any
+ * stream capture.  All calls share the array and see the previous call's
+ * contents; each call clears what must start at zero.  Calls that overlap on
+ * the GPU race on the array: serialise them. */
+int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv);
+size_t rbg_static_scratch_bytes(void);
+const char* rbg_static_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -25,7 +25,7 @@ def R():
 def declared_functions():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:void|int|const char\s*\*|uint64_t)\s*\**\s*(\w+)\s*\(", src, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:void|int|const char\s*\*|uint64_t|size_t)\s*\**\s*(\w+)\s*\(", src, flags=re.M)))
 
 
 def test_library_exports_every_declared_symbol(R):

@@ -1,0 +1,73 @@
+"""The allocation-free entry point rbg_price_rt_static, through the C ABI.
+
+It serves callers that cannot call cudaMalloc (a host that pre-reserved all
+device memory for its own pool, or a latency-critical loop that cannot take
+cudaMalloc's device-wide synchronisation).  Its results must match the
+regular entry point rbg_price_rt on the same inputs, on two calls in a row
+(the shared static scratch keeps the previous call's contents, so a second
+call checks that everything that must start at zero is cleared).
+
+This file is collected last so that a run stopping at the first failure has
+already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12  # same kernels, same batching of the Philox stream: roundoff only
+
+
+@pytest.fixture(scope="module")
+def R():
+    import rbergomi_gb300 as R
+    L = R.lib()
+    L.rbg_price_rt_static.argtypes = [C.POINTER(R.RbgParams), C.POINTER(R.RbgOptions), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.rbg_price_rt_static.restype = C.c_int
+    L.rbg_static_last_error.restype = C.c_char_p
+    L.rbg_static_scratch_bytes.restype = C.c_size_t
+    return R
+
+
+def static_price(R, xi, H, eta, rho, T, K, N, M, **opts):
+    p = R._Params(xi, H, eta, rho, T, K, N, M)
+    o = R.options(precision=R.MIXED, **opts)
+    price, stat, iv = np.empty(p.out), np.empty(p.out), np.empty(p.out)
+    dp = C.POINTER(C.c_double)
+    rc = R.lib().rbg_price_rt_static(C.byref(p.s), C.byref(o), price.ctypes.data_as(dp), stat.ctypes.data_as(dp),
+                                     iv.ctypes.data_as(dp))
+    if rc != 0:
+        raise R.RbgError(f"static entry point status {rc}: {R.lib().rbg_static_last_error().decode()}")
+    return price, stat, iv
+
+
+CASES = [
+    # workload-2 shape, reduced M
+    dict(xi=0.235 ** 2, H=[0.1], eta=[1.9], rho=[-0.9], T=[1.0] * 21, K=list(np.linspace(0.6, 1.4, 21)), N=512,
+         M=(1 << 18) + 77, seed=11),
+    # two Volterra passes, several variance groups, long horizon (FFT backend)
+    dict(xi=0.04, H=[0.07, 0.3], eta=[1.5, 2.0], rho=[-0.7, -0.5], T=[0.5, 2.0], K=[0.9, 1.2], N=1024, M=5000,
+         seed=3),
+]
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_static_entry_point_matches_regular(R, case):
+    c = dict(CASES[case])
+    seed = c.pop("seed")
+    args = (c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], c["N"], c["M"])
+    want_p, want_s, want_iv = R.price_rt(*args, seed=seed, precision=R.MIXED)
+    for _ in range(2):  # second call runs on the contents the first call left behind
+        p, s, iv = static_price(R, *args, seed=seed)
+        np.testing.assert_allclose(p, want_p, rtol=RTOL, atol=0)
+        np.testing.assert_allclose(s, want_s, rtol=1e-9, atol=0)
+        np.testing.assert_allclose(iv, want_iv, rtol=1e-9, atol=0)
+
+
+def test_static_entry_point_rejects_oversize(R):
+    assert R.lib().rbg_static_scratch_bytes() == 16 << 20
+    with pytest.raises(R.RbgError, match="4096 outputs"):
+        static_price(R, 0.04, [0.1] * 70, [1.5] * 70, [-0.7] * 70, [1.0] * 60, [1.0] * 60, 64, 1024)
