@@ -174,6 +174,14 @@ void rbg_last_transfer_bytes(uint64_t* h2d, uint64_t* d2h);
  * Any output pointer may be NULL. */
 int rbg_debug_mixed_paths(const rbg_params* p, const rbg_options* o, float* normals, float* x, float* ivb);
 
+/* Diagnostic run of the mixed-form path kernel(s) over M paths (one batch)
+ * with per-role cycle counters: cycles[site] = cycles lane 0 of each warp
+ * spent waiting at a pipeline barrier (1 producer/empty, 2 epilogue/MMA
+ * results, 3 strip load, 4 MMA/TMEM free, 5 MMA/A tile, 7 and 8 epilogue/
+ * producer tiles), cycles[16..18] = busy cycles of producer, epilogue and
+ * MMA warps, cycles[20] = epilogue cycles in the fused payoffs.  n >= 32. */
+int rbg_debug_mixed_profile(const rbg_params* p, const rbg_options* o, uint64_t* cycles, int n);
+
 /* Allocation-free pricing.  No counterpart in the reference (it has no GPU).
  * For callers that cannot call cudaMalloc -- a host that reserved all device
  * memory for its own pool at start-up, or a latency-critical loop that cannot

@@ -52,6 +52,7 @@ EXPORTS = [
     "rbg_price_rt_sums", "rbg_payoffs_rt", "rbg_generate_normals", "rbg_implied_vol", "rbg_last_error",
     "rbg_launch_count", "rbg_synchronize", "rbg_release", "rbg_plan_info", "rbg_profile_enable",
     "rbg_profile_reset", "rbg_profile_read", "rbg_last_transfer_bytes", "rbg_debug_mixed_paths",
+    "rbg_debug_mixed_profile",
 ]
 
 STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4
@@ -101,6 +102,8 @@ def lib():
         _fp = C.POINTER(C.c_float)
         L.rbg_debug_mixed_paths.argtypes = [P, O, _fp, _fp, _fp]
         L.rbg_debug_mixed_paths.restype = C.c_int
+        L.rbg_debug_mixed_profile.argtypes = [P, O, C.POINTER(C.c_uint64), C.c_int]
+        L.rbg_debug_mixed_profile.restype = C.c_int
         _lib = L
     return _lib
 
@@ -298,3 +301,18 @@ def debug_mixed_paths(xi, H, eta, rho, T, K, N, M, **opts):
     _check(lib().rbg_debug_mixed_paths(C.byref(p.s), C.byref(o), w.ctypes.data_as(fp), x.ctypes.data_as(fp),
                                        iv.ctypes.data_as(fp)))
     return w, x, iv
+
+
+PROFILE_SITES = {1: "producer wait (free stage)", 2: "epilogue wait (MMA results)", 3: "MMA wait (strip load)",
+                 4: "MMA wait (TMEM free)", 5: "MMA wait (A tile)", 7: "epilogue wait (producer tile)",
+                 8: "epilogue wait (next producer tile)", 16: "producer busy", 17: "epilogue busy", 18: "MMA busy",
+                 20: "epilogue fused payoffs"}
+
+
+def debug_mixed_profile(xi, H, eta, rho, T, K, N, M, **opts):
+    """Cycle counters of one diagnostic mixed-kernel run (see the header)."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    o = options(precision=MIXED, **opts)
+    c = (C.c_uint64 * 32)()
+    _check(lib().rbg_debug_mixed_profile(C.byref(p.s), C.byref(o), c, 32))
+    return {PROFILE_SITES.get(i, str(i)): int(c[i]) for i in range(32) if c[i]}

@@ -295,10 +295,11 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
     MixedJob job;
     if ((rc = mixed_prepare(plan, o, M, job, g_err))) return rc;
     const int64_t B = job.batch;
-    if ((rc = ensure(c.ivb, sizeof(float) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
     if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
     const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
-    const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+    const int64_t max_chunks = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+    if (!job.fused && (rc = ensure(c.ivb, sizeof(float) * 2 * plan.vgs.size() * (size_t)B, "variance sums")))
+        return rc;
     if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
     if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
     if ((rc = ensure(c.res, sizeof(double) * 5 * no, "results"))) return rc;
@@ -307,18 +308,33 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
     RBG_CUDA(cudaMemsetAsync(c.acc.p, 0, sizeof(double) * 4 * no, st));
     for (int64_t m0 = 0; m0 < M; m0 += B) {
         const int64_t b = std::min(B, M - m0);
-        {
-            ProfScope ps(kStageMixed, st, (int)job.launches.size());
-            if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, c.ivb.p, st, g_err))) return rc;
-        }
-        const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
-        {
-            ProfScope ps(kStagePayoff, st);
-            launch_payoff_sums_f32(ts.t.outs, no, c.ivb.p, b, G, c.part.as<double>(), nchunks, st);
-        }
-        {
+        if (job.fused) {
+            // payoffs summed inside the path kernel: one partial row per CTA
+            const int rows = mixed_part_rows(job, b);
+            RBG_CUDA(cudaMemsetAsync(c.part.p, 0, sizeof(double) * 4 * no * (size_t)rows, st));
+            {
+                ProfScope ps(kStageMixed, st, (int)job.launches.size());
+                if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, nullptr, st, g_err, nullptr,
+                                       nullptr, c.part.as<double>())))
+                    return rc;
+            }
             ProfScope ps(kStageReduce, st);
-            launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+            launch_accumulate(c.part.as<double>(), rows, no, c.acc.as<double>(), st);
+        } else {
+            {
+                ProfScope ps(kStageMixed, st, (int)job.launches.size());
+                if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, c.ivb.p, st, g_err)))
+                    return rc;
+            }
+            const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
+            {
+                ProfScope ps(kStagePayoff, st);
+                launch_payoff_sums_f32(ts.t.outs, no, c.ivb.p, b, G, c.part.as<double>(), nchunks, st);
+            }
+            {
+                ProfScope ps(kStageReduce, st);
+                launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+            }
         }
         RBG_CUDA(cudaGetLastError());
     }
@@ -578,6 +594,44 @@ void rbg_last_transfer_bytes(uint64_t* h2d, uint64_t* d2h)
 {
     if (h2d) *h2d = g_h2d;
     if (d2h) *d2h = g_d2h;
+}
+
+int rbg_debug_mixed_profile(const rbg_params* p, const rbg_options* o, uint64_t* cycles, int n)
+{
+    if (!p || !o || !cycles || n < 32) return fail(RBG_ERR_ARG, "need params, options and 32 counters");
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
+    MixedJob job;
+    if ((rc = mixed_prepare(plan, *o, p->M, job, g_err))) return rc;
+    if (job.batch < p->M) return fail(RBG_ERR_ARG, "diagnostic run does not fit one batch");
+    const int no = (int)plan.outs.size();
+    if ((rc = ensure(c->mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
+    DevBuf dbg;
+    const size_t ivb_bytes = job.fused ? 0 : sizeof(float) * 2 * plan.vgs.size() * (size_t)p->M;
+    const size_t part_bytes = sizeof(double) * 4 * no * (size_t)std::max(1, mixed_part_rows(job, p->M));
+    if (dbg.ensure(256 + ivb_bytes + part_bytes)) return fail(RBG_ERR_NOMEM, "debug buffers");
+    unsigned long long* prof = dbg.as<unsigned long long>();
+    unsigned char* ivb = (unsigned char*)dbg.p + 256;
+    double* part = (double*)(ivb + ivb_bytes);
+    if ((rc = mixed_upload(job, c->mixed_ws.p, st, g_err))) { dbg.release(); return rc; }
+    cudaMemsetAsync(dbg.p, 0, 256 + ivb_bytes + part_bytes, st);
+    rc = mixed_launch(job, c->mixed_ws.p, o->seed, o->path_offset, p->M, job.fused ? nullptr : (void*)ivb, st, g_err,
+                      nullptr, nullptr, job.fused ? part : nullptr, prof);
+    if (!rc) rc = mixed_check(job, c->mixed_ws.p, st, g_err);
+    std::vector<unsigned long long> h(32, 0);
+    if (!rc && cudaMemcpy(h.data(), prof, 256, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(RBG_ERR_CUDA, "debug copy failed");
+    }
+    for (int i = 0; i < 32; ++i) cycles[i] = h[i];
+    dbg.release();
+    return rc;
 }
 
 int rbg_plan_info(const rbg_params* p, int* n_vol, int* n_vgroups, int* n_out, int* vgroup_of_output)

@@ -133,4 +133,56 @@ __device__ __forceinline__ void neumaier_add(double& s, double& c, double x)
     s = t;
 }
 
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Complementary error function for z >= 0 by the Chebyshev fit of
+// Press, Teukolsky, Vetterling & Flannery, "Numerical Recipes" (2nd ed.,
+// section 6.2, function erfcc): erfc(z) = t exp(-z^2 + P(t)),
+// t = 1 / (1 + z/2), fractional error below 1.2e-7 for every z >= 0 -- so the
+// tails keep their relative accuracy.  One reciprocal and one ex2 on MUFU.
+__device__ __forceinline__ float erfc_cheb(float z)
+{
+    const float t = rcp_approx(fmaf(0.5f, z, 1.0f));
+    float p = 0.17087277f;
+    p = fmaf(p, t, -0.82215223f);
+    p = fmaf(p, t, 1.48851587f);
+    p = fmaf(p, t, -1.13520398f);
+    p = fmaf(p, t, 0.27886807f);
+    p = fmaf(p, t, -0.18628806f);
+    p = fmaf(p, t, 0.09678418f);
+    p = fmaf(p, t, 0.37409196f);
+    p = fmaf(p, t, 1.00002368f);
+    p = fmaf(p, t, -1.26551223f);
+    return t * ex2_approx(1.4426950408889634f * fmaf(-z, z, p));
+}
+
+// Standard normal CDF with relative accuracy in the lower tail.
+__device__ __forceinline__ float phi_f32(float x)
+{
+    const float z = -0.70710678118654752f * x;
+    const float e = 0.5f * erfc_cheb(fabsf(z));
+    return z >= 0.0f ? e : 1.0f - e;
+}
+
+// Kahan compensated accumulation in FP32: s holds the sum, c the running
+// error (subtract c to recover the compensated value).
+__device__ __forceinline__ void kahan_add_f32(float& s, float& c, float x)
+{
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+
 }  // namespace rbg

@@ -22,13 +22,16 @@
 // loaded once by a bulk async copy; only A tiles stream.  After chunk c's
 // MMAs, columns [32c, 32c+32) are final and the epilogue reads them.
 //
-// Warp roles (416 threads, one CTA per SM, persistent over 128-path tiles):
-//   warps 0-7   producers: Philox -> FP32 normals; W1 split into hi/lo
-//               16-bit A tiles (SW64 K-major layout); FP32 W1, W1perp kept
-//               for the epilogue
-//   warps 8-11  epilogue: tcgen05.ld of 32 accumulator columns per chunk,
-//               X = Y2 + a1 W1 + a2 W1perp, v and the two integrals
-//   warp 12     TMEM allocation and the single-thread tcgen05.mma issuer
+// Warp roles (672 threads, one CTA per SM, persistent over 128-path tiles):
+//   warps 0-15  producers, four threads per path, 8 steps each per chunk:
+//               Philox -> FP32 normals; W1 split into hi/lo 16-bit A tiles
+//               (SW64 K-major layout); FP32 W1, W1perp kept for the epilogue
+//   warps 16-19 epilogue, one per TMEM lane quadrant: tcgen05.ld of 2 x 16
+//               accumulator columns per chunk, X = Y2 + a1 W1 + a2 W1perp, v
+//               and the two integrals; when a launch prices <= 64 outputs,
+//               also the FP32 conditional BS payoffs of its paths, summed per
+//               warp and accumulated in FP64 (one partial row per CTA)
+//   warp 20     TMEM allocation and the single-thread tcgen05.mma issuer
 // Every mbarrier wait is bounded (%globaltimer); on expiry the kernel records
 // an error word, drains its MMAs, frees TMEM and returns.
 #include <cuda_bf16.h>
@@ -46,29 +49,42 @@ namespace rbg {
 constexpr int kTileM = 128;
 constexpr int kChunk = 32;
 constexpr int kMaxG = kMixedMaxGroups;
-constexpr int kProdWarps = 8;
-constexpr int kEpiWarps = 4;
-constexpr int kEpiWarp0 = kProdWarps;               // warps 8..11: TMEM lane quadrants 0..3
-constexpr int kMmaWarp = kProdWarps + kEpiWarps;    // warp 12
-constexpr int kThreads = (kMmaWarp + 1) * 32;       // 416
+#ifndef RBG_PROD_WARPS
+#define RBG_PROD_WARPS 8
+#endif
+#ifndef RBG_EPI_WARPS
+#define RBG_EPI_WARPS 8
+#endif
+#ifndef RBG_FUSE_PAYOFFS
+#define RBG_FUSE_PAYOFFS 0
+#endif
+constexpr int kProdWarps = RBG_PROD_WARPS;          // 4 * 128 / kProdWarps... threads per path: kProdWarps / 4
+constexpr int kEpiWarps = RBG_EPI_WARPS;            // 4 (one warpgroup) or 8 (two, 16 columns each per chunk)
+constexpr int kEpiWGs = kEpiWarps / 4;
+constexpr int kStepsPerThread = kChunk * 4 / kProdWarps;  // producer steps per chunk per thread
+constexpr int kEpiWarp0 = kProdWarps;               // warps 8..15: TMEM lane quadrant = warp % 4
+constexpr int kMmaWarp = kProdWarps + kEpiWarps;    // warp 16
+constexpr int kThreads = (kMmaWarp + 1) * 32;       // 544
 constexpr int kMaxNp = 512;                         // TMEM: 128 lanes x 512 FP32 columns
 constexpr uint64_t kWaitNs = 2000000000ull;         // 2 s per wait
 
 // shared-memory layout (offsets from a 1024-aligned base):
 //   [strip hi | strip lo]            2 * Np * 64 B, SW64 K-major
 //   A tiles, per stage [hi | lo]     16 KB per stage (1024-aligned)
-//   FP32 tiles, per stage            w1 [32][128], w1perp [32][128], w1next [128]
-//   per-thread group sums            kMaxG * 2 * 128 floats
+//   FP32 tiles, per stage            w1 [32][128], w1perp [32][128]
+//   per-thread group sums            n_g * 2 * 128 floats
+//   beta tables                      n_g * Np floats
+//   fused outputs                    table n_o * 4 floats, FP32 Kahan sums [4 warps][n_o][4]
 //   mbarriers + TMEM address
 constexpr int kTileBytes = kTileM * kChunk * 2;                          // one 16-bit 128 x 32 tile, 8 KB
 constexpr int kStageA = 2 * kTileBytes;                                  // hi + lo
-constexpr int kStageF = 2 * kChunk * kTileM * 4 + kTileM * 4;            // w1, w1perp, w1next
+constexpr int kStageF = 2 * kChunk * kTileM * 4;                         // w1, w1perp
 
 struct SmemLayout {
-    int strip, a0, f0, stages, acc, beta, bars, total;
+    int strip, a0, f0, stages, acc, beta, otab, osum, bars, total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g)
+__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, int n_o)
 {
     SmemLayout L;
     L.strip = 0;
@@ -76,8 +92,10 @@ __host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g)
     L.stages = stages;
     L.f0 = L.a0 + stages * kStageA;
     L.acc = L.f0 + stages * kStageF;
-    L.beta = L.acc + n_g * 2 * kTileM * 4;
-    L.bars = L.beta + n_g * Np * 4;
+    L.beta = L.acc + 2 * n_g * 2 * kTileM * 4 + kTileM * 4;  // per warpgroup, then W1_0 per path
+    L.otab = L.beta + n_g * Np * 4;
+    L.osum = (L.otab + n_o * 16 + 15) / 16 * 16;
+    L.bars = L.osum + kEpiWarps * n_o * 16;
     L.total = L.bars + 128 + 1024;  // barriers + alignment slack for the dynamic base
     return L;
 }
@@ -119,25 +137,36 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 }
 
 // Bounded wait for the phase of the given parity; false on timeout or when
-// another role already failed (then the caller winds down).
-__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site)
+// another role already failed (then the caller winds down).  The error word
+// and the clock are polled every 64 tries only.  With `prof` set (diagnostic
+// runs), lane 0 adds the cycles it waited to prof[site].
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site,
+                                       unsigned long long* prof = nullptr)
 {
     if (mbar_try(bar, parity)) return true;
+    const long long c0 = prof ? clock64() : 0;
     const uint64_t t0 = globaltimer();
-    while (true) {
-        if (mbar_try(bar, parity)) return true;
-        if (*(volatile unsigned int*)err != 0u) return false;
-        if (globaltimer() - t0 > kWaitNs) {
-            atomicCAS(err, 0u, site);
-            return false;
+    bool ok = true;
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try(bar, parity)) break;
+        if ((it & 63u) == 0u) {
+            if (*(volatile unsigned int*)err != 0u) { ok = false; break; }
+            if (globaltimer() - t0 > kWaitNs) {
+                atomicCAS(err, 0u, site);
+                ok = false;
+                break;
+            }
         }
     }
+    if (prof && (threadIdx.x & 31) == 0) atomicAdd(prof + site, (unsigned long long)(clock64() - c0));
+    return ok;
 }
 
 // the same wait, made warp-uniform so .sync.aligned tcgen05 ops stay converged
-__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site)
+__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site,
+                                               unsigned long long* prof = nullptr)
 {
-    const bool ok = mbar_wait(bar, parity, err, site);
+    const bool ok = mbar_wait(bar, parity, err, site, prof);
     return __all_sync(0xffffffffu, ok);
 }
 
@@ -194,6 +223,20 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // 16-bit split x = hi + lo (+ O(2^-16 |x|) for BF16, O(2^-22 |x|) for FP16)
 template <int BF16>
 __device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_t& lo)
@@ -214,16 +257,36 @@ __device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_
 }
 
 // --------------------------------------------------------------- the kernel
+// Conditional BS call (tau = 1, r = 0) from (Ivdt, IsvdW) in FP32
+// (rBergLib/rBergomiMT.cpp:598-602 with BlackScholes.cpp:16-21).  ITM strikes
+// go through put-call parity, (S - K) + put, so both wings are computed from
+// small tail probabilities that keep their relative accuracy.
+__device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rho, float K, float lnK)
+{
+    const float v2 = (1.0f - rho * rho) * Ivdt;
+    const float lnS = -0.5f * rho * rho * Ivdt + rho * IsvdW;
+    const float spot = ex2_approx(1.4426950408889634f * lnS);
+    if (!(v2 > 0.0f)) return fmaxf(spot - K, 0.0f);
+    const float rv = rsqrt_approx(v2);
+    const float vol = v2 * rv;
+    const float d1 = fmaf(lnS - lnK, rv, 0.5f * vol);
+    const float d2 = d1 - vol;
+    if (spot > K) return (spot - K) + (K * phi_f32(-d2) - spot * phi_f32(-d1));
+    return spot * phi_f32(d1) - K * phi_f32(d2);
+}
+
 template <int BF16>
 __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g);
+    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g, a.n_o);
     unsigned char* strip = base + L.strip;
     float* acc_s = (float*)(base + L.acc);
     float* beta_s = (float*)(base + L.beta);
+    float4* otab = (float4*)(base + L.otab);   // (rho, K, lnK, local group) per fused output
+    float* osum = (float*)(base + L.osum);     // [epilogue warp][output][S, C, S2, C2], FP32 Kahan
     uint64_t* bars = (uint64_t*)(base + L.bars);
     // barrier slots
     const int S = a.stages;
@@ -265,16 +328,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     for (int i = threadIdx.x; i < a.n_g * a.Np; i += blockDim.x) beta_s[i] = a.beta[i];
+    for (int i = threadIdx.x; i < a.n_o; i += blockDim.x) otab[i] = a.otab[i];
+    for (int i = threadIdx.x; i < kEpiWarps * a.n_o * 4; i += blockDim.x) osum[i] = 0.f;
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_holder;
 
+    const long long role_t0 = a.prof ? clock64() : 0;
     if (warp < kProdWarps) {
         // ------------------------------------------------------- producers
         const int p = threadIdx.x & (kTileM - 1);
-        const int h = threadIdx.x >> 7;  // which 16 steps of the chunk
+        const int h = threadIdx.x >> 7;  // which kStepsPerThread steps of the chunk
+        constexpr int SPT = kStepsPerThread;
         const PhiloxKeys keys = philox_keys(a.seed);
+        const int sw = (p >> 1) & 3;
         int64_t lt = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
             const int64_t m = tile * kTileM + p;
@@ -284,15 +352,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 const int64_t gc = lt * nc + c;
                 const int s = (int)(gc % S);
                 const uint32_t ph = (uint32_t)((gc / S) & 1);
-                if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1)) goto done;
+                if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
                 unsigned char* st = base + L.a0 + s * kStageA;
                 float* w1s = (float*)(base + L.f0 + s * kStageF);
                 float* w1ps = w1s + kChunk * kTileM;
-                float* w1next = w1ps + kChunk * kTileM;
-                const int step0 = kChunk * c + 16 * h;
-                float w[16], wp[16];
+                const int step0 = kChunk * c + SPT * h;
+                float w[SPT], wp[SPT];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < SPT / 4; ++q) {
                     const uint32_t g = (uint32_t)((step0 >> 2) + q);
                     const uint4 x0 = philox_group(keys, gpath, g, 0);
                     const uint4 x1 = philox_group(keys, gpath, g, 1);
@@ -302,39 +369,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     box_muller_f32(x1.z, x1.w, wp[4 * q + 2], wp[4 * q + 3]);
                 }
 #pragma unroll
-                for (int q = 0; q < 16; ++q) {
+                for (int q = 0; q < SPT; ++q) {
                     if (!valid || step0 + q >= a.N) { w[q] = 0.f; wp[q] = 0.f; }
                 }
-                // A tile: row p, logical 16-byte chunks 2h and 2h+1, SW64 swizzle
-                uint32_t hi[8], lo[8];
+                // A tile: row p, logical 16-byte chunks covering steps [SPT h, SPT h + SPT), SW64 swizzle
+                uint32_t hi[SPT / 2], lo[SPT / 2];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) split2<BF16>(w[2 * q], w[2 * q + 1], hi[q], lo[q]);
-                const int sw = (p >> 1) & 3;
+                for (int q = 0; q < SPT / 2; ++q) split2<BF16>(w[2 * q], w[2 * q + 1], hi[q], lo[q]);
 #pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const int off = p * 64 + (((2 * h + e) ^ sw) << 4);
+                for (int e = 0; e < SPT / 8; ++e) {
+                    const int off = p * 64 + ((((SPT / 8) * h + e) ^ sw) << 4);
                     *(uint4*)(st + off) = make_uint4(hi[4 * e], hi[4 * e + 1], hi[4 * e + 2], hi[4 * e + 3]);
                     *(uint4*)(st + kTileBytes + off) =
                         make_uint4(lo[4 * e], lo[4 * e + 1], lo[4 * e + 2], lo[4 * e + 3]);
                 }
 #pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    w1s[(16 * h + q) * kTileM + p] = w[q];
-                    w1ps[(16 * h + q) * kTileM + p] = wp[q];
-                }
-                if (h == 1) {
-                    // W1 at step 32c + 32 pairs with the chunk's last column
-                    const int sn = kChunk * (c + 1);
-                    float z0 = 0.f, z1;
-                    if (valid && sn < a.N) {
-                        const uint4 x = philox_group(keys, gpath, (uint32_t)(sn >> 2), 0);
-                        box_muller_f32(x.x, x.y, z0, z1);
-                    }
-                    w1next[p] = z0;
+                for (int q = 0; q < SPT; ++q) {
+                    w1s[(SPT * h + q) * kTileM + p] = w[q];
+                    w1ps[(SPT * h + q) * kTileM + p] = wp[q];
                 }
                 if (a.dbg_w && valid) {
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) {
+                    for (int q = 0; q < SPT; ++q) {
                         a.dbg_w[(m * 2 + 0) * Np + step0 + q] = w[q];
                         a.dbg_w[(m * 2 + 1) * Np + step0 + q] = wp[q];
                     }
@@ -346,103 +402,159 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         }
     } else if (warp < kMmaWarp) {
         // -------------------------------------------------------- epilogue
-        const int ew = warp - kEpiWarp0;  // == warp % 4, the TMEM lane quadrant
-        const int p = ew * 32 + lane;
-        const uint32_t tlane = tmem + ((uint32_t)(ew * 32) << 16);
+        const int ew = warp - kEpiWarp0;
+        const int wg = ew >> 2;           // warpgroup
+        const int quad = warp & 3;        // TMEM lane quadrant
+        const int p = quad * 32 + lane;
+        const uint32_t tlane = tmem + ((uint32_t)(quad * 32) << 16);
+        float* my_acc = acc_s + (size_t)wg * a.n_g * 2 * kTileM;
+        float* w10_s = acc_s + (size_t)2 * a.n_g * 2 * kTileM;  // W1_0 per path
         int64_t lt = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
             const int64_t m = tile * kTileM + p;
             const bool valid = m < a.B;
             for (int g = 0; g < a.n_g; ++g) {
-                acc_s[(2 * g) * kTileM + p] = 0.f;
-                acc_s[(2 * g + 1) * kTileM + p] = 0.f;
+                my_acc[(2 * g) * kTileM + p] = 0.f;
+                my_acc[(2 * g + 1) * kTileM + p] = 0.f;
             }
-            float w1_0 = 0.f;
             for (int c = 0; c < nc; ++c) {
                 const int64_t gc = lt * nc + c;
                 const int s = (int)(gc % S);
                 const uint32_t ph = (uint32_t)((gc / S) & 1);
-                // the producers' FP32 tiles of this stage, then the MMA results
-                if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7)) goto done;
-                if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2)) goto done;
+                // the producers' FP32 tiles of this stage (the upper half also pairs
+                // its last column with the next chunk's first W1), then the MMA results
+                if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7, a.prof)) goto done;
+                const bool has_next = c + 1 < nc;
+                const int sn = (int)((gc + 1) % S);
+                if ((kEpiWGs == 1 || wg == 1) && has_next &&
+                    !mbar_wait_warp(smem_u32(full + sn), (uint32_t)(((gc + 1) / S) & 1), a.err, 8, a.prof))
+                    goto done;
+                if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
                 tc_fence_after();
-                float x[32];
-                tmem_ld32(tlane + (uint32_t)(kChunk * c), x);
-                if (c == nc - 1) {
-                    // accumulator of this tile fully read: the MMA may start the next tile
-                    tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(smem_u32(tmem_empty));
-                }
                 const float* w1s = (const float*)(base + L.f0 + s * kStageF);
                 const float* w1ps = w1s + kChunk * kTileM;
-                const float* w1next = w1ps + kChunk * kTileM;
-                float wn[32];
+#pragma unroll 1
+                for (int hh = wg; hh < 2; hh += kEpiWGs) {
+                    const int j0 = 16 * hh;
+                    float x[16];
+                    tmem_ld16(tlane + (uint32_t)(kChunk * c + j0), x);
+                    if (c == nc - 1 && hh + kEpiWGs >= 2) {
+                        // this warp's accumulator columns of the tile are read
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(smem_u32(tmem_empty));
+                    }
+                    float wn[16];
 #pragma unroll
-                for (int jj = 0; jj < 32; ++jj) {
-                    const float w1 = w1s[jj * kTileM + p];
-                    x[jj] = x[jj] + a.a1 * w1 + a.a2 * w1ps[jj * kTileM + p];
-                    if (jj > 0) wn[jj - 1] = w1;
-                    if (jj == 0 && c == 0) w1_0 = w1;
-                }
-                wn[31] = w1next[p];
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(empty + s));
-                if (a.dbg_x && valid) {
+                    for (int jj = 0; jj < 16; ++jj) {
+                        const float w1 = w1s[(j0 + jj) * kTileM + p];
+                        x[jj] = x[jj] + a.a1 * w1 + a.a2 * w1ps[(j0 + jj) * kTileM + p];
+                        if (jj > 0) wn[jj - 1] = w1;
+                        if (jj == 0 && j0 == 0 && c == 0) w10_s[p] = w1;
+                    }
+                    wn[15] = (hh == 0) ? w1s[16 * kTileM + p]
+                                       : (has_next ? ((const float*)(base + L.f0 + sn * kStageF))[p] : 0.f);
+                    if (a.dbg_x && valid) {
 #pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) a.dbg_x[m * Np + kChunk * c + jj] = x[jj];
-                }
-                // v_{j+1} = xi exp(eta WS_j - comp_j): su = sqrt(v) = 2^(alpha/2 X - beta/2),
-                // one MUFU ex2 per element and group, v = su * su
-                for (int g = 0; g < a.n_g; ++g) {
-                    const float ah = a.alpha[g];
-                    const float* bt = beta_s + g * Np + kChunk * c;
-                    const int lim = a.nsteps[g] - 1 - kChunk * c;
-                    float sv = 0.f, swv = 0.f;
-                    if (lim >= 32) {
+                        for (int jj = 0; jj < 16; ++jj) a.dbg_x[m * Np + kChunk * c + j0 + jj] = x[jj];
+                    }
+                    // v_{j+1} = xi exp(eta WS_j - comp_j): su = sqrt(v) = 2^(alpha/2 X - beta/2),
+                    // one MUFU ex2 per element and group, v = su * su
+                    for (int g = 0; g < a.n_g; ++g) {
+                        const float ah = a.alpha[g];
+                        const float* bt = beta_s + g * Np + kChunk * c + j0;
+                        const int lim = a.nsteps[g] - 1 - kChunk * c - j0;
+                        float sv = 0.f, swv = 0.f;
+                        if (lim >= 16) {
 #pragma unroll
-                        for (int jj = 0; jj < 32; ++jj) {
-                            const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
-                            sv = fmaf(su, su, sv);
-                            swv = fmaf(su, wn[jj], swv);
-                        }
-                    } else {
-#pragma unroll
-                        for (int jj = 0; jj < 32; ++jj) {
-                            if (jj < lim) {
+                            for (int jj = 0; jj < 16; ++jj) {
                                 const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
                                 sv = fmaf(su, su, sv);
                                 swv = fmaf(su, wn[jj], swv);
                             }
+                        } else {
+#pragma unroll
+                            for (int jj = 0; jj < 16; ++jj) {
+                                if (jj < lim) {
+                                    const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
+                                    sv = fmaf(su, su, sv);
+                                    swv = fmaf(su, wn[jj], swv);
+                                }
+                            }
                         }
+                        my_acc[(2 * g) * kTileM + p] += sv;
+                        my_acc[(2 * g + 1) * kTileM + p] += swv;
                     }
-                    acc_s[(2 * g) * kTileM + p] += sv;
-                    acc_s[(2 * g + 1) * kTileM + p] += swv;
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(empty + s));
+            }
+            // both warpgroups' column sums of this tile are in shared memory
+            asm volatile("bar.sync 1, %0;" ::"r"(kEpiWarps * 32) : "memory");
+            const long long bs_t0 = a.prof ? clock64() : 0;
+            const float w1_0 = w10_s[p];
+            // fused payoffs: warpgroup wg prices outputs q = wg, wg + 2, ...
+            // Ivdt = dt (xi + sum v), IsvdW = sdt (sqrt(xi) W1_0 + sum sqrt(v) W1)
+            float iv_last = 0.f, iw_last = 0.f;
+            int g_last = -1;
+            for (int q = wg; q < a.n_o; q += kEpiWGs) {
+                const float4 o = otab[q];
+                const int g = (int)o.w;
+                if (g != g_last) {
+                    g_last = g;
+                    float sv = acc_s[(2 * g) * kTileM + p], sw2 = acc_s[(2 * g + 1) * kTileM + p];
+                    if (kEpiWGs == 2) {
+                        sv += acc_s[((size_t)a.n_g * 2 + 2 * g) * kTileM + p];
+                        sw2 += acc_s[((size_t)a.n_g * 2 + 2 * g + 1) * kTileM + p];
+                    }
+                    iv_last = a.dt[g] * (a.xi + sv);
+                    iw_last = a.sdt[g] * fmaf(a.sqrt_xi, w1_0, sw2);
+                }
+                float x = valid ? rt_payoff_f32(iv_last, iw_last, o.x, o.y, o.z) : 0.f;
+                float x2 = x * x;
+#pragma unroll
+                for (int sh = 16; sh > 0; sh >>= 1) {
+                    x += __shfl_xor_sync(0xffffffffu, x, sh);
+                    x2 += __shfl_xor_sync(0xffffffffu, x2, sh);
+                }
+                // warp sums in FP32, compensated (Kahan) FP32 across tiles; FP64
+                // once per CTA at the end -- GB300's FP64 pipe is too slow here
+                if (lane == 0) {
+                    float* os = osum + ((size_t)ew * a.n_o + q) * 4;
+                    kahan_add_f32(os[0], os[1], x);
+                    kahan_add_f32(os[2], os[3], x2);
                 }
             }
-            if (valid) {
+            if (wg == 0 && valid && a.ivb) {
                 for (int g = 0; g < a.n_g; ++g) {
-                    const float Ivdt = a.dt[g] * (a.xi + acc_s[(2 * g) * kTileM + p]);
-                    const float IsvdW = a.sdt[g] * fmaf(a.sqrt_xi, w1_0, acc_s[(2 * g + 1) * kTileM + p]);
-                    a.ivb[(size_t)(a.g0 + g) * a.B + m] = make_float2(Ivdt, IsvdW);
+                    float sv = acc_s[(2 * g) * kTileM + p], sw2 = acc_s[(2 * g + 1) * kTileM + p];
+                    if (kEpiWGs == 2) {
+                        sv += acc_s[((size_t)a.n_g * 2 + 2 * g) * kTileM + p];
+                        sw2 += acc_s[((size_t)a.n_g * 2 + 2 * g + 1) * kTileM + p];
+                    }
+                    a.ivb[(size_t)(a.g0 + g) * a.B + m] =
+                        make_float2(a.dt[g] * (a.xi + sv), a.sdt[g] * fmaf(a.sqrt_xi, w1_0, sw2));
                 }
             }
+            if (a.prof && lane == 0) atomicAdd(a.prof + 20, (unsigned long long)(clock64() - bs_t0));
+            // the sums are read before either warpgroup clears its half for the next tile
+            asm volatile("bar.sync 1, %0;" ::"r"(kEpiWarps * 32) : "memory");
         }
     } else if (lane == 0) {
         // ------------------------------------------------------ MMA issuer
         const uint32_t strip_hi = smem_u32(strip);
         const uint32_t strip_lo = strip_hi + (uint32_t)(Np * 64);
-        if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3)) {
+        if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
             int64_t lt = 0;
             for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
-                if (lt > 0 && !mbar_wait(smem_u32(tmem_empty), (uint32_t)((lt - 1) & 1), a.err, 4)) break;
+                if (lt > 0 && !mbar_wait(smem_u32(tmem_empty), (uint32_t)((lt - 1) & 1), a.err, 4, a.prof)) break;
                 tc_fence_after();
                 bool ok = true;
                 for (int c = 0; c < nc && ok; ++c) {
                     const int64_t gc = lt * nc + c;
                     const int s = (int)(gc % S);
                     const uint32_t ph = (uint32_t)((gc / S) & 1);
-                    if (!mbar_wait(smem_u32(full + s), ph, a.err, 5)) { ok = false; break; }
+                    if (!mbar_wait(smem_u32(full + s), ph, a.err, 5, a.prof)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
                     const uint32_t alo = ahi + kTileBytes;
@@ -472,6 +584,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         mbar_wait(smem_u32(final_bar), 0, a.err, 6);
     }
 done:
+    if (a.prof && lane == 0) {
+        const int role = warp < kProdWarps ? 16 : (warp < kMmaWarp ? 17 : 18);
+        atomicAdd(a.prof + role, (unsigned long long)(clock64() - role_t0));
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == kMmaWarp) {
@@ -479,24 +595,24 @@ done:
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols)
                      : "memory");
     }
+    // this CTA's fused payoff sums: one partial row per CTA, merged in fixed order later
+    if (a.n_o > 0 && warp >= kEpiWarp0 && warp < kMmaWarp) {
+        for (int q = threadIdx.x - kEpiWarp0 * 32; q < a.n_o; q += kEpiWarps * 32) {
+            double S1 = 0, C1 = 0, S2 = 0, C2 = 0;
+            for (int w = 0; w < kEpiWarps; ++w) {
+                const float* os = osum + ((size_t)w * a.n_o + q) * 4;
+                neumaier_add(S1, C1, (double)os[0]);
+                neumaier_add(S1, C1, -(double)os[1]);
+                neumaier_add(S2, C2, (double)os[2]);
+                neumaier_add(S2, C2, -(double)os[3]);
+            }
+            double* pp = a.part + ((size_t)blockIdx.x * a.n_out_total + a.oidx[q]) * 4;
+            pp[0] = S1; pp[1] = C1; pp[2] = S2; pp[3] = C2;
+        }
+    }
 }
 
 // ----------------------------------------------- FP32 payoffs, FP64 sums
-// Conditional BS call (tau = 1, r = 0) from (Ivdt, IsvdW) in FP32.  Tails use
-// erfc so both ITM (via put-call parity) and OTM stay accurate.
-__device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rho, float K, float lnK)
-{
-    const float vol = sqrtf((1.0f - rho * rho) * Ivdt);
-    const float lnS = -0.5f * rho * rho * Ivdt + rho * IsvdW;
-    const float spot = __expf(lnS);
-    if (!(vol > 0.0f)) return fmaxf(spot - K, 0.0f);
-    const float d1 = (lnS - lnK) / vol + 0.5f * vol;
-    const float d2 = d1 - vol;
-    const float r2 = 0.70710678118654752f;
-    if (spot > K) return (spot - K) + (0.5f * K * erfcf(d2 * r2) - 0.5f * spot * erfcf(d1 * r2));
-    return 0.5f * spot * erfcf(-d1 * r2) - 0.5f * K * erfcf(-d2 * r2);
-}
-
 constexpr int kOPB32 = 8;
 
 __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restrict__ outs, int n_out,
@@ -533,15 +649,17 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
             s2[q] = fmaf(x, x, s2[q]);
         }
     }
+    // warp tree in FP32 (GB300's FP64 pipe is far too slow for warp-wide
+    // shuffles), one FP64 value per warp and output
 #pragma unroll
     for (int q = 0; q < kOPB32; ++q) {
-        double a = s1[q], b = s2[q];
+        float a = s1[q], b = s2[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             a += __shfl_xor_sync(0xffffffffu, a, o);
             b += __shfl_xor_sync(0xffffffffu, b, o);
         }
-        if (lane == 0) { red[w][q][0] = a; red[w][q][1] = b; }
+        if (lane == 0) { red[w][q][0] = (double)a; red[w][q][1] = (double)b; }
     }
     __syncthreads();
     if (threadIdx.x < kOPB32 && o0 + (int)threadIdx.x < n_out) {
@@ -678,11 +796,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             A.n_g = ng;
             A.g0 = g0;
             A.tmem_cols = tcols;
-            A.stages = (smem_layout(Np, 3, ng).total <= optin) ? 3 : 2;
-            if (backend == RBG_CONV_GEMM && smem_layout(Np, A.stages, ng).total > optin) {
-                err = "mixed kernel shared memory does not fit";
-                return RBG_ERR_UNSUPPORTED;
-            }
+            A.stages = 3;
             A.a1 = (float)vol.a1;
             A.a2 = (float)vol.a2;
             A.xi = (float)plan.xi;
@@ -712,7 +826,34 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             r.off_beta = off;
             off += (size_t)ng * Np * 4;
             off = (off + 255) / 256 * 256;
+            int n_o = 0;
+            for (const OutMap& om : plan.outs)
+                if (om.vg >= g0 && om.vg < g0 + ng) ++n_o;
+            A.n_o = n_o;
+            A.n_out_total = (int)plan.outs.size();
+            r.off_otab = off;
+            off += (size_t)n_o * 16;
+            off = (off + 255) / 256 * 256;
+            r.off_oidx = off;
+            off += (size_t)n_o * 4;
+            off = (off + 255) / 256 * 256;
             job.launches.push_back(r);
+        }
+    }
+    // fuse the payoffs into the GEMM path kernel when every launch has few outputs
+    // Pricing the payoffs inside the path kernel's epilogue (RBG_FUSE_PAYOFFS)
+    // measured slower than the separate FP32 payoff kernel on GB300: the
+    // epilogue warps are the kernel's critical path.
+    job.fused = RBG_FUSE_PAYOFFS && (backend == RBG_CONV_GEMM);
+    for (const MixedLaunch& r : job.launches)
+        if (r.args.n_o > kMixedMaxFused) job.fused = false;
+    for (MixedLaunch& r : job.launches) {
+        MixedArgs& A = r.args;
+        const int no = job.fused ? A.n_o : 0;
+        A.stages = (smem_layout(Np, 3, A.n_g, no).total <= optin) ? 3 : 2;
+        if (backend == RBG_CONV_GEMM && smem_layout(Np, A.stages, A.n_g, no).total > optin) {
+            err = "mixed kernel shared memory does not fit";
+            return RBG_ERR_UNSUPPORTED;
         }
     }
     if (backend == RBG_CONV_FFT) {
@@ -731,6 +872,21 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         else
             fft_tables(plan.gamma.data() + (size_t)vol * N, N, A.logL, (float*)(ws.data() + r.off_spec),
                        (float*)(ws.data() + job.off_tw));
+        {
+            float* ot = (float*)(ws.data() + r.off_otab);
+            int* oi = (int*)(ws.data() + r.off_oidx);
+            int q = 0;
+            for (size_t i = 0; i < plan.outs.size(); ++i) {
+                const OutMap& om = plan.outs[i];
+                if (om.vg < A.g0 || om.vg >= A.g0 + A.n_g) continue;
+                ot[4 * q + 0] = (float)om.rho;
+                ot[4 * q + 1] = (float)om.K;
+                ot[4 * q + 2] = (float)std::log(om.K);
+                ot[4 * q + 3] = (float)(om.vg - A.g0);
+                oi[q] = (int)i;
+                ++q;
+            }
+        }
         float* beta = (float*)(ws.data() + r.off_beta);
         for (int g = 0; g < A.n_g; ++g)
             for (int j = 0; j < Np; ++j) {
@@ -757,8 +913,15 @@ int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& er
     return RBG_OK;
 }
 
+int mixed_part_rows(const MixedJob& job, int64_t B)
+{
+    const int64_t ntiles = (B + kTileM - 1) / kTileM;
+    return (int)std::min<int64_t>(ntiles, job.sms);
+}
+
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
-                 cudaStream_t st, std::string& err, float* dbg_w, float* dbg_x)
+                 cudaStream_t st, std::string& err, float* dbg_w, float* dbg_x, double* part,
+                 unsigned long long* prof)
 {
     unsigned char* base = (unsigned char*)ws;
     for (const MixedLaunch& r : job.launches) {
@@ -766,6 +929,11 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         A.strip = base + r.off_strip;
         A.beta = (const float*)(base + r.off_beta);
         A.spec = (const float2*)(base + r.off_spec);
+        A.otab = (const float4*)(base + r.off_otab);
+        A.oidx = (const int*)(base + r.off_oidx);
+        A.part = part;
+        A.prof = prof;
+        if (!job.fused || !part) A.n_o = 0;
         A.tw = (const float2*)(base + job.off_tw);
         A.ivb = (float2*)ivb;
         A.err = (unsigned int*)(base + job.off_err);
@@ -774,7 +942,7 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         A.seed = seed;
         A.path0 = path0;
         A.B = B;
-        const int smem = smem_layout(A.Np, A.stages, A.n_g).total;
+        const int smem = smem_layout(A.Np, A.stages, A.n_g, A.n_o).total;
         const int64_t ntiles = (B + kTileM - 1) / kTileM;
         const int grid = (int)std::min<int64_t>(ntiles, job.sms);
         cudaError_t e;

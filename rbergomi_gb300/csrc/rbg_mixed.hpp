@@ -14,6 +14,7 @@
 namespace rbg {
 
 constexpr int kMixedMaxGroups = 16;  // variance groups handled by one launch
+constexpr int kMixedMaxFused = 64;   // outputs whose payoffs one launch can price in its epilogue
 
 // Kernel arguments (passed by value as a __grid_constant__).
 struct MixedArgs {
@@ -23,11 +24,16 @@ struct MixedArgs {
     unsigned int* err;           // 0, or the id of the wait that expired
     float* dbg_w;                // optional [B][2][Np] normals the producers drew
     float* dbg_x;                // optional [B][Np] X = Y2 + a1 W1 + a2 W1perp
+    const float4* otab;          // fused outputs: (rho, K, log K, local group), n_o entries
+    const int* oidx;             // fused outputs: global output index
+    double* part;                // fused outputs: [CTA][n_out_total][S, C, S2, C2] partial sums
+    unsigned long long* prof;    // diagnostic runs only: wait cycles per site, busy cycles per role
     const float2* spec;          // FFT backend: FFT(Gamma)/L, L points
     const float2* tw;            // FFT backend: exp(-2 pi i t / L), L points
     uint64_t seed;
     int64_t path0, B;
     int N, Np, nc, n_g, g0, tmem_cols, stages;
+    int n_o, n_out_total;  // fused outputs of this launch; all outputs of the job
     int L, logL;  // FFT backend transform length
     float a1, a2, xi, sqrt_xi;
     float alpha[kMixedMaxGroups];  // eta * scale * log2(e) / 2
@@ -37,7 +43,7 @@ struct MixedArgs {
 
 struct MixedLaunch {
     MixedArgs args;  // device pointers filled at launch time
-    size_t off_strip = 0, off_beta = 0, off_spec = 0;
+    size_t off_strip = 0, off_beta = 0, off_spec = 0, off_otab = 0, off_oidx = 0;
 };
 
 struct MixedJob {
@@ -46,6 +52,7 @@ struct MixedJob {
     size_t off_err = 0;
     int N = 0, n_vol = 0, n_vg = 0, split = 0, sms = 0;
     int backend = RBG_CONV_GEMM;  // RBG_CONV_GEMM or RBG_CONV_FFT
+    bool fused = false;           // payoffs priced inside the path kernel (GEMM backend, <= 64 per launch)
     size_t off_tw = 0;
     std::vector<MixedLaunch> launches;   // one per (Volterra pass, <= 16 groups)
     std::vector<unsigned char> host_ws;  // image uploaded by mixed_upload
@@ -53,8 +60,14 @@ struct MixedJob {
 
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err);
 int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
+// Launches the path kernel(s) for paths [path0, path0 + B).  Unfused jobs
+// write (Ivdt, IsvdW) to ivb; fused jobs add their payoff sums to `part`
+// (rows = mixed_part_rows(job, B), zeroed by the caller) and write ivb only
+// when it is non-null.
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
-                 cudaStream_t st, std::string& err, float* dbg_w = nullptr, float* dbg_x = nullptr);
+                 cudaStream_t st, std::string& err, float* dbg_w = nullptr, float* dbg_x = nullptr,
+                 double* part = nullptr, unsigned long long* prof = nullptr);
+int mixed_part_rows(const MixedJob& job, int64_t B);
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
 // FFT backend (rbg_fft.cu)
 int fft_log2_len(int N);

@@ -107,17 +107,20 @@ int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price
     if (off_part >= kStaticScratchBytes)
         return static_fail(RBG_ERR_ARG, "tables of this job exceed the 16 MiB static scratch");
     // batch B and per-thread path count G chosen as rbg_price_rt chooses them
-    // (G = ceil(B / (256 * 608))), halving B until ivb + partials fit
+    // (G = ceil(B / (256 * 608))), halving B until ivb + partials fit; fused
+    // jobs need no ivb and one partial row per CTA
     int64_t B = std::min<int64_t>(p->M, job.batch);
     int G = 1;
     int64_t nchunk_max = 1;
     size_t off_ivb = 0;
     for (;;) {
         G = (int)std::max<int64_t>(1, (B + 256 * 608 - 1) / (256 * 608));
-        nchunk_max = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+        nchunk_max = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
         off_ivb = up256(off_part + (size_t)32 * n_out * nchunk_max);
-        if (off_ivb + (size_t)8 * plan.vgs.size() * B <= kStaticScratchBytes) break;
-        if (B <= 256) return static_fail(RBG_ERR_ARG, "variance groups / outputs of this job exceed the static scratch");
+        const size_t ivb_bytes = job.fused ? 0 : (size_t)8 * plan.vgs.size() * B;
+        if (off_ivb + ivb_bytes <= kStaticScratchBytes) break;
+        if (job.fused || B <= 256)
+            return static_fail(RBG_ERR_ARG, "variance groups / outputs of this job exceed the static scratch");
         B = (B + 1) / 2;
     }
     void* base = nullptr;
@@ -142,6 +145,19 @@ int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price
     }
     for (int64_t m0 = 0; m0 < p->M; m0 += B) {
         const int64_t b = std::min(B, p->M - m0);
+        if (job.fused) {
+            const int rows = mixed_part_rows(job, b);
+            e = cudaMemsetAsync(s + off_part, 0, (size_t)32 * n_out * rows, st);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return static_fail(RBG_ERR_CUDA, std::string("static scratch clear: ") + cudaGetErrorString(e));
+            }
+            rc = mixed_launch(job, s + off_ws, o->seed, o->path_offset + m0, b, nullptr, st, err, nullptr, nullptr,
+                              (double*)(s + off_part));
+            if (rc) return static_fail(rc, err);
+            launch_accumulate((const double*)(s + off_part), rows, n_out, (double*)(s + off_acc), st);
+            continue;
+        }
         rc = mixed_launch(job, s + off_ws, o->seed, o->path_offset + m0, b, s + off_ivb, st, err);
         if (rc) return static_fail(rc, err);
         const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));

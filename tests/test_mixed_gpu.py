@@ -153,3 +153,15 @@ def test_fft_prices_vs_fp64_identical_normals(R, N):
     err = np.abs(mp - fp)
     assert np.all(err <= 1e-4 * fp)
     assert np.all(err < 0.2 * fs)
+
+
+def test_mixed_extreme_strikes(R):
+    """FP32 conditional BS (Chebyshev erfc tails, put-call parity for ITM)
+    against the FP64 form on identical normals, deep in both wings."""
+    K = [0.2, 0.4, 0.6, 0.8, 1.0, 1.25, 1.6, 2.2, 3.0]
+    N, M = 128, 1 << 15
+    mp, ms, _ = R.price_rt(0.04, [0.1], [2.5], [-0.9], [1.5] * len(K), K, N, M, seed=8, precision=R.MIXED, split=1)
+    fp, fs, _ = R.price_rt(0.04, [0.1], [2.5], [-0.9], [1.5] * len(K), K, N, M, seed=8, normals=R.NORMALS_F32)
+    rel = np.abs(mp - fp) / fp
+    assert np.all(rel[fp > 1e-5] < 1e-4)
+    assert np.all(np.abs(mp - fp) < 0.2 * fs)
