@@ -306,13 +306,107 @@ def run_gpu(args, w):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------ serving arm
+def serving_requests(n: int, rate: float, seed: int = 20261203):
+    """Calibration-style traffic: Poisson arrivals at `rate`/s; H ~ U[.03,.45],
+    eta ~ U[.5,3], rho ~ U[-.99,-.3], xi ~ U[.01,.1], T ~ U[.05,3], 1-64 strikes
+    on [0.5, 1.5], N and M log-uniform on [64, 1024] and [2^14, 2^22], Philox
+    seed = request index."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    reqs = []
+    for i in range(n):
+        nk = int(rng.integers(1, 65))
+        reqs.append(dict(
+            H=[float(rng.uniform(0.03, 0.45))], eta=[float(rng.uniform(0.5, 3.0))], rho=[float(rng.uniform(-0.99, -0.3))],
+            xi=float(rng.uniform(0.01, 0.1)), T=[float(rng.uniform(0.05, 3.0))] * nk,
+            K=list(np.linspace(0.5, 1.5, nk)) if nk > 1 else [1.0],
+            N=int(np.exp(rng.uniform(np.log(64), np.log(1024)))),
+            M=int(np.exp(rng.uniform(np.log(2 ** 14), np.log(2 ** 22)))), seed=i, t=float(t[i])))
+    return reqs
+
+
+def run_serving(args):
+    import threading
+
+    import rbergomi_gb300 as R
+
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    R.lib()
+    reqs = serving_requests(args.requests, args.rate)
+    # warm the kernels and the allocator on a few off-schedule requests
+    with R.Server() as srv:
+        for r in reqs[:8]:
+            srv.wait(srv.submit(r["xi"], r["H"], r["eta"], r["rho"], r["T"], r["K"], r["N"], 1 << 14, seed=r["seed"]))
+    lat = [None] * len(reqs)
+    n0 = R.launch_count()
+    with ClockSampler(local) as clk:
+        with R.Server(use_graphs=0 if args.no_graphs else 1) as srv:
+            tickets = [None] * len(reqs)
+            ready = threading.Semaphore(0)
+
+            def submitter():
+                t0 = time.perf_counter()
+                for i, r in enumerate(reqs):
+                    dt = r["t"] - (time.perf_counter() - t0)
+                    if dt > 0:
+                        time.sleep(dt)
+                    tickets[i] = srv.submit(r["xi"], r["H"], r["eta"], r["rho"], r["T"], r["K"], r["N"], r["M"],
+                                            seed=r["seed"])
+                    ready.release()
+
+            wall0 = time.perf_counter()
+            th = threading.Thread(target=submitter)
+            th.start()
+            for i in range(len(reqs)):
+                ready.acquire()
+                _, _, _, lat[i] = srv.wait(tickets[i])
+            th.join()
+            wall = time.perf_counter() - wall0
+            st = srv.stats()
+    launches = R.launch_count() - n0
+    lat = np.array(lat)
+    prices = sum(len(r["K"]) for r in reqs)
+    psteps = sum(r["M"] * r["N"] for r in reqs)
+    # FP64 one-request-at-a-time form on a sample of the same stream
+    fp64 = None
+    if args.fp64_sample > 0:
+        samp = reqs[:args.fp64_sample]
+        t0 = time.perf_counter()
+        tl = []
+        for r in samp:
+            t1 = time.perf_counter()
+            R.price_rt(r["xi"], r["H"], r["eta"], r["rho"], r["T"], r["K"], r["N"], r["M"], seed=r["seed"])
+            tl.append(1e3 * (time.perf_counter() - t1))
+        dt = time.perf_counter() - t0
+        fp64 = {"requests": len(samp), "prices_per_s": sum(len(r["K"]) for r in samp) / dt,
+                "path_steps_per_s": sum(r["M"] * r["N"] for r in samp) / dt,
+                "p50_ms_alone": float(np.percentile(tl, 50)), "max_ms_alone": float(np.max(tl)),
+                "note": "one request at a time, no queueing: latency is service time only"}
+    line = {
+        "metric": "serving prices/s (p50/p99 latency ms)", "value": prices / wall, "unit": "prices/s",
+        "n_gpus": ws, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * wall, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3+f32+f64", "data": "synthetic request stream",
+        "config": {"workload": "serving-poisson", "requests": len(reqs), "rate_per_s": args.rate,
+                   "graphs": not args.no_graphs},
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "max_ms": float(np.max(lat)), "mean_ms": float(np.mean(lat)),
+        "path_steps_per_s": psteps / wall, "requests_per_s": len(reqs) / wall,
+        "server": st, "gpu_launches": launches, "clocks": clk.summary(), "fp64_one_at_a_time": fp64,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS) + ["serving-poisson"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
     ap.add_argument("--split", type=int, default=0, help="0 = BF16x3, 1 = FP16x3")
     ap.add_argument("--cpu-paths", type=int, default=1 << 17)
@@ -320,8 +414,15 @@ def main():
     ap.add_argument("--steps-per-path", type=int, default=None, help="override N (crossover sweeps)")
     ap.add_argument("--conv", default="auto", choices=["auto", "gemm", "fft"], help="mixed-form Volterra backend")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--requests", type=int, default=10000, help="serving: number of requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: Poisson arrival rate per second")
+    ap.add_argument("--fp64-sample", type=int, default=20, help="serving: FP64 one-at-a-time sample size")
+    ap.add_argument("--no-graphs", action="store_true", help="serving: launch without CUDA graphs")
     ap.add_argument("--skip-cpu", action="store_true")
     args = ap.parse_args()
+    if args.workload == "serving-poisson":
+        run_serving(args)
+        return
     w = dict(WORKLOADS[args.workload])
     if args.paths:
         w["M"] = int(args.paths)

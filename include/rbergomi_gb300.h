@@ -182,6 +182,56 @@ int rbg_debug_mixed_paths(const rbg_params* p, const rbg_options* o, float* norm
  * MMA warps, cycles[20] = epilogue cycles in the fused payoffs.  n >= 32. */
 int rbg_debug_mixed_profile(const rbg_params* p, const rbg_options* o, uint64_t* cycles, int n);
 
+/* ------------------------------------------------------------------------ */
+/* Serving loop (no counterpart in the reference: its callers fan out over   */
+/* console processes, rBergomiR/rbergomi_console.R:88-160)                  */
+/* ------------------------------------------------------------------------ */
+
+/* A persistent, continuously batched pricing loop.  Submitted requests are
+ * admitted onto device slots (each with its own CUDA stream) as soon as a
+ * slot and enough of the HBM budget are free, first fit in arrival order;
+ * the footprint charged is M * N * 4 bytes plus the request's tables.  Small
+ * requests (M*N*n_H <= small_request_path_steps) use high-priority streams;
+ * large ones are cut into launches of at most max_batch_paths paths so they
+ * yield the GPU between launches.  Volterra tables are cached on the device
+ * per (backend, H, N, split).  With use_graphs, each request's device work is
+ * launched as a CUDA graph, one executable per launch shape, updated in
+ * place.  All requests run the mixed form; results do not depend on what
+ * else is in flight (counter-based normals, per-request sums). */
+typedef struct rbg_server rbg_server;
+
+typedef struct rbg_server_config {
+    int slots;                       /* concurrent requests on the device (1..64) */
+    int high_priority_slots;         /* of which on high-priority streams */
+    uint64_t hbm_budget;             /* admission budget in bytes */
+    int64_t max_batch_paths;         /* paths per kernel launch */
+    double small_request_path_steps; /* threshold for the high-priority slots */
+    int table_cache_entries;         /* device-resident Volterra tables kept */
+    int use_graphs;                  /* launch each request as a CUDA graph */
+    int device;                      /* CUDA device, -1 = current */
+} rbg_server_config;
+
+typedef struct rbg_server_stats {
+    uint64_t completed, failed, pending, in_flight, hbm_in_use;
+    uint64_t table_cache_hits, table_cache_misses, graph_launches;
+} rbg_server_stats;
+
+void rbg_server_default_config(rbg_server_config* cfg);
+int rbg_server_create(const rbg_server_config* cfg, rbg_server** out);
+/* Copies the request (parameters and options; precision is forced to mixed)
+ * and returns a ticket at once. */
+int rbg_server_submit(rbg_server* s, const rbg_params* p, const rbg_options* o, uint64_t* ticket);
+/* done = 1 once the request's results are on the host. */
+int rbg_server_poll(rbg_server* s, uint64_t ticket, int* done);
+/* Blocks until the request is done, copies its prices, standard errors and
+ * implied vols (any may be NULL) and the latency from submit to completion,
+ * and forgets the ticket.  Returns the request's status. */
+int rbg_server_wait(rbg_server* s, uint64_t ticket, double* price, double* stat, double* iv, double* latency_ms);
+int rbg_server_get_stats(rbg_server* s, rbg_server_stats* st);
+/* Finishes the queued work and frees the server. */
+int rbg_server_destroy(rbg_server* s);
+const char* rbg_server_last_error(void);
+
 /* Allocation-free pricing.  No counterpart in the reference (it has no GPU).
  * For callers that cannot call cudaMalloc -- a host that reserved all device
  * memory for its own pool at start-up, or a latency-critical loop that cannot

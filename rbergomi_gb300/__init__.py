@@ -52,7 +52,8 @@ EXPORTS = [
     "rbg_price_rt_sums", "rbg_payoffs_rt", "rbg_generate_normals", "rbg_implied_vol", "rbg_last_error",
     "rbg_launch_count", "rbg_synchronize", "rbg_release", "rbg_plan_info", "rbg_profile_enable",
     "rbg_profile_reset", "rbg_profile_read", "rbg_last_transfer_bytes", "rbg_debug_mixed_paths",
-    "rbg_debug_mixed_profile",
+    "rbg_debug_mixed_profile", "rbg_server_default_config", "rbg_server_create", "rbg_server_submit",
+    "rbg_server_poll", "rbg_server_wait", "rbg_server_get_stats", "rbg_server_destroy", "rbg_server_last_error",
 ]
 
 STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4
@@ -316,3 +317,92 @@ def debug_mixed_profile(xi, H, eta, rho, T, K, N, M, **opts):
     c = (C.c_uint64 * 32)()
     _check(lib().rbg_debug_mixed_profile(C.byref(p.s), C.byref(o), c, 32))
     return {PROFILE_SITES.get(i, str(i)): int(c[i]) for i in range(32) if c[i]}
+
+
+# ------------------------------------------------------------ serving loop
+class RbgServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int), ("high_priority_slots", C.c_int), ("hbm_budget", C.c_uint64),
+                ("max_batch_paths", C.c_int64), ("small_request_path_steps", C.c_double),
+                ("table_cache_entries", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int)]
+
+
+class RbgServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("completed", "failed", "pending", "in_flight", "hbm_in_use",
+                                          "table_cache_hits", "table_cache_misses", "graph_launches")]
+
+
+def _server_lib():
+    L = lib()
+    if not getattr(L, "_server_ready", False):
+        SP = C.c_void_p
+        L.rbg_server_default_config.argtypes = [C.POINTER(RbgServerConfig)]
+        L.rbg_server_create.argtypes = [C.POINTER(RbgServerConfig), C.POINTER(SP)]
+        L.rbg_server_create.restype = C.c_int
+        L.rbg_server_submit.argtypes = [SP, C.POINTER(RbgParams), C.POINTER(RbgOptions), C.POINTER(C.c_uint64)]
+        L.rbg_server_submit.restype = C.c_int
+        L.rbg_server_poll.argtypes = [SP, C.c_uint64, C.POINTER(C.c_int)]
+        L.rbg_server_poll.restype = C.c_int
+        L.rbg_server_wait.argtypes = [SP, C.c_uint64, _dp, _dp, _dp, _dp]
+        L.rbg_server_wait.restype = C.c_int
+        L.rbg_server_get_stats.argtypes = [SP, C.POINTER(RbgServerStats)]
+        L.rbg_server_get_stats.restype = C.c_int
+        L.rbg_server_destroy.argtypes = [SP]
+        L.rbg_server_destroy.restype = C.c_int
+        L.rbg_server_last_error.restype = C.c_char_p
+        L._server_ready = True
+    return L
+
+
+class Server:
+    """Continuously batched pricing loop (rbg_server_* in the C ABI).
+
+    submit() copies the request and returns a ticket at once; wait(ticket)
+    blocks until its results are on the host and returns (price, stat, iv,
+    latency_ms), latency measured by the server from submit to completion."""
+
+    def __init__(self, **cfg):
+        L = _server_lib()
+        c = RbgServerConfig()
+        L.rbg_server_default_config(C.byref(c))
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        self._h = C.c_void_p()
+        rc = L.rbg_server_create(C.byref(c), C.byref(self._h))
+        if rc:
+            raise RbgError(f"server create: {L.rbg_server_last_error().decode()}")
+        self._nout = {}
+
+    def submit(self, xi, H, eta, rho, T, K, N, M, **opts) -> int:
+        p = _Params(xi, H, eta, rho, T, K, N, M)
+        o = options(precision=MIXED, **opts)
+        t = C.c_uint64()
+        rc = _server_lib().rbg_server_submit(self._h, C.byref(p.s), C.byref(o), C.byref(t))
+        if rc:
+            raise RbgError(f"submit status {rc}: {_server_lib().rbg_server_last_error().decode()}")
+        self._nout[t.value] = p.out
+        return t.value
+
+    def wait(self, ticket):
+        n = self._nout.pop(ticket)
+        price, stat, iv, lat = np.empty(n), np.empty(n), np.empty(n), C.c_double()
+        rc = _server_lib().rbg_server_wait(self._h, ticket, price.ctypes.data_as(_dp), stat.ctypes.data_as(_dp),
+                                           iv.ctypes.data_as(_dp), C.byref(lat))
+        if rc:
+            raise RbgError(f"request status {rc}: {_server_lib().rbg_server_last_error().decode()}")
+        return price, stat, iv, lat.value
+
+    def stats(self) -> dict:
+        s = RbgServerStats()
+        _server_lib().rbg_server_get_stats(self._h, C.byref(s))
+        return {n: int(getattr(s, n)) for n, _ in RbgServerStats._fields_}
+
+    def close(self):
+        if self._h:
+            _server_lib().rbg_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -738,7 +738,26 @@ void build_strip(const double* gamma, int N, int Np, int bf16, unsigned char* im
 
 }  // namespace
 
-int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err)
+void mixed_table_range(const MixedJob& job, int i, size_t* off, size_t* bytes)
+{
+    const MixedLaunch& r = job.launches[i];
+    if (job.backend == RBG_CONV_GEMM) {
+        *off = r.off_strip;
+        *bytes = (size_t)2 * r.args.Np * 64;
+    } else {
+        *off = r.off_spec;
+        *bytes = (size_t)r.args.L * 8;
+    }
+}
+
+void mixed_twiddle_range(const MixedJob& job, size_t* off, size_t* bytes)
+{
+    *off = job.off_tw;
+    *bytes = (job.backend == RBG_CONV_FFT && !job.launches.empty()) ? (size_t)job.launches[0].args.L * 8 : 0;
+}
+
+int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
+                  int64_t max_batch)
 {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -898,6 +917,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     // batch: float2 per (variance group, path) within 1 GiB
     int64_t cap = ((int64_t)1 << 30) / (8 * (int64_t)std::max(1, job.n_vg));
     cap = std::max<int64_t>(kTileM, cap / kTileM * kTileM);
+    if (max_batch > 0) cap = std::min<int64_t>(cap, std::max<int64_t>(kTileM, max_batch / kTileM * kTileM));
     job.batch = std::min<int64_t>(M, cap);
     return RBG_OK;
 }
@@ -926,9 +946,11 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
     unsigned char* base = (unsigned char*)ws;
     for (const MixedLaunch& r : job.launches) {
         MixedArgs A = r.args;
-        A.strip = base + r.off_strip;
+        const size_t li = (size_t)(&r - job.launches.data());
+        const bool over = li < job.table_dev.size() && job.table_dev[li];
+        A.strip = over ? (const unsigned char*)job.table_dev[li] : base + r.off_strip;
         A.beta = (const float*)(base + r.off_beta);
-        A.spec = (const float2*)(base + r.off_spec);
+        A.spec = over ? (const float2*)job.table_dev[li] : (const float2*)(base + r.off_spec);
         A.otab = (const float4*)(base + r.off_otab);
         A.oidx = (const int*)(base + r.off_oidx);
         A.part = part;

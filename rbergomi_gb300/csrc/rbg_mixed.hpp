@@ -55,10 +55,16 @@ struct MixedJob {
     bool fused = false;           // payoffs priced inside the path kernel (GEMM backend, <= 64 per launch)
     size_t off_tw = 0;
     std::vector<MixedLaunch> launches;   // one per (Volterra pass, <= 16 groups)
+    std::vector<const void*> table_dev;  // optional device copies of each launch's strip / spectrum
     std::vector<unsigned char> host_ws;  // image uploaded by mixed_upload
 };
 
-int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err);
+int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
+                  int64_t max_batch = 0);
+// Byte range of launch i's strip (GEMM) or spectrum (FFT) inside host_ws, and
+// of the shared FFT twiddle table (empty for the GEMM backend).
+void mixed_table_range(const MixedJob& job, int i, size_t* off, size_t* bytes);
+void mixed_twiddle_range(const MixedJob& job, size_t* off, size_t* bytes);
 int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
 // Launches the path kernel(s) for paths [path0, path0 + B).  Unfused jobs
 // write (Ivdt, IsvdW) to ivb; fused jobs add their payoff sums to `part`

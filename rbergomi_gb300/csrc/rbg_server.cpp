@@ -1,0 +1,622 @@
+// rbg_server.cpp -- a persistent, continuously batched pricing loop.
+//
+// Calibration traffic sends many independent pricing requests of different
+// shapes (N, M, number of strikes, parameters).  The server:
+//   * admits requests continuously: a scheduler thread moves submitted
+//     requests onto free device slots as soon as a slot and enough of the
+//     HBM budget are free (first-in first-out, but a request that does not
+//     fit does not block smaller ones behind it).  The footprint charged is
+//     M * N * 4 bytes plus the request's tables;
+//   * overlaps requests on the device: every slot owns a CUDA stream and its
+//     own buffers; small requests (M * N below a threshold) go to
+//     high-priority streams, so the hardware scheduler hands them SMs first,
+//     and large requests are cut into launches of at most max_batch_paths
+//     paths so they yield the GPU between launches;
+//   * keeps device-resident Volterra tables (the GEMM strip or the FFT
+//     spectrum) cached per (backend, H, N, split), LRU with reference counts;
+//   * draws normals from the counter-based Philox stream (seed = the
+//     request's seed, counter = path and step), so a request's result does
+//     not depend on what else is in flight;
+//   * optionally captures each request's device work (everything after the
+//     table upload) as a CUDA graph and launches the graph;
+//   * records per-request latency (submit -> results on the host).
+// Every request runs the mixed form (tcgen05 GEMM for N <= 512, FFT above).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <list>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "rbg_internal.hpp"
+#include "rbg_mixed.hpp"
+
+namespace rbg {
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// Stream-ordered, grow-only device buffer.
+struct SBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t bytes, cudaStream_t st)
+    {
+        if (bytes <= n) return cudaSuccess;
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+        n = 0;
+        const size_t want = std::max(bytes, (size_t)4096);
+        cudaError_t e = cudaMallocAsync(&p, want, st);
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+};
+
+struct Req {
+    uint64_t id = 0;
+    Plan plan;
+    rbg_options opt{};
+    int64_t M = 0;
+    MixedJob job;
+    std::vector<OutDev> outs;
+    std::vector<double> Tv;
+    size_t footprint = 0;
+    double work = 0;  // path-steps
+    std::vector<double> res;
+    int status = RBG_OK;
+    std::string err;
+    bool done = false;
+    std::vector<int> cache_keys;  // cache entries pinned while in flight
+    Clock::time_point t_submit, t_start, t_done;
+};
+
+struct Slot {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    bool high = false;
+    SBuf ws, ivb, part, acc, res, outs;
+    double* pin = nullptr;  // [0] error word, then 5 * n_out results
+    size_t pin_n = 0;
+    Req* req = nullptr;
+    // graph cache: one instantiated graph per launch shape
+    std::map<std::string, cudaGraphExec_t> graphs;
+};
+
+struct CacheEntry {
+    void* dev = nullptr;
+    size_t bytes = 0;
+    int refs = 0;
+    cudaEvent_t ready = nullptr;
+    std::list<int>::iterator lru;
+};
+
+}  // namespace
+
+struct Server {
+    rbg_server_config cfg{};
+    int dev = 0;
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Req*> pending;
+    std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
+    uint64_t next_id = 1;
+    size_t in_use = 0;
+    bool stop = false;
+    std::thread thr;
+    cudaStream_t copy_st = nullptr;
+    // table cache
+    std::map<std::tuple<int, uint64_t, int, int>, int> cache_index;
+    std::vector<CacheEntry> cache;
+    std::list<int> lru;
+    // statistics
+    uint64_t completed = 0, failed = 0, cache_hits = 0, cache_misses = 0, graph_launches = 0;
+    double busy_since_ms = -1;
+
+    void run();
+    int launch(Slot& s, Req& r, std::string& err);
+    void finish(Slot& s);
+    int acquire_tables(Req& r, cudaStream_t st, std::string& err);
+    void release_tables(Req& r);
+};
+
+static uint64_t hbits(double x)
+{
+    uint64_t u;
+    std::memcpy(&u, &x, 8);
+    return u;
+}
+
+int Server::acquire_tables(Req& r, cudaStream_t st, std::string& err)
+{
+    MixedJob& job = r.job;
+    job.table_dev.assign(job.launches.size(), nullptr);
+    for (size_t i = 0; i < job.launches.size(); ++i) {
+        const MixedArgs& A = job.launches[i].args;
+        const double H = r.plan.vols[r.plan.vgs[A.g0].vol].H;
+        auto key = std::make_tuple(job.backend, hbits(H), r.plan.N, job.split);
+        size_t off = 0, bytes = 0;
+        mixed_table_range(job, (int)i, &off, &bytes);
+        int idx;
+        auto it = cache_index.find(key);
+        if (it != cache_index.end()) {
+            idx = it->second;
+            lru.erase(cache[idx].lru);
+            ++cache_hits;
+        } else {
+            ++cache_misses;
+            // evict unreferenced entries beyond the capacity
+            while ((int)cache_index.size() >= cfg.table_cache_entries) {
+                auto victim = std::find_if(lru.rbegin(), lru.rend(), [&](int k) { return cache[k].refs == 0; });
+                if (victim == lru.rend()) break;
+                const int k = *victim;
+                for (auto jt = cache_index.begin(); jt != cache_index.end(); ++jt)
+                    if (jt->second == k) { cache_index.erase(jt); break; }
+                lru.erase(std::next(victim).base());
+                cudaFreeAsync(cache[k].dev, copy_st);
+                cache[k].dev = nullptr;
+            }
+            idx = -1;
+            for (size_t k = 0; k < cache.size(); ++k)
+                if (!cache[k].dev && cache[k].refs == 0) { idx = (int)k; break; }
+            if (idx < 0) {
+                cache.emplace_back();
+                idx = (int)cache.size() - 1;
+                cudaEventCreateWithFlags(&cache[idx].ready, cudaEventDisableTiming);
+            }
+            CacheEntry& e = cache[idx];
+            cudaError_t ce = cudaMallocAsync(&e.dev, bytes, copy_st);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpyAsync(e.dev, job.host_ws.data() + off, bytes, cudaMemcpyHostToDevice, copy_st);
+            if (ce == cudaSuccess) ce = cudaEventRecord(e.ready, copy_st);
+            if (ce != cudaSuccess) {
+                cudaGetLastError();
+                err = std::string("table cache: ") + cudaGetErrorString(ce);
+                return RBG_ERR_CUDA;
+            }
+            // the copy reads host_ws: finish it before the request (and its host image) can go
+            cudaStreamSynchronize(copy_st);
+            e.bytes = bytes;
+            cache_index[key] = idx;
+        }
+        CacheEntry& e = cache[idx];
+        lru.push_front(idx);
+        e.lru = lru.begin();
+        ++e.refs;
+        r.cache_keys.push_back(idx);
+        cudaStreamWaitEvent(st, e.ready, 0);
+        job.table_dev[i] = e.dev;
+    }
+    return RBG_OK;
+}
+
+void Server::release_tables(Req& r)
+{
+    for (int k : r.cache_keys) --cache[k].refs;
+    r.cache_keys.clear();
+}
+
+int Server::launch(Slot& s, Req& r, std::string& err)
+{
+    cudaStream_t st = s.st;
+    MixedJob& job = r.job;
+    const int no = (int)r.plan.outs.size();
+    const int64_t B = job.batch;
+    const int G = (int)std::max<int64_t>(1, (B + 256 * 608 - 1) / (256 * 608));
+    const int64_t rows = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+    cudaError_t e = s.ws.ensure(job.workspace_bytes, st);
+    if (e == cudaSuccess && !job.fused) e = s.ivb.ensure(sizeof(float) * 2 * r.plan.vgs.size() * (size_t)B, st);
+    if (e == cudaSuccess) e = s.part.ensure(sizeof(double) * 4 * no * (size_t)rows, st);
+    if (e == cudaSuccess) e = s.acc.ensure(sizeof(double) * 4 * no, st);
+    if (e == cudaSuccess) e = s.res.ensure(sizeof(double) * 5 * no, st);
+    if (e == cudaSuccess) e = s.outs.ensure(sizeof(OutDev) * no + sizeof(double) * no + 256, st);
+    const size_t pin_need = sizeof(double) * (1 + 5 * (size_t)no);
+    if (e == cudaSuccess && s.pin_n < pin_need) {
+        if (s.pin) cudaFreeHost(s.pin);
+        s.pin = nullptr;
+        s.pin_n = 0;
+        e = cudaMallocHost((void**)&s.pin, pin_need);
+        if (e == cudaSuccess) s.pin_n = pin_need;
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("slot buffers: ") + cudaGetErrorString(e);
+        return RBG_ERR_NOMEM;
+    }
+    int rc = acquire_tables(r, st, err);
+    if (rc) return rc;
+    OutDev* d_outs = (OutDev*)s.outs.p;
+    double* d_T = (double*)((unsigned char*)s.outs.p + ((sizeof(OutDev) * no + 255) / 256) * 256);
+    // inputs (pageable host memory; the request keeps them alive until it completes)
+    e = cudaMemcpyAsync(s.ws.p, job.host_ws.data(), job.host_ws.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_outs, r.outs.data(), sizeof(OutDev) * no, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_T, r.Tv.data(), sizeof(double) * no, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("request upload: ") + cudaGetErrorString(e);
+        return RBG_ERR_CUDA;
+    }
+
+    // device work of the request: captured as a CUDA graph when configured
+    const bool graph = cfg.use_graphs != 0;
+    if (graph) {
+        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            err = std::string("graph capture: ") + cudaGetErrorString(e);
+            return RBG_ERR_CUDA;
+        }
+    }
+    std::string kerr;
+    rc = RBG_OK;
+    cudaMemsetAsync(s.acc.p, 0, sizeof(double) * 4 * no, st);
+    for (int64_t m0 = 0; m0 < r.M && rc == RBG_OK; m0 += B) {
+        const int64_t b = std::min(B, r.M - m0);
+        if (job.fused) {
+            const int nr = mixed_part_rows(job, b);
+            cudaMemsetAsync(s.part.p, 0, sizeof(double) * 4 * no * (size_t)nr, st);
+            rc = mixed_launch(job, s.ws.p, r.opt.seed, r.opt.path_offset + m0, b, nullptr, st, kerr, nullptr,
+                              nullptr, (double*)s.part.p);
+            if (rc == RBG_OK) launch_accumulate((const double*)s.part.p, nr, no, (double*)s.acc.p, st);
+        } else {
+            rc = mixed_launch(job, s.ws.p, r.opt.seed, r.opt.path_offset + m0, b, s.ivb.p, st, kerr);
+            const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
+            if (rc == RBG_OK) {
+                launch_payoff_sums_f32(d_outs, no, s.ivb.p, b, G, (double*)s.part.p, nchunks, st);
+                launch_accumulate((const double*)s.part.p, nchunks, no, (double*)s.acc.p, st);
+            }
+        }
+    }
+    if (rc == RBG_OK) {
+        launch_finalize((const double*)s.acc.p, no, r.M, d_outs, d_T, r.opt.compute_iv, (double*)s.res.p, st);
+        cudaMemcpyAsync(s.pin, (unsigned char*)s.ws.p + job.off_err, 4, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(s.pin + 1, s.res.p, sizeof(double) * 5 * no, cudaMemcpyDeviceToHost, st);
+    }
+    if (graph) {
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(st, &g);
+        if (rc == RBG_OK && e == cudaSuccess) {
+            // one executable graph per launch shape, updated in place for new parameters
+            char key[128];
+            std::snprintf(key, sizeof key, "%d/%d/%lld/%lld/%d/%d", job.backend, (int)job.launches.size(),
+                          (long long)B, (long long)r.M, no, job.fused ? 1 : 0);
+            auto it = s.graphs.find(key);
+            bool ok = false;
+            if (it != s.graphs.end()) {
+                cudaGraphExecUpdateResultInfo info;
+                ok = cudaGraphExecUpdate(it->second, g, &info) == cudaSuccess;
+                if (!ok) {
+                    cudaGetLastError();
+                    cudaGraphExecDestroy(it->second);
+                    s.graphs.erase(it);
+                }
+            }
+            if (!ok) {
+                cudaGraphExec_t ex = nullptr;
+                e = cudaGraphInstantiate(&ex, g, 0);
+                if (e == cudaSuccess) {
+                    s.graphs[key] = ex;
+                    ok = true;
+                }
+            }
+            if (ok) {
+                e = cudaGraphLaunch(s.graphs[key], st);
+                ++graph_launches;
+            }
+        }
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess && rc == RBG_OK) {
+            cudaGetLastError();
+            err = std::string("graph launch: ") + cudaGetErrorString(e);
+            return RBG_ERR_CUDA;
+        }
+    }
+    if (rc != RBG_OK) {
+        err = kerr;
+        return rc;
+    }
+    e = cudaEventRecord(s.ev, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("request launch: ") + cudaGetErrorString(e);
+        return RBG_ERR_CUDA;
+    }
+    return RBG_OK;
+}
+
+void Server::finish(Slot& s)
+{
+    Req& r = *s.req;
+    const int no = (int)r.plan.outs.size();
+    unsigned int word = 0;
+    std::memcpy(&word, s.pin, 4);
+    if (word != 0) {
+        r.status = RBG_ERR_TIMEOUT;
+        r.err = "mixed kernel: a bounded pipeline wait expired (site " + std::to_string(word) + ")";
+    } else {
+        r.res.assign(s.pin + 1, s.pin + 1 + 5 * (size_t)no);
+    }
+    r.t_done = Clock::now();
+    r.done = true;
+    release_tables(r);
+    in_use -= r.footprint;
+    if (r.status == RBG_OK) ++completed; else ++failed;
+    s.req = nullptr;
+}
+
+void Server::run()
+{
+    cudaSetDevice(dev);
+    std::unique_lock<std::mutex> lk(mu);
+    while (true) {
+        bool progressed = false;
+        // completions
+        for (Slot& s : slots) {
+            if (!s.req) continue;
+            cudaError_t q = cudaEventQuery(s.ev);
+            if (q == cudaSuccess) {
+                finish(s);
+                progressed = true;
+            } else if (q != cudaErrorNotReady) {
+                cudaGetLastError();
+                s.req->status = RBG_ERR_CUDA;
+                s.req->err = std::string("device: ") + cudaGetErrorString(q);
+                s.req->t_done = Clock::now();
+                s.req->done = true;
+                release_tables(*s.req);
+                in_use -= s.req->footprint;
+                ++failed;
+                s.req = nullptr;
+                progressed = true;
+            }
+        }
+        if (progressed) cv_done.notify_all();
+        if (stop && pending.empty()) {
+            bool busy = false;
+            for (Slot& s : slots) busy = busy || s.req;
+            if (!busy) break;
+        }
+        // admissions: first fit in arrival order
+        for (auto it = pending.begin(); it != pending.end();) {
+            Req* r = *it;
+            const bool small = r->work <= cfg.small_request_path_steps;
+            Slot* free_slot = nullptr;
+            for (Slot& s : slots)
+                if (!s.req && (s.high == small || (!small && s.high == false))) { free_slot = &s; break; }
+            if (!free_slot && small)
+                for (Slot& s : slots)
+                    if (!s.req) { free_slot = &s; break; }
+            const bool fits = in_use + r->footprint <= cfg.hbm_budget || in_use == 0;
+            if (!free_slot || !fits) {
+                ++it;
+                continue;
+            }
+            it = pending.erase(it);
+            free_slot->req = r;
+            in_use += r->footprint;
+            r->t_start = Clock::now();
+            std::string err;
+            const int rc = launch(*free_slot, *r, err);
+            if (rc != RBG_OK) {
+                r->status = rc;
+                r->err = err;
+                r->t_done = Clock::now();
+                r->done = true;
+                release_tables(*r);
+                in_use -= r->footprint;
+                ++failed;
+                free_slot->req = nullptr;
+                cv_done.notify_all();
+            }
+            progressed = true;
+        }
+        if (!progressed) {
+            bool busy = false;
+            for (Slot& s : slots) busy = busy || s.req;
+            // poll the device quickly while work is in flight, sleep otherwise
+            cv_work.wait_for(lk, busy ? std::chrono::microseconds(50) : std::chrono::milliseconds(5));
+        }
+    }
+}
+
+}  // namespace rbg
+
+using namespace rbg;
+
+struct rbg_server {
+    std::unique_ptr<Server> s;
+};
+
+static thread_local std::string g_srv_err;
+
+static int srv_fail(int code, const std::string& m)
+{
+    g_srv_err = m;
+    return code;
+}
+
+extern "C" {
+
+void rbg_server_default_config(rbg_server_config* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->slots = 12;
+    c->high_priority_slots = 8;
+    c->hbm_budget = (uint64_t)96 << 30;
+    c->max_batch_paths = (int64_t)1 << 19;
+    c->small_request_path_steps = (double)(1u << 28);
+    c->table_cache_entries = 256;
+    c->use_graphs = 1;
+    c->device = -1;
+}
+
+const char* rbg_server_last_error(void) { return g_srv_err.c_str(); }
+
+int rbg_server_create(const rbg_server_config* cfg_in, rbg_server** out)
+{
+    if (!out) return srv_fail(RBG_ERR_ARG, "null output");
+    rbg_server_config cfg;
+    rbg_server_default_config(&cfg);
+    if (cfg_in) cfg = *cfg_in;
+    if (cfg.slots < 1 || cfg.slots > 64 || cfg.high_priority_slots < 0 || cfg.high_priority_slots > cfg.slots)
+        return srv_fail(RBG_ERR_ARG, "slots must be 1..64 and high_priority_slots <= slots");
+    std::unique_ptr<Server> s(new Server());
+    s->cfg = cfg;
+    int dev = cfg.device;
+    if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) return srv_fail(RBG_ERR_CUDA, "no CUDA device");
+    s->dev = dev;
+    if (cudaSetDevice(dev) != cudaSuccess) return srv_fail(RBG_ERR_CUDA, "cudaSetDevice failed");
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    s->slots.resize(cfg.slots);
+    for (int i = 0; i < cfg.slots; ++i) {
+        Slot& sl = s->slots[i];
+        sl.high = i < cfg.high_priority_slots;
+        if (cudaStreamCreateWithPriority(&sl.st, cudaStreamNonBlocking, sl.high ? hi : lo) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess)
+            return srv_fail(RBG_ERR_CUDA, "stream/event creation failed");
+    }
+    if (cudaStreamCreateWithFlags(&s->copy_st, cudaStreamNonBlocking) != cudaSuccess)
+        return srv_fail(RBG_ERR_CUDA, "stream creation failed");
+    Server* raw = s.get();
+    s->thr = std::thread([raw] { raw->run(); });
+    *out = new rbg_server{std::move(s)};
+    return RBG_OK;
+}
+
+int rbg_server_submit(rbg_server* srv, const rbg_params* p, const rbg_options* o, uint64_t* ticket)
+{
+    if (!srv || !p || !ticket) return srv_fail(RBG_ERR_ARG, "null argument");
+    std::unique_ptr<Req> r(new Req());
+    r->t_submit = Clock::now();
+    std::string err;
+    if (!build_plan(*p, r->plan, err)) return srv_fail(RBG_ERR_ARG, err);
+    rbg_default_options(&r->opt);
+    if (o) r->opt = *o;
+    r->opt.precision = RBG_MIXED;
+    r->opt.stream = nullptr;
+    r->M = p->M;
+    cudaSetDevice(srv->s->dev);
+    int rc = mixed_prepare(r->plan, r->opt, p->M, r->job, err, srv->s->cfg.max_batch_paths);
+    if (rc) return srv_fail(rc, err);
+    const int no = (int)r->plan.outs.size();
+    r->outs.resize(no);
+    r->Tv.resize(no);
+    for (int i = 0; i < no; ++i) {
+        r->outs[i] = OutDev{r->plan.outs[i].rho, r->plan.outs[i].K, r->plan.outs[i].vg, 0};
+        r->Tv[i] = r->plan.outs[i].T;
+    }
+    r->work = (double)p->M * p->N * (double)r->plan.vols.size();
+    r->footprint = (size_t)p->M * (size_t)p->N * 4 + r->job.workspace_bytes;
+    Server& s = *srv->s;
+    {
+        std::lock_guard<std::mutex> lk(s.mu);
+        if (s.stop) return srv_fail(RBG_ERR_ARG, "server is stopping");
+        r->id = s.next_id++;
+        *ticket = r->id;
+        s.pending.push_back(r.get());
+        s.reqs[r->id] = std::move(r);
+    }
+    s.cv_work.notify_one();
+    return RBG_OK;
+}
+
+int rbg_server_poll(rbg_server* srv, uint64_t ticket, int* done)
+{
+    if (!srv || !done) return srv_fail(RBG_ERR_ARG, "null argument");
+    Server& s = *srv->s;
+    std::lock_guard<std::mutex> lk(s.mu);
+    auto it = s.reqs.find(ticket);
+    if (it == s.reqs.end()) return srv_fail(RBG_ERR_ARG, "unknown ticket");
+    *done = it->second->done ? 1 : 0;
+    return RBG_OK;
+}
+
+int rbg_server_wait(rbg_server* srv, uint64_t ticket, double* price, double* stat, double* iv, double* latency_ms)
+{
+    if (!srv) return srv_fail(RBG_ERR_ARG, "null server");
+    Server& s = *srv->s;
+    std::unique_lock<std::mutex> lk(s.mu);
+    auto it = s.reqs.find(ticket);
+    if (it == s.reqs.end()) return srv_fail(RBG_ERR_ARG, "unknown ticket");
+    Req* r = it->second.get();
+    s.cv_done.wait(lk, [&] { return r->done; });
+    const int status = r->status;
+    if (status == RBG_OK) {
+        const size_t no = r->plan.outs.size();
+        if (price) std::memcpy(price, r->res.data(), no * sizeof(double));
+        if (stat) std::memcpy(stat, r->res.data() + no, no * sizeof(double));
+        if (iv) std::memcpy(iv, r->res.data() + 2 * no, no * sizeof(double));
+    } else {
+        g_srv_err = r->err;
+    }
+    if (latency_ms)
+        *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    s.reqs.erase(it);
+    return status;
+}
+
+int rbg_server_get_stats(rbg_server* srv, rbg_server_stats* st)
+{
+    if (!srv || !st) return srv_fail(RBG_ERR_ARG, "null argument");
+    Server& s = *srv->s;
+    std::lock_guard<std::mutex> lk(s.mu);
+    std::memset(st, 0, sizeof(*st));
+    st->completed = s.completed;
+    st->failed = s.failed;
+    st->pending = s.pending.size();
+    for (Slot& sl : s.slots) st->in_flight += sl.req ? 1 : 0;
+    st->hbm_in_use = s.in_use;
+    st->table_cache_hits = s.cache_hits;
+    st->table_cache_misses = s.cache_misses;
+    st->graph_launches = s.graph_launches;
+    return RBG_OK;
+}
+
+int rbg_server_destroy(rbg_server* srv)
+{
+    if (!srv) return RBG_OK;
+    Server& s = *srv->s;
+    {
+        std::lock_guard<std::mutex> lk(s.mu);
+        s.stop = true;
+    }
+    s.cv_work.notify_all();
+    if (s.thr.joinable()) s.thr.join();
+    cudaSetDevice(s.dev);
+    for (Slot& sl : s.slots) {
+        cudaStreamSynchronize(sl.st);
+        for (auto& g : sl.graphs) cudaGraphExecDestroy(g.second);
+        for (SBuf* b : {&sl.ws, &sl.ivb, &sl.part, &sl.acc, &sl.res, &sl.outs})
+            if (b->p) cudaFreeAsync(b->p, sl.st);
+        cudaStreamSynchronize(sl.st);
+        if (sl.pin) cudaFreeHost(sl.pin);
+        cudaEventDestroy(sl.ev);
+        cudaStreamDestroy(sl.st);
+    }
+    for (CacheEntry& e : s.cache) {
+        if (e.dev) cudaFreeAsync(e.dev, s.copy_st);
+        if (e.ready) cudaEventDestroy(e.ready);
+    }
+    cudaStreamSynchronize(s.copy_st);
+    cudaStreamDestroy(s.copy_st);
+    delete srv;
+    return RBG_OK;
+}
+
+}  // extern "C"
