@@ -237,7 +237,7 @@ def run_gpu(args, w):
     exec_flops = 6.0 * 32 * 32 * nc * (nc + 1) / 2 * w["M"] / max(1, kn // args.steps)
     roof = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
             "frac": achieved_tf / bf16_peak, "traffic": traffic_per_launch("k_mixed_gemm", w),
-            "kernel": ("k_mixed_fft" if (args.conv == "fft" or (args.conv == "auto" and w["N"] > 512))
+            "kernel": ("k_mixed_fft" if (args.conv == "fft" or (args.conv == "auto" and w["N"] > 1024))
                        else "k_mixed_gemm") if prec == R.MIXED else "k_path_fp64",
             "kernel_ms": avg_kernel_ms, "peak_source": f"{peak_src} bf16 burst",
             "algorithmic_flops_per_launch": algo_flops,

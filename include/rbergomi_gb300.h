@@ -36,6 +36,20 @@ extern "C" {
 /* Drop-in layer                                                            */
 /* ------------------------------------------------------------------------ */
 
+/* Plain Monte Carlo prices, implied vols and MC standard errors over the
+ * ParamTot grid.  Replaces computeIV_tensor, rBergLib/cinterface.h:63-66
+ * (cinterface.cpp:10-46; estimator rBergomiMT.cpp:174-289): a third normal
+ * stream Wperp per path, S_T = exp(sum sqrt(v) sqrt(dt) Z - dt/2 sum v) with
+ * Z = rho W1 + sqrt(1 - rho^2) Wperp, payoff max(S_T - K, 0); S is
+ * recomputed on the reference's rho trigger (eps 1e-10).  Same size checks,
+ * exit codes and seed folding as computeIVRT_tensor.  Always FP64.  Like the
+ * reference (cinterface.cpp:45), eta_tot receives the rho values and
+ * rho_tot the eta values. */
+void computeIV_tensor(double xi, double* H, double* eta, double* rho, int par_size, double* T, double* K,
+                      int op_size, int N, long M, uint64_t* seed, int seed_size, int num_threads, double* price,
+                      double* iv, double* stat, double* H_tot, double* eta_tot, double* rho_tot, double* T_tot,
+                      double* K_tot, int out_size);
+
 /* Romano-Touzi prices, implied vols and MC standard errors over the ParamTot
  * grid.  Replaces computeIVRT_tensor, rBergLib/cinterface.h:68-71
  * (cinterface.cpp:49-85).  out_size must equal par_size * op_size, else the
@@ -75,8 +89,9 @@ enum rbg_status {
 
 enum rbg_precision { RBG_FP64 = 0, RBG_MIXED = 1 };
 
-/* Volterra convolution backend.  AUTO picks the tcgen05 Toeplitz GEMM for
- * N <= 512 in mixed mode and the direct sum otherwise. */
+/* Volterra convolution backend.  In mixed mode AUTO picks the tcgen05
+ * Toeplitz GEMM for N <= 1024 (one TMEM pass up to 512 steps, two above) and
+ * the batched FFT convolution above; the FP64 form uses the direct sum. */
 enum rbg_conv { RBG_CONV_AUTO = 0, RBG_CONV_GEMM = 1, RBG_CONV_FFT = 2, RBG_CONV_DIRECT = 3 };
 
 /* Normal transform used by the FP64 form: its own FP64 Box-Muller (default),
@@ -118,6 +133,28 @@ void rbg_default_options(rbg_options* opts);
  * par_size*op_size doubles (iv may be NULL).  Returns enum rbg_status. */
 int rbg_price_rt(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv);
 
+/* Unordered parameter list: output i prices the tuple (H[i], eta[i],
+ * rho[i], T[i], K[i]); every array has `size` entries.  Replaces the
+ * reference's ParamTotUnordered + ComputeIVRTMTunstructured
+ * (rBergomi/ParamTot.h:57-75, rBergomi/rBergomiMT.cpp:837-938), the form
+ * calibration-style traffic sends. */
+typedef struct rbg_unordered {
+    double xi;
+    const double* H;
+    const double* eta;
+    const double* rho;
+    const double* T;
+    const double* K;
+    long size;
+    int N;
+    int64_t M;
+} rbg_unordered;
+
+/* Prices an unordered list on the Philox stream; price, stat, iv as for
+ * rbg_price_rt with `size` entries.  Tuples are not required to be sorted:
+ * equal H share one Volterra pass and equal (H, T, eta) one variance path. */
+int rbg_price_rt_unordered(const rbg_unordered* u, const rbg_options* o, double* price, double* stat, double* iv);
+
 /* Same, with the raw sums instead of finished moments: sum[i] = sum_m x,
  * sum2[i] = sum_m x^2 over this call's paths (for merging shards/replicas). */
 int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, double* sum2);
@@ -127,11 +164,23 @@ int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, do
  * device pointers on the current device.  FP64 only. */
 int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs);
 
+/* Plain Monte Carlo on the Philox stream (streams W1, W1perp, Wperp): the
+ * estimator of computeIV_tensor with status codes.  FP64 form only. */
+int rbg_price_mc(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv);
+
+/* Plain Monte Carlo per-path payoffs for caller-supplied normals: Z holds
+ * 3*N*M doubles, sample m uses Z[3mN + sN, 3mN + sN + N) for s = 0 (W1),
+ * 1 (W1perp), 2 (Wperp); payoff[m*out + i].  FP64 only. */
+int rbg_payoffs_mc(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs);
+
 /* Writes the normals the pricer would draw for paths
  * [path_offset, path_offset + M), N steps, streams W1 and W1perp, in the
  * quadrature layout (M * 2 * N doubles, host pointer).  precision selects the
  * FP64 or the FP32 transform (the latter widened exactly to double). */
 int rbg_generate_normals(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, double* Z);
+/* Same with 2 (RT) or 3 (plain MC: + Wperp) streams per path, M*streams*N doubles. */
+int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, int streams,
+                                 double* Z);
 
 /* Implied vols of call prices (S0 = 1, r = 0) on the GPU; NaN where no
  * volatility reproduces the price. */

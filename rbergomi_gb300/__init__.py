@@ -35,6 +35,11 @@ class RbgParams(C.Structure):
                 ("T", _dp), ("K", _dp), ("op_size", C.c_int), ("N", C.c_int), ("M", C.c_int64)]
 
 
+class RbgUnordered(C.Structure):
+    _fields_ = [("xi", C.c_double), ("H", _dp), ("eta", _dp), ("rho", _dp), ("T", _dp), ("K", _dp),
+                ("size", C.c_long), ("N", C.c_int), ("M", C.c_int64)]
+
+
 class RbgOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("conv", C.c_int), ("normals", C.c_int), ("split", C.c_int),
                 ("compute_iv", C.c_int), ("seed", C.c_uint64), ("path_offset", C.c_int64),
@@ -54,6 +59,7 @@ EXPORTS = [
     "rbg_profile_reset", "rbg_profile_read", "rbg_last_transfer_bytes", "rbg_debug_mixed_paths",
     "rbg_debug_mixed_profile", "rbg_server_default_config", "rbg_server_create", "rbg_server_submit",
     "rbg_server_poll", "rbg_server_wait", "rbg_server_get_stats", "rbg_server_destroy", "rbg_server_last_error",
+    "rbg_price_rt_unordered", "computeIV_tensor", "rbg_price_mc", "rbg_payoffs_mc", "rbg_generate_normals_streams",
 ]
 
 STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4
@@ -71,6 +77,8 @@ def lib():
                 C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int]
         L.computeIVRT_tensor.argtypes = full
         L.computeIVRT_tensor.restype = None
+        L.computeIV_tensor.argtypes = full
+        L.computeIV_tensor.restype = None
         L.computeIVRT_tensor_quadrature.argtypes = [C.c_double, _dp, _dp, _dp, C.c_int, _dp, _dp, C.c_int,
                                                     C.c_int, C.c_long, _dp, C.c_int, _dp]
         L.computeIVRT_tensor_quadrature.restype = None
@@ -82,6 +90,12 @@ def lib():
         L.rbg_price_rt_sums.restype = C.c_int
         L.rbg_payoffs_rt.argtypes = [P, O, C.c_void_p, C.c_void_p, C.c_int]
         L.rbg_payoffs_rt.restype = C.c_int
+        L.rbg_price_mc.argtypes = [P, O, _dp, _dp, _dp]
+        L.rbg_price_mc.restype = C.c_int
+        L.rbg_payoffs_mc.argtypes = [P, O, C.c_void_p, C.c_void_p, C.c_int]
+        L.rbg_payoffs_mc.restype = C.c_int
+        L.rbg_generate_normals_streams.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_int, _dp]
+        L.rbg_generate_normals_streams.restype = C.c_int
         L.rbg_generate_normals.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int, C.c_int, _dp]
         L.rbg_generate_normals.restype = C.c_int
         L.rbg_implied_vol.argtypes = [C.c_int, _dp, _dp, _dp, _dp]
@@ -163,6 +177,21 @@ class ResultSimple:
     numThreads: int
 
 
+def computeIV_tensor(xi, H, eta, rho, T, K, N, M, seed, num_threads=1) -> ResultSimple:
+    """Drop-in plain Monte Carlo pricing (rBergLib/cinterface.h:63-66) through
+    the C ABI.  As in the reference (cinterface.cpp:45) the library writes rho
+    into eta_tot and eta into rho_tot; the fields here are read back as the
+    C arrays hold them."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    seed = np.ascontiguousarray(np.atleast_1d(np.asarray(seed, dtype=np.uint64)))
+    outs = [np.empty(p.out) for _ in range(8)]
+    lib().computeIV_tensor(float(xi), p.s.H, p.s.eta, p.s.rho, p.s.par_size, p.s.T, p.s.K, p.s.op_size, int(N),
+                           int(M), seed.ctypes.data_as(_u64p), len(seed), int(num_threads),
+                           *[o.ctypes.data_as(_dp) for o in outs], p.out)
+    price, iv, stat, Ht, et, rt, Tt, Kt = outs
+    return ResultSimple(price, iv, Ht, rt, et, Tt, Kt, float(xi), stat, int(N), int(M), int(num_threads))
+
+
 def computeIVRT_tensor(xi, H, eta, rho, T, K, N, M, seed, num_threads=1) -> ResultSimple:
     """Drop-in RT pricing (rBergLib/cinterface.h:68-71) through the C ABI."""
     p = _Params(xi, H, eta, rho, T, K, N, M)
@@ -201,6 +230,22 @@ def price_rt(xi, H, eta, rho, T, K, N, M, **opts):
     return price, stat, iv
 
 
+def price_rt_unordered(xi, H, eta, rho, T, K, N, M, **opts):
+    """Unordered parameter list (the reference's ComputeIVRTMTunstructured,
+    rBergomi/rBergomiMT.cpp:837-938): output i prices (H[i], eta[i], rho[i],
+    T[i], K[i]).  Returns (price, stat, iv) arrays."""
+    arrs = [_arr(x) for x in (H, eta, rho, T, K)]
+    n = len(arrs[0])
+    if any(len(x) != n for x in arrs):
+        raise ValueError("H, eta, rho, T, K must have the same length")
+    u = RbgUnordered(float(xi), *[x.ctypes.data_as(_dp) for x in arrs], n, int(N), int(M))
+    o = options(**opts)
+    price, stat, iv = np.empty(n), np.empty(n), np.empty(n)
+    _check(lib().rbg_price_rt_unordered(C.byref(u), C.byref(o), price.ctypes.data_as(_dp),
+                                        stat.ctypes.data_as(_dp), iv.ctypes.data_as(_dp)))
+    return price, stat, iv
+
+
 def price_rt_sums(xi, H, eta, rho, T, K, N, M, **opts):
     """Extended API: raw (sum x, sum x^2) per output over this call's paths."""
     p = _Params(xi, H, eta, rho, T, K, N, M)
@@ -228,13 +273,36 @@ def payoffs_rt(xi, H, eta, rho, T, K, Z, device_ptrs=False, M=None, N=None, **op
     return pay
 
 
-def generate_normals(seed, M, N, precision=FP64, path_offset=0) -> np.ndarray:
-    """The normals the pricer draws: [M, 2, N] float64 (FP32 values widened
-    exactly when precision=MIXED)."""
-    Z = np.empty((M, 2, N))
-    _check(lib().rbg_generate_normals(int(seed) & 0xFFFFFFFFFFFFFFFF, int(path_offset), int(M), int(N),
-                                      int(precision), Z.ctypes.data_as(_dp)))
+def generate_normals(seed, M, N, precision=FP64, path_offset=0, streams=2) -> np.ndarray:
+    """The normals the pricer draws: [M, streams, N] float64 (FP32 values
+    widened exactly when precision=MIXED); streams=3 adds plain MC's Wperp."""
+    Z = np.empty((M, streams, N))
+    _check(lib().rbg_generate_normals_streams(int(seed) & 0xFFFFFFFFFFFFFFFF, int(path_offset), int(M), int(N),
+                                              int(precision), int(streams), Z.ctypes.data_as(_dp)))
     return Z
+
+
+def price_mc(xi, H, eta, rho, T, K, N, M, **opts):
+    """Plain Monte Carlo (the estimator behind computeIV_tensor): (price, stat, iv)."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    o = options(**opts)
+    price, stat, iv = np.empty(p.out), np.empty(p.out), np.empty(p.out)
+    _check(lib().rbg_price_mc(C.byref(p.s), C.byref(o), price.ctypes.data_as(_dp), stat.ctypes.data_as(_dp),
+                              iv.ctypes.data_as(_dp)))
+    return price, stat, iv
+
+
+def payoffs_mc(xi, H, eta, rho, T, K, Z, **opts):
+    """Plain MC per-path FP64 payoffs for host normals Z [M, 3, N]."""
+    o = options(**opts)
+    Z = np.ascontiguousarray(Z, dtype=np.float64)
+    M, three, N = Z.shape
+    if three != 3:
+        raise ValueError("Z must be [M, 3, N]")
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    pay = np.empty((M, p.out))
+    _check(lib().rbg_payoffs_mc(C.byref(p.s), C.byref(o), Z.ctypes.data, pay.ctypes.data, 0))
+    return pay
 
 
 def implied_vol(price, K, T) -> np.ndarray:

@@ -136,7 +136,7 @@ struct Ctx {
     int dev = -1;
     cudaStream_t stream = nullptr;
     std::mutex mu;
-    DevBuf z, ivb, part, acc, tabs, res, pay, mixed_ws;
+    DevBuf z, ivb, ivp, part, acc, tabs, res, pay, mixed_ws;
     ~Ctx() {}
 };
 
@@ -227,26 +227,30 @@ static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts
 // ------------------------------------------------------------ FP64 form
 static const int64_t kChunkTarget = 608;  // ~4 chunks per SM of a 152-SM part
 
-static int64_t fp64_batch(const Plan& plan, int64_t M)
+static int64_t fp64_batch(const Plan& plan, int64_t M, int ns = 2)
 {
-    // normals (16 N B/path) within 2 GiB, variance-path sums within 1 GiB
-    int64_t by_z = ((int64_t)1 << 31) / (16 * (int64_t)plan.N);
-    int64_t by_iv = ((int64_t)1 << 30) / (16 * (int64_t)std::max<size_t>(1, plan.vgs.size()));
+    // normals (8 ns N B/path) within 2 GiB, variance-path sums within 1 GiB
+    int64_t by_z = ((int64_t)1 << 31) / (8 * ns * (int64_t)plan.N);
+    int64_t by_iv = ((int64_t)1 << 30) / (8 * ns * (int64_t)std::max<size_t>(1, plan.vgs.size()));
     int64_t B = std::min(by_z, by_iv);
     B = std::max<int64_t>(256, B / 256 * 256);
     return std::min(B, M);
 }
 
+// mc: the plain Monte Carlo estimator (third normal stream Wperp, payoff
+// max(S_T - K, 0)) instead of the Romano-Touzi conditional price.
 static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M, cudaStream_t st,
-                      double* host_res)
+                      double* host_res, bool mc)
 {
     TableSet ts;
     int rc = upload_tables(c, plan, st, ts);
     if (rc) return rc;
-    const int no = (int)plan.outs.size(), N = plan.N;
-    const int64_t B = fp64_batch(plan, M);
-    if ((rc = ensure(c.z, sizeof(double) * 2 * N * (size_t)B, "normals"))) return rc;
+    const int no = (int)plan.outs.size(), N = plan.N, ns = mc ? 3 : 2;
+    const int64_t B = fp64_batch(plan, M, ns);
+    if ((rc = ensure(c.z, sizeof(double) * ns * N * (size_t)B, "normals"))) return rc;
     if ((rc = ensure(c.ivb, sizeof(double) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    if (mc && (rc = ensure(c.ivp, sizeof(double) * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    double* ivp = mc ? c.ivp.as<double>() : nullptr;
     const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
     const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
     if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
@@ -257,16 +261,17 @@ static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M,
         const int64_t b = std::min(B, M - m0);
         {
             ProfScope ps(kStageNormals, st);
-            launch_normals(o.seed, o.path_offset + m0, b, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st);
+            launch_normals(o.seed, o.path_offset + m0, b, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st,
+                           ns);
         }
         {
             ProfScope ps(kStagePathFp64, st);
-            launch_path_fp64(ts.t, c.z.as<double>(), b, c.ivb.as<double>(), st);
+            launch_path_fp64(ts.t, c.z.as<double>(), b, c.ivb.as<double>(), st, ivp);
         }
         const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
         {
             ProfScope ps(kStagePayoff, st);
-            launch_payoff_sums(ts.t, c.ivb.as<double>(), b, b, G, c.part.as<double>(), nchunks, st);
+            launch_payoff_sums(ts.t, c.ivb.as<double>(), b, b, G, c.part.as<double>(), nchunks, st, ivp);
         }
         {
             ProfScope ps(kStageReduce, st);
@@ -349,13 +354,8 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
     return RBG_OK;
 }
 
-static int price_any(const rbg_params* p, const rbg_options* o, std::vector<double>& res)
+static int price_plan(const Plan& plan, int64_t M, const rbg_options* o, std::vector<double>& res, bool mc = false)
 {
-    if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
-    g_h2d = g_d2h = 0;
-    Plan plan;
-    std::string err;
-    if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
     Ctx* c = nullptr;
     int rc = get_ctx(&c);
     if (rc) return rc;
@@ -365,18 +365,29 @@ static int price_any(const rbg_params* p, const rbg_options* o, std::vector<doub
     if (o->precision == RBG_FP64) {
         if (o->conv == RBG_CONV_GEMM || o->conv == RBG_CONV_FFT)
             return fail(RBG_ERR_UNSUPPORTED, "FP64 form uses the direct Volterra sum");
-        return price_fp64(*c, plan, *o, p->M, st, res.data());
+        return price_fp64(*c, plan, *o, M, st, res.data(), mc);
     }
-    if (o->precision == RBG_MIXED) return price_mixed(*c, plan, *o, p->M, st, res.data());
+    if (mc) return fail(RBG_ERR_UNSUPPORTED, "the plain Monte Carlo estimator runs in the FP64 form");
+    if (o->precision == RBG_MIXED) return price_mixed(*c, plan, *o, M, st, res.data());
     return fail(RBG_ERR_ARG, "unknown precision");
 }
 
+static int price_any(const rbg_params* p, const rbg_options* o, std::vector<double>& res, bool mc = false)
+{
+    if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
+    g_h2d = g_d2h = 0;
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err, mc)) return fail(RBG_ERR_ARG, err);
+    return price_plan(plan, p->M, o, res, mc);
+}
+
 static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payoff, int device_ptrs,
-                              cudaStream_t user_stream)
+                              cudaStream_t user_stream, bool mc = false)
 {
     Plan plan;
     std::string err;
-    if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
+    if (!build_plan(*p, plan, err, mc)) return fail(RBG_ERR_ARG, err);
     if (!Z || !payoff) return fail(RBG_ERR_ARG, "null Z/payoff");
     Ctx* c = nullptr;
     int rc = get_ctx(&c);
@@ -385,14 +396,16 @@ static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payo
     cudaStream_t st = user_stream ? user_stream : c->stream;
     TableSet ts;
     if ((rc = upload_tables(*c, plan, st, ts))) return rc;
-    const int no = (int)plan.outs.size(), N = plan.N;
+    const int no = (int)plan.outs.size(), N = plan.N, ns = mc ? 3 : 2;
     const int64_t M = p->M;
-    int64_t B = fp64_batch(plan, M);
+    int64_t B = fp64_batch(plan, M, ns);
     // payoffs of a batch within 1 GiB too
     B = std::min<int64_t>(B, std::max<int64_t>(256, ((int64_t)1 << 30) / (8 * (int64_t)no)));
     if ((rc = ensure(c->ivb, sizeof(double) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    if (mc && (rc = ensure(c->ivp, sizeof(double) * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    double* ivp = mc ? c->ivp.as<double>() : nullptr;
     if (!device_ptrs) {
-        if ((rc = ensure(c->z, sizeof(double) * 2 * N * (size_t)B, "normals"))) return rc;
+        if ((rc = ensure(c->z, sizeof(double) * ns * N * (size_t)B, "normals"))) return rc;
         if ((rc = ensure(c->pay, sizeof(double) * no * (size_t)B, "payoffs"))) return rc;
     }
     for (int64_t m0 = 0; m0 < M; m0 += B) {
@@ -400,15 +413,16 @@ static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payo
         const double* Zd;
         double* Pd;
         if (device_ptrs) {
-            Zd = Z + m0 * 2 * N;
+            Zd = Z + m0 * ns * N;
             Pd = payoff + m0 * no;
         } else {
-            RBG_CUDA(cudaMemcpyAsync(c->z.p, Z + m0 * 2 * N, sizeof(double) * 2 * N * b, cudaMemcpyHostToDevice, st));
+            RBG_CUDA(cudaMemcpyAsync(c->z.p, Z + m0 * ns * N, sizeof(double) * ns * N * b, cudaMemcpyHostToDevice,
+                                     st));
             Zd = c->z.as<double>();
             Pd = c->pay.as<double>();
         }
-        launch_path_fp64(ts.t, Zd, b, c->ivb.as<double>(), st);
-        launch_payoff_store(ts.t, c->ivb.as<double>(), b, b, Pd, st);
+        launch_path_fp64(ts.t, Zd, b, c->ivb.as<double>(), st, ivp);
+        launch_payoff_store(ts.t, c->ivb.as<double>(), b, b, Pd, st, ivp);
         RBG_CUDA(cudaGetLastError());
         if (!device_ptrs)
             RBG_CUDA(cudaMemcpyAsync(payoff + m0 * no, Pd, sizeof(double) * no * b, cudaMemcpyDeviceToHost, st));
@@ -451,6 +465,23 @@ int rbg_price_rt(const rbg_params* p, const rbg_options* o, double* price, doubl
     return RBG_OK;
 }
 
+int rbg_price_rt_unordered(const rbg_unordered* u, const rbg_options* o, double* price, double* stat, double* iv)
+{
+    if (!u || !o) return fail(RBG_ERR_ARG, "null params/options");
+    g_h2d = g_d2h = 0;
+    Plan plan;
+    std::string err;
+    if (!build_plan_unordered(*u, plan, err)) return fail(RBG_ERR_ARG, err);
+    std::vector<double> res;
+    int rc = price_plan(plan, u->M, o, res);
+    if (rc) return rc;
+    const size_t no = res.size() / 5;
+    if (price) std::memcpy(price, res.data(), no * sizeof(double));
+    if (stat) std::memcpy(stat, res.data() + no, no * sizeof(double));
+    if (iv) std::memcpy(iv, res.data() + 2 * no, no * sizeof(double));
+    return RBG_OK;
+}
+
 int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, double* sum2)
 {
     std::vector<double> res;
@@ -469,24 +500,51 @@ int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, d
     return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr);
 }
 
-int rbg_generate_normals(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, double* Z)
+int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, int streams,
+                                 double* Z)
 {
     if (M < 1 || N < 1 || !Z) return fail(RBG_ERR_ARG, "bad sizes");
+    if (streams != 2 && streams != 3) return fail(RBG_ERR_ARG, "streams must be 2 or 3");
     Ctx* c = nullptr;
     int rc = get_ctx(&c);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
-    const int64_t B = std::max<int64_t>(1, std::min<int64_t>(M, ((int64_t)1 << 30) / (16 * (int64_t)N)));
-    if ((rc = ensure(c->z, sizeof(double) * 2 * N * (size_t)B, "normals"))) return rc;
+    const int ns = streams;
+    const int64_t B = std::max<int64_t>(1, std::min<int64_t>(M, ((int64_t)1 << 30) / (8 * ns * (int64_t)N)));
+    if ((rc = ensure(c->z, sizeof(double) * ns * N * (size_t)B, "normals"))) return rc;
     for (int64_t m0 = 0; m0 < M; m0 += B) {
         const int64_t b = std::min(B, M - m0);
-        launch_normals(seed, path_offset + m0, b, N, precision == RBG_MIXED, c->z.as<double>(), c->stream);
+        launch_normals(seed, path_offset + m0, b, N, precision == RBG_MIXED, c->z.as<double>(), c->stream, ns);
         RBG_CUDA(cudaGetLastError());
-        RBG_CUDA(cudaMemcpyAsync(Z + m0 * 2 * N, c->z.p, sizeof(double) * 2 * N * b, cudaMemcpyDeviceToHost,
+        RBG_CUDA(cudaMemcpyAsync(Z + m0 * ns * N, c->z.p, sizeof(double) * ns * N * b, cudaMemcpyDeviceToHost,
                                  c->stream));
     }
     RBG_CUDA(cudaStreamSynchronize(c->stream));
     return RBG_OK;
+}
+
+int rbg_generate_normals(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, double* Z)
+{
+    return rbg_generate_normals_streams(seed, path_offset, M, N, precision, 2, Z);
+}
+
+int rbg_price_mc(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv)
+{
+    std::vector<double> res;
+    int rc = price_any(p, o, res, true);
+    if (rc) return rc;
+    const size_t no = res.size() / 5;
+    if (price) std::memcpy(price, res.data(), no * sizeof(double));
+    if (stat) std::memcpy(stat, res.data() + no, no * sizeof(double));
+    if (iv) std::memcpy(iv, res.data() + 2 * no, no * sizeof(double));
+    return RBG_OK;
+}
+
+int rbg_payoffs_mc(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs)
+{
+    if (!p) return fail(RBG_ERR_ARG, "null params");
+    if (o && o->precision != RBG_FP64) return fail(RBG_ERR_UNSUPPORTED, "per-path payoffs are FP64 only");
+    return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr, true);
 }
 
 int rbg_implied_vol(int n, const double* price, const double* K, const double* T, double* iv)
@@ -525,7 +583,8 @@ int rbg_release(void)
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     RBG_CUDA(cudaStreamSynchronize(c->stream));
-    for (DevBuf* b : {&c->z, &c->ivb, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws}) b->release();
+    for (DevBuf* b : {&c->z, &c->ivb, &c->ivp, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws})
+        b->release();
     return RBG_OK;
 }
 
@@ -683,10 +742,7 @@ static uint64_t fold_seed(const uint64_t* seed, int seed_size)
     return h;
 }
 
-void computeIVRT_tensor(double xi, double* H, double* eta, double* rho, int par_size, double* T, double* K,
-                        int op_size, int N, long M, uint64_t* seed, int seed_size, int num_threads, double* price,
-                        double* iv, double* stat, double* H_tot, double* eta_tot, double* rho_tot, double* T_tot,
-                        double* K_tot, int out_size)
+static void check_dropin_sizes(int par_size, int op_size, int num_threads, int out_size)
 {
     if (out_size != par_size * op_size) {
         std::cerr << "Output arrays have wrong size:\n"
@@ -698,6 +754,32 @@ void computeIVRT_tensor(double xi, double* H, double* eta, double* rho, int par_
                   << "obtained num_threads = " << num_threads << ".\n";
         std::exit(21);
     }
+}
+
+// Plain Monte Carlo (rBergLib/cinterface.cpp:10-46): FP64 form, third normal
+// stream, payoff max(S_T - K, 0).  The reference hands rho_tot and eta_tot to
+// Result2Array in swapped order (cinterface.cpp:45), so eta_tot receives the
+// rho values and rho_tot the eta values; kept for drop-in compatibility.
+void computeIV_tensor(double xi, double* H, double* eta, double* rho, int par_size, double* T, double* K,
+                      int op_size, int N, long M, uint64_t* seed, int seed_size, int num_threads, double* price,
+                      double* iv, double* stat, double* H_tot, double* eta_tot, double* rho_tot, double* T_tot,
+                      double* K_tot, int out_size)
+{
+    check_dropin_sizes(par_size, op_size, num_threads, out_size);
+    rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
+    rbg_options o;
+    rbg_default_options(&o);
+    o.seed = fold_seed(seed, seed_size);
+    die_on(rbg_price_mc(&p, &o, price, stat, iv));
+    fill_tot(H, eta, rho, par_size, T, K, op_size, H_tot, rho_tot, eta_tot, T_tot, K_tot);
+}
+
+void computeIVRT_tensor(double xi, double* H, double* eta, double* rho, int par_size, double* T, double* K,
+                        int op_size, int N, long M, uint64_t* seed, int seed_size, int num_threads, double* price,
+                        double* iv, double* stat, double* H_tot, double* eta_tot, double* rho_tot, double* T_tot,
+                        double* K_tot, int out_size)
+{
+    check_dropin_sizes(par_size, op_size, num_threads, out_size);
     rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
     rbg_options o;
     rbg_default_options(&o);

@@ -124,6 +124,17 @@ __device__ __forceinline__ double rt_payoff(double Ivdt, double IsvdW, double rh
     return bs_call_tau1(spot, K, vol);
 }
 
+// Plain Monte Carlo payoff (rBergLib/rBergomiMT.cpp:134-136 updateZ, :129-132
+// scaleZ, :111-116 updateS, aux.h:31-34 posPart): with Z = rho W1 + sqrt(1 - rho^2) Wperp,
+// log S = sum sqrt(v) sdt Z - dt/2 sum v = rho IsvdW + sqrt(1 - rho^2) IsvdWp
+// - Ivdt / 2, the same sum regrouped by normal stream.
+__device__ __forceinline__ double mc_payoff(double Ivdt, double IsvdW, double IsvdWp, double rho, double K)
+{
+    const double S = exp(rho * IsvdW + sqrt(1.0 - rho * rho) * IsvdWp - 0.5 * Ivdt);
+    const double d = S - K;
+    return d > 0.0 ? d : 0.0;
+}
+
 // Neumaier compensated accumulation.
 __device__ __forceinline__ void neumaier_add(double& s, double& c, double x)
 {

@@ -23,17 +23,18 @@
 namespace rbg {
 
 // ------------------------------------------------------------------ normals
+// Z[m][s][j], s < ns: W1, W1perp and (plain MC) Wperp on Philox streams 0, 1, 2.
 template <int F32>
-__global__ void k_normals(uint64_t seed, int64_t path0, int64_t B, int N, double* __restrict__ Z)
+__global__ void k_normals(uint64_t seed, int64_t path0, int64_t B, int N, int ns, double* __restrict__ Z)
 {
     const int ng = (N + 3) >> 2;
-    const int64_t total = B * 2 * ng;
+    const int64_t total = B * ns * ng;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int g = (int)(t % ng);
         const int64_t r = t / ng;
-        const int s = (int)(r & 1);
-        const int64_t m = r >> 1;
+        const int s = (int)(r % ns);
+        const int64_t m = r / ns;
         const uint4 x = philox_group(seed, (uint64_t)(path0 + m), (uint32_t)g, (uint32_t)s);
         double z[4];
         if (F32) {
@@ -45,7 +46,7 @@ __global__ void k_normals(uint64_t seed, int64_t path0, int64_t B, int N, double
             box_muller_f64(x.x, x.y, z[0], z[1]);
             box_muller_f64(x.z, x.w, z[2], z[3]);
         }
-        double* o = Z + (m * 2 + s) * (int64_t)N + 4 * g;
+        double* o = Z + (m * ns + s) * (int64_t)N + 4 * g;
         const int left = N - 4 * g;
         if (left >= 4) {
             o[0] = z[0]; o[1] = z[1]; o[2] = z[2]; o[3] = z[3];
@@ -55,21 +56,24 @@ __global__ void k_normals(uint64_t seed, int64_t path0, int64_t B, int N, double
     }
 }
 
-void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream)
+void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream, int ns)
 {
-    const int64_t total = B * 2 * ((N + 3) / 4);
+    const int64_t total = B * ns * ((N + 3) / 4);
     const int threads = 256;
     int64_t blocks = (total + threads - 1) / threads;
     if (blocks > (1 << 20)) blocks = 1 << 20;
-    if (f32) k_normals<1><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(seed, path0, B, N, Z);
-    else k_normals<0><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(seed, path0, B, N, Z);
+    if (f32) k_normals<1><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(seed, path0, B, N, ns, Z);
+    else k_normals<0><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(seed, path0, B, N, ns, Z);
     count_launch();
 }
 
 // --------------------------------------------------------------- path pass
 // One warp per path.  Shared memory: Gamma of the current pass (N doubles),
-// then per warp W1 (N) and X (N).
-__global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t B, double2* __restrict__ ivb)
+// then per warp W1 (N) and X (N).  NS = 3 (plain MC) also sums
+// IsvdWp = sum sqrt(v) sdt Wperp into ivp.
+template <int NS>
+__global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t B, double2* __restrict__ ivb,
+                            double* __restrict__ ivp)
 {
     extern __shared__ double sm[];
     const int N = t.N;
@@ -80,8 +84,9 @@ __global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t 
     double* X = W1s + N;
     const int64_t m = (int64_t)blockIdx.x * warps + w;
     const bool active = m < B;
-    const double* W1 = Z + m * 2 * (int64_t)N;
+    const double* W1 = Z + m * NS * (int64_t)N;
     const double* W1p = W1 + N;
+    const double* Wperp = W1 + 2 * N;  // NS = 3 only
     if (active)
         for (int j = lane; j < N; j += 32) W1s[j] = W1[j];
 
@@ -101,18 +106,24 @@ __global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t 
         for (int g = vol.vg_begin; g < vol.vg_end; ++g) {
             const VGDev vg = t.vgs[g];
             const double* comp = t.comp + (size_t)g * N;
-            double sv = 0.0, sw = 0.0;
+            double sv = 0.0, sw = 0.0, sp = 0.0;
             for (int j = lane; j < vg.nsteps; j += 32) {
                 const double vj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * X[j - 1]) - comp[j - 1]);
                 sv += vj;
-                sw += sqrt(vj) * vg.sdt * W1s[j];
+                const double sq = sqrt(vj) * vg.sdt;
+                sw += sq * W1s[j];
+                if (NS == 3) sp += sq * Wperp[j];
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 sv += __shfl_xor_sync(0xffffffffu, sv, o);
                 sw += __shfl_xor_sync(0xffffffffu, sw, o);
+                if (NS == 3) sp += __shfl_xor_sync(0xffffffffu, sp, o);
             }
-            if (lane == 0) ivb[(size_t)g * B + m] = make_double2(vg.dt * sv, sw);
+            if (lane == 0) {
+                ivb[(size_t)g * B + m] = make_double2(vg.dt * sv, sw);
+                if (NS == 3) ivp[(size_t)g * B + m] = sp;
+            }
         }
         __syncwarp();
     }
@@ -130,17 +141,21 @@ int path_fp64_warps(int N)
 
 size_t path_fp64_smem(int N, int warps) { return 8 * (size_t)N + (size_t)warps * 16 * N; }
 
-void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream)
+void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream, double* ivp)
 {
     const int warps = path_fp64_warps(t.N);
     const size_t smem = path_fp64_smem(t.N, warps);
     static size_t configured = 0;
     if (smem > configured) {
-        cudaFuncSetAttribute(k_path_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_path_fp64<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_path_fp64<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = smem;
     }
     const int64_t blocks = (B + warps - 1) / warps;
-    k_path_fp64<<<(unsigned)blocks, warps * 32, smem, (cudaStream_t)stream>>>(t, Z, B, (double2*)ivb);
+    if (ivp)
+        k_path_fp64<3><<<(unsigned)blocks, warps * 32, smem, (cudaStream_t)stream>>>(t, Z, B, (double2*)ivb, ivp);
+    else
+        k_path_fp64<2><<<(unsigned)blocks, warps * 32, smem, (cudaStream_t)stream>>>(t, Z, B, (double2*)ivb, ivp);
     count_launch();
 }
 
@@ -150,8 +165,11 @@ constexpr int kOPB = 8;  // outputs per block
 // grid (nchunks, ceil(n_out / kOPB)), 256 threads; chunk c covers paths
 // [c G 256, (c+1) G 256) of the batch; part[(c * n_out + i) * 4 + {0,1,2,3}] =
 // (sum, comp, sum2, comp2).
+// MC = 1: plain Monte Carlo payoff from (Ivdt, IsvdW) and ivp = IsvdWp.
+template <int MC>
 __global__ void __launch_bounds__(256) k_payoff_sums(Fp64Tables t, const double2* __restrict__ ivb, int64_t B,
-                                                     int64_t stride, int G, double* __restrict__ part)
+                                                     int64_t stride, int G, double* __restrict__ part,
+                                                     const double* __restrict__ ivp)
 {
     __shared__ double red[8][kOPB][2];
     const int c = blockIdx.x;
@@ -170,8 +188,9 @@ __global__ void __launch_bounds__(256) k_payoff_sums(Fp64Tables t, const double2
         for (int q = 0; q < kOPB; ++q) {
             double x = 0.0;
             if (m < B && od[q].vg >= 0) {
-                const double2 iv = ivb[(size_t)od[q].vg * stride + m];
-                x = rt_payoff(iv.x, iv.y, od[q].rho, od[q].K);
+                const size_t at = (size_t)od[q].vg * stride + m;
+                const double2 iv = ivb[at];
+                x = MC ? mc_payoff(iv.x, iv.y, ivp[at], od[q].rho, od[q].K) : rt_payoff(iv.x, iv.y, od[q].rho, od[q].K);
             }
             double x2 = x * x;
 #pragma unroll
@@ -198,10 +217,13 @@ __global__ void __launch_bounds__(256) k_payoff_sums(Fp64Tables t, const double2
 }
 
 void launch_payoff_sums(const Fp64Tables& t, const double* ivb, int64_t B, int64_t stride, int G, double* part,
-                        int nchunks, void* stream)
+                        int nchunks, void* stream, const double* ivp)
 {
     dim3 grid(nchunks, (t.n_out + kOPB - 1) / kOPB);
-    k_payoff_sums<<<grid, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride, G, part);
+    if (ivp)
+        k_payoff_sums<1><<<grid, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride, G, part, ivp);
+    else
+        k_payoff_sums<0><<<grid, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride, G, part, ivp);
     count_launch();
 }
 
@@ -342,8 +364,9 @@ void launch_implied_vol(int n, const double* price, const double* K, const doubl
 }
 
 // ------------------------------------------------------------ quadrature
+template <int MC>
 __global__ void k_payoff_store(Fp64Tables t, const double2* __restrict__ ivb, int64_t B, int64_t stride,
-                               double* __restrict__ payoff)
+                               double* __restrict__ payoff, const double* __restrict__ ivp)
 {
     const int64_t total = B * t.n_out;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
@@ -351,18 +374,24 @@ __global__ void k_payoff_store(Fp64Tables t, const double2* __restrict__ ivb, in
         const int64_t m = idx / t.n_out;
         const int i = (int)(idx - m * t.n_out);
         const OutDev od = t.outs[i];
-        const double2 iv = ivb[(size_t)od.vg * stride + m];
-        payoff[idx] = rt_payoff(iv.x, iv.y, od.rho, od.K);
+        const size_t at = (size_t)od.vg * stride + m;
+        const double2 iv = ivb[at];
+        payoff[idx] = MC ? mc_payoff(iv.x, iv.y, ivp[at], od.rho, od.K) : rt_payoff(iv.x, iv.y, od.rho, od.K);
     }
 }
 
 void launch_payoff_store(const Fp64Tables& t, const double* ivb, int64_t B, int64_t stride, double* payoff,
-                         void* stream)
+                         void* stream, const double* ivp)
 {
     const int64_t total = B * t.n_out;
     int64_t blocks = (total + 255) / 256;
     if (blocks > (1 << 20)) blocks = 1 << 20;
-    k_payoff_store<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride, payoff);
+    if (ivp)
+        k_payoff_store<1><<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride,
+                                                                             payoff, ivp);
+    else
+        k_payoff_store<0><<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride,
+                                                                             payoff, ivp);
     count_launch();
 }
 

@@ -51,7 +51,12 @@ struct Plan {
 // (rBergLib/ParamTot.h:28-43, eps 1e-10 at ParamTot.cpp:27).  Volterra passes
 // are deduplicated by exact H value, variance groups by exact tuple.
 // Returns false and sets err on invalid input.
-bool build_plan(const rbg_params& p, Plan& plan, std::string& err);
+// plain_mc: outputs carry the rho of the last H/T/eta/rho trigger, the
+// state the reference's plain Monte Carlo driver prices S with.
+bool build_plan(const rbg_params& p, Plan& plan, std::string& err, bool plain_mc = false);
+// The unordered form: one output per tuple, every tuple's chain recomputed
+// as the reference's updatePayoffUnordered does (equal tuples share state).
+bool build_plan_unordered(const rbg_unordered& u, Plan& plan, std::string& err);
 
 // ---- device-side views -------------------------------------------------
 struct VolDev {
@@ -78,17 +83,20 @@ struct Fp64Tables {
     double xi;
 };
 
-void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream);
+// ns normal streams per path: 2 (W1, W1perp) for RT, 3 (+ Wperp) for plain MC
+void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream, int ns = 2);
 int path_fp64_warps(int N);
 size_t path_fp64_smem(int N, int warps);
-void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream);
+// ivp non-null: Z has three streams per path (plain MC) and ivp[g][B] gets IsvdWp
+void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream,
+                      double* ivp = nullptr);
 void launch_payoff_sums(const Fp64Tables& t, const double* ivb, int64_t B, int64_t ivb_stride, int G,
-                        double* part, int nchunks, void* stream);
+                        double* part, int nchunks, void* stream, const double* ivp = nullptr);
 void launch_accumulate(const double* part, int nchunks, int n_out, double* acc, void* stream);
 void launch_finalize(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,
                      int compute_iv, double* res, void* stream);
 void launch_payoff_store(const Fp64Tables& t, const double* ivb, int64_t B, int64_t ivb_stride, double* payoff,
-                         void* stream);
+                         void* stream, const double* ivp = nullptr);
 void launch_implied_vol(int n, const double* price, const double* K, const double* T, double* iv, void* stream);
 
 // Kernel-launch counter shared by all launchers.

@@ -17,21 +17,29 @@
 // Toeplitz structure.  Time steps are cut into K-chunks of 32.  Chunk c
 // multiplies the A tile W1[:, 32c, 32c+32) into output columns [32c, Np):
 //   D[:, 32c + j'] += sum_{k'<32} A_c[:, k'] * S[j'][k'],  S[j'][k'] = Gamma[j' - k'],
-// and S does not depend on c.  So one 32 x Np strip S (hi and lo halves,
+// and S does not depend on c.  So one Np x 32 strip S (hi and lo halves,
 // 64 KB at N = 512) stays resident in shared memory for the whole kernel,
-// loaded once by a bulk async copy; only A tiles stream.  After chunk c's
-// MMAs, columns [32c, 32c+32) are final and the epilogue reads them.
+// loaded once by a bulk async copy; only A tiles stream.  Two-pass tiles
+// (below) use a narrow strip instead: the two K = 16 halves of a chunk read
+// the same 16-wide P[r][k''] = Gamma[r - 16 - k''] at row offsets 16 apart,
+// (Np + 16) x 16 (65 KB at N = 1024).  After chunk c's MMAs, columns
+// [32c, 32c+32) are final and the epilogue reads them.
 //
-// Warp roles (672 threads, one CTA per SM, persistent over 128-path tiles):
-//   warps 0-15  producers, four threads per path, 8 steps each per chunk:
+// TMEM holds 128 lanes x 512 FP32 columns.  For 512 < Np <= 1024 a tile runs
+// two passes: pass 0 accumulates columns [0, P0), P0 = Np - 512, from chunks
+// 0 .. n0-1 (n0 = P0 / 32); pass 1 accumulates the last 512 columns from the
+// A tiles of chunks 0 .. n0-1 drawn again (W1 only, no epilogue work), then
+// from chunks n0 .. nc-1.  Per tile the producers' virtual chunk sequence is
+//   [0, n0) real | [0, n0) redrawn | [n0, nc) real      (n0 = 0: one pass).
+//
+// Warp roles (544 threads, one CTA per SM, persistent over 128-path tiles):
+//   warps 0-7   producers, two threads per path, 16 steps each per chunk:
 //               Philox -> FP32 normals; W1 split into hi/lo 16-bit A tiles
 //               (SW64 K-major layout); FP32 W1, W1perp kept for the epilogue
-//   warps 16-19 epilogue, one per TMEM lane quadrant: tcgen05.ld of 2 x 16
-//               accumulator columns per chunk, X = Y2 + a1 W1 + a2 W1perp, v
-//               and the two integrals; when a launch prices <= 64 outputs,
-//               also the FP32 conditional BS payoffs of its paths, summed per
-//               warp and accumulated in FP64 (one partial row per CTA)
-//   warp 20     TMEM allocation and the single-thread tcgen05.mma issuer
+//   warps 8-15  epilogue, two warpgroups (16 accumulator columns each per
+//               chunk), one TMEM lane quadrant per warp: tcgen05.ld,
+//               X = Y2 + a1 W1 + a2 W1perp, v and the two integrals
+//   warp 16     TMEM allocation and the single-thread tcgen05.mma issuer
 // Every mbarrier wait is bounded (%globaltimer); on expiry the kernel records
 // an error word, drains its MMAs, frees TMEM and returns.
 #include <cuda_bf16.h>
@@ -65,20 +73,32 @@ constexpr int kStepsPerThread = kChunk * 4 / kProdWarps;  // producer steps per 
 constexpr int kEpiWarp0 = kProdWarps;               // warps 8..15: TMEM lane quadrant = warp % 4
 constexpr int kMmaWarp = kProdWarps + kEpiWarps;    // warp 16
 constexpr int kThreads = (kMmaWarp + 1) * 32;       // 544
-constexpr int kMaxNp = 512;                         // TMEM: 128 lanes x 512 FP32 columns
+constexpr int kPassCols = 512;                      // TMEM: 128 lanes x 512 FP32 columns per pass
+constexpr int kMaxNp = 2 * kPassCols;               // two passes
+constexpr int kStripK = 16;                         // narrow strip width: one K = 16 MMA step
+constexpr int kHPerPath = kProdWarps * 32 / kTileM; // producer threads per path
 constexpr uint64_t kWaitNs = 2000000000ull;         // 2 s per wait
 
 // shared-memory layout (offsets from a 1024-aligned base):
-//   [strip hi | strip lo]            2 * Np * 64 B, SW64 K-major
+//   [strip hi | strip lo]            2 * Np * 64 B, SW64 (one pass), or 2 * (Np + 16) * 32 B, SW32
 //   A tiles, per stage [hi | lo]     16 KB per stage (1024-aligned)
-//   FP32 tiles, per stage            w1 [32][128], w1perp [32][128]
+//   FP32 tiles, per stage            w1 [32][128], w1perp [32][128], W1 of step P0 [128]
 //   per-thread group sums            n_g * 2 * 128 floats
 //   beta tables                      n_g * Np floats
 //   fused outputs                    table n_o * 4 floats, FP32 Kahan sums [4 warps][n_o][4]
 //   mbarriers + TMEM address
 constexpr int kTileBytes = kTileM * kChunk * 2;                          // one 16-bit 128 x 32 tile, 8 KB
 constexpr int kStageA = 2 * kTileBytes;                                  // hi + lo
-constexpr int kStageF = 2 * kChunk * kTileM * 4;                         // w1, w1perp
+constexpr int kStageF = (2 * kChunk + 1) * kTileM * 4;                   // w1, w1perp, boundary W1
+
+// Strip width in K: the full chunk (32, SW64 rows, one row per output
+// column) where one TMEM pass covers Np; 16 (SW32, 16 leading zero rows)
+// for two-pass tiles, whose Np-row strip would not fit shared memory at 32.
+__host__ __device__ inline int strip_k(int Np) { return Np <= kPassCols ? kChunk : kStripK; }
+__host__ __device__ inline int strip_bytes(int Np)
+{
+    return strip_k(Np) == kChunk ? 2 * Np * kChunk * 2 : 2 * (Np + kStripK) * kStripK * 2;
+}
 
 struct SmemLayout {
     int strip, a0, f0, stages, acc, beta, otab, osum, bars, total;
@@ -88,7 +108,7 @@ __host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, i
 {
     SmemLayout L;
     L.strip = 0;
-    L.a0 = ((2 * Np * 64) + 1023) / 1024 * 1024;
+    L.a0 = (strip_bytes(Np) + 1023) / 1024 * 1024;
     L.stages = stages;
     L.f0 = L.a0 + stages * kStageA;
     L.acc = L.f0 + stages * kStageF;
@@ -183,6 +203,14 @@ __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t addr)
            ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
 }
 
+// SW32 K-major descriptor for the 16-wide strip: 32-byte rows, SBO = 8 rows
+// x 32 B, layout type SWIZZLE_32B (6).
+__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t addr)
+{
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(256 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)6 << 61);
+}
+
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16 (1) or F16 (0),
 // both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
 __device__ __forceinline__ uint32_t idesc_f16(int n, int ab_bf16)
@@ -275,7 +303,77 @@ __device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rh
     return spot * phi_f32(d1) - K * phi_f32(d2);
 }
 
-template <int BF16>
+// One producer thread's share of a chunk: Philox -> FP32 normals for steps
+// [32 c + SPT h, + SPT) of path p, its hi/lo row of the A tile and, unless
+// REDRAW (a first-pass chunk drawn again for the second pass), the FP32 W1 /
+// W1perp tiles the epilogue reads.  Compiled per REDRAW so that the W1 and
+// W1perp Philox streams stay interleaved in the common case.
+template <int BF16, bool REDRAW>
+__device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKeys& keys, uint64_t gpath, bool valid,
+                                              int64_t m, int p, int h, int c, int n0, unsigned char* st,
+                                              float* w1s)
+{
+    constexpr int SPT = kStepsPerThread;
+    const int Np = a.Np;
+    const int sw = (p >> 1) & 3;
+    float* w1ps = w1s + kChunk * kTileM;
+    const int step0 = kChunk * c + SPT * h;
+    float w[SPT], wp[SPT];
+#pragma unroll
+    for (int q = 0; q < SPT / 4; ++q) {
+        const uint32_t g = (uint32_t)((step0 >> 2) + q);
+        const uint4 x0 = philox_group(keys, gpath, g, 0);
+        box_muller_f32(x0.x, x0.y, w[4 * q], w[4 * q + 1]);
+        box_muller_f32(x0.z, x0.w, w[4 * q + 2], w[4 * q + 3]);
+        if (!REDRAW) {
+            const uint4 x1 = philox_group(keys, gpath, g, 1);
+            box_muller_f32(x1.x, x1.y, wp[4 * q], wp[4 * q + 1]);
+            box_muller_f32(x1.z, x1.w, wp[4 * q + 2], wp[4 * q + 3]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < SPT; ++q) {
+        if (!valid || step0 + q >= a.N) { w[q] = 0.f; wp[q] = 0.f; }
+    }
+    // A tile: row p, logical 16-byte chunks covering steps [SPT h, SPT h + SPT), SW64 swizzle
+    uint32_t hi[SPT / 2], lo[SPT / 2];
+#pragma unroll
+    for (int q = 0; q < SPT / 2; ++q) split2<BF16>(w[2 * q], w[2 * q + 1], hi[q], lo[q]);
+#pragma unroll
+    for (int e = 0; e < SPT / 8; ++e) {
+        const int off = p * 64 + ((((SPT / 8) * h + e) ^ sw) << 4);
+        *(uint4*)(st + off) = make_uint4(hi[4 * e], hi[4 * e + 1], hi[4 * e + 2], hi[4 * e + 3]);
+        *(uint4*)(st + kTileBytes + off) = make_uint4(lo[4 * e], lo[4 * e + 1], lo[4 * e + 2], lo[4 * e + 3]);
+    }
+    if (!REDRAW) {
+#pragma unroll
+        for (int q = 0; q < SPT; ++q) {
+            w1s[(SPT * h + q) * kTileM + p] = w[q];
+            w1ps[(SPT * h + q) * kTileM + p] = wp[q];
+        }
+        // last chunk of the first pass: its successor (chunk n0) follows the
+        // redrawn chunks, so W1 at step 32 n0 for the last column's sqrt(v) dW
+        // goes into this stage's boundary row
+        if (c == n0 - 1 && h == kHPerPath - 1) {
+            const uint4 xb = philox_group(keys, gpath, (uint32_t)(8 * n0), 0);
+            float b0, b1;
+            box_muller_f32(xb.x, xb.y, b0, b1);
+            w1s[2 * kChunk * kTileM + p] = valid ? b0 : 0.f;
+        }
+        if (a.dbg_w && valid) {
+#pragma unroll
+            for (int q = 0; q < SPT; ++q) {
+                a.dbg_w[(m * 2 + 0) * Np + step0 + q] = w[q];
+                a.dbg_w[(m * 2 + 1) * Np + step0 + q] = wp[q];
+            }
+        }
+    }
+}
+
+// TWO: two TMEM passes per tile (512 < Np <= 1024).  The one-pass
+// instantiation has n0 = 0 at compile time, so the virtual-chunk bookkeeping
+// folds away there.
+template <int BF16, bool TWO>
 __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
     extern __shared__ unsigned char smem_raw[];
@@ -299,9 +397,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     uint32_t* tmem_holder = (uint32_t*)(bars + 12);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int Np = a.Np, nc = a.nc;
+    const int Np = a.Np, nc = a.nc, n0 = TWO ? a.n0 : 0;
+    const int nv = nc + n0;  // virtual chunks per tile
     const int64_t ntiles = (a.B + kTileM - 1) / kTileM;
-    const uint32_t strip_bytes = (uint32_t)(2 * Np * 64);
+    const uint32_t sbytes = (uint32_t)strip_bytes(Np);
 
     if (threadIdx.x == kMmaWarp * 32) {
         for (int s = 0; s < S; ++s) {
@@ -313,11 +412,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         mbar_init(smem_u32(strip_bar), 1);
         mbar_init(smem_u32(final_bar), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        mbar_expect_tx(smem_u32(strip_bar), strip_bytes);
+        mbar_expect_tx(smem_u32(strip_bar), sbytes);
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                 smem_u32(strip)),
-            "l"(a.strip), "r"(strip_bytes), "r"(smem_u32(strip_bar))
+            "l"(a.strip), "r"(sbytes), "r"(smem_u32(strip_bar))
             : "memory");
     }
     if (warp == kMmaWarp) {
@@ -340,61 +439,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         // ------------------------------------------------------- producers
         const int p = threadIdx.x & (kTileM - 1);
         const int h = threadIdx.x >> 7;  // which kStepsPerThread steps of the chunk
-        constexpr int SPT = kStepsPerThread;
         const PhiloxKeys keys = philox_keys(a.seed);
-        const int sw = (p >> 1) & 3;
         int64_t lt = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
             const int64_t m = tile * kTileM + p;
             const bool valid = m < a.B;
             const uint64_t gpath = (uint64_t)(a.path0 + m);
-            for (int c = 0; c < nc; ++c) {
-                const int64_t gc = lt * nc + c;
+            for (int v = 0; v < nv; ++v) {
+                const int64_t gc = lt * nv + v;
                 const int s = (int)(gc % S);
                 const uint32_t ph = (uint32_t)((gc / S) & 1);
+                // redrawn chunks of the second pass feed only the MMA (W1 A tile)
+                const bool redraw = v >= n0 && v < 2 * n0;
+                const int c = (v < n0) ? v : v - n0;
                 if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
                 unsigned char* st = base + L.a0 + s * kStageA;
                 float* w1s = (float*)(base + L.f0 + s * kStageF);
-                float* w1ps = w1s + kChunk * kTileM;
-                const int step0 = kChunk * c + SPT * h;
-                float w[SPT], wp[SPT];
-#pragma unroll
-                for (int q = 0; q < SPT / 4; ++q) {
-                    const uint32_t g = (uint32_t)((step0 >> 2) + q);
-                    const uint4 x0 = philox_group(keys, gpath, g, 0);
-                    const uint4 x1 = philox_group(keys, gpath, g, 1);
-                    box_muller_f32(x0.x, x0.y, w[4 * q], w[4 * q + 1]);
-                    box_muller_f32(x0.z, x0.w, w[4 * q + 2], w[4 * q + 3]);
-                    box_muller_f32(x1.x, x1.y, wp[4 * q], wp[4 * q + 1]);
-                    box_muller_f32(x1.z, x1.w, wp[4 * q + 2], wp[4 * q + 3]);
-                }
-#pragma unroll
-                for (int q = 0; q < SPT; ++q) {
-                    if (!valid || step0 + q >= a.N) { w[q] = 0.f; wp[q] = 0.f; }
-                }
-                // A tile: row p, logical 16-byte chunks covering steps [SPT h, SPT h + SPT), SW64 swizzle
-                uint32_t hi[SPT / 2], lo[SPT / 2];
-#pragma unroll
-                for (int q = 0; q < SPT / 2; ++q) split2<BF16>(w[2 * q], w[2 * q + 1], hi[q], lo[q]);
-#pragma unroll
-                for (int e = 0; e < SPT / 8; ++e) {
-                    const int off = p * 64 + ((((SPT / 8) * h + e) ^ sw) << 4);
-                    *(uint4*)(st + off) = make_uint4(hi[4 * e], hi[4 * e + 1], hi[4 * e + 2], hi[4 * e + 3]);
-                    *(uint4*)(st + kTileBytes + off) =
-                        make_uint4(lo[4 * e], lo[4 * e + 1], lo[4 * e + 2], lo[4 * e + 3]);
-                }
-#pragma unroll
-                for (int q = 0; q < SPT; ++q) {
-                    w1s[(SPT * h + q) * kTileM + p] = w[q];
-                    w1ps[(SPT * h + q) * kTileM + p] = wp[q];
-                }
-                if (a.dbg_w && valid) {
-#pragma unroll
-                    for (int q = 0; q < SPT; ++q) {
-                        a.dbg_w[(m * 2 + 0) * Np + step0 + q] = w[q];
-                        a.dbg_w[(m * 2 + 1) * Np + step0 + q] = wp[q];
-                    }
-                }
+                if (TWO && redraw)
+                    produce_chunk<BF16, true>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+                else
+                    produce_chunk<BF16, false>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
                 fence_proxy_async();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(full + s));
@@ -417,16 +481,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 my_acc[(2 * g) * kTileM + p] = 0.f;
                 my_acc[(2 * g + 1) * kTileM + p] = 0.f;
             }
-            for (int c = 0; c < nc; ++c) {
-                const int64_t gc = lt * nc + c;
+            for (int v = 0; v < nv; ++v) {
+                const int64_t gc = lt * nv + v;
                 const int s = (int)(gc % S);
                 const uint32_t ph = (uint32_t)((gc / S) & 1);
                 // the producers' FP32 tiles of this stage (the upper half also pairs
                 // its last column with the next chunk's first W1), then the MMA results
                 if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7, a.prof)) goto done;
+                if (v >= n0 && v < 2 * n0) {
+                    // redrawn chunk: no column becomes final.  Its MMA completion is still
+                    // awaited, so that every accf phase is observed in order.
+                    if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(smem_u32(empty + s));
+                    continue;
+                }
+                const int c = (v < n0) ? v : v - n0;
+                const uint32_t tcol0 = (c >= n0) ? (uint32_t)(kChunk * n0) : 0u;  // TMEM column of output 0
+                const bool pass_end = (c == nc - 1) || (c == n0 - 1);
                 const bool has_next = c + 1 < nc;
+                const bool bnd = (c == n0 - 1);  // successor W1 in this stage's boundary row
                 const int sn = (int)((gc + 1) % S);
-                if ((kEpiWGs == 1 || wg == 1) && has_next &&
+                if ((kEpiWGs == 1 || wg == 1) && has_next && !bnd &&
                     !mbar_wait_warp(smem_u32(full + sn), (uint32_t)(((gc + 1) / S) & 1), a.err, 8, a.prof))
                     goto done;
                 if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
@@ -437,9 +513,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 for (int hh = wg; hh < 2; hh += kEpiWGs) {
                     const int j0 = 16 * hh;
                     float x[16];
-                    tmem_ld16(tlane + (uint32_t)(kChunk * c + j0), x);
-                    if (c == nc - 1 && hh + kEpiWGs >= 2) {
-                        // this warp's accumulator columns of the tile are read
+                    tmem_ld16(tlane + (uint32_t)(kChunk * c + j0) - tcol0, x);
+                    if (pass_end && hh + kEpiWGs >= 2) {
+                        // this warp's accumulator columns of the pass are read
                         tc_fence_before();
                         __syncwarp();
                         if (lane == 0) mbar_arrive(smem_u32(tmem_empty));
@@ -453,7 +529,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                         if (jj == 0 && j0 == 0 && c == 0) w10_s[p] = w1;
                     }
                     wn[15] = (hh == 0) ? w1s[16 * kTileM + p]
-                                       : (has_next ? ((const float*)(base + L.f0 + sn * kStageF))[p] : 0.f);
+                                       : (!has_next ? 0.f
+                                          : bnd     ? w1s[2 * kChunk * kTileM + p]
+                                                    : ((const float*)(base + L.f0 + sn * kStageF))[p]);
                     if (a.dbg_x && valid) {
 #pragma unroll
                         for (int jj = 0; jj < 16; ++jj) a.dbg_x[m * Np + kChunk * c + j0 + jj] = x[jj];
@@ -543,32 +621,57 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     } else if (lane == 0) {
         // ------------------------------------------------------ MMA issuer
         const uint32_t strip_hi = smem_u32(strip);
-        const uint32_t strip_lo = strip_hi + (uint32_t)(Np * 64);
+        const uint32_t strip_lo = strip_hi + (uint32_t)(strip_bytes(Np) / 2);
+        constexpr bool wide = !TWO;  // strip_k(Np) == kChunk exactly when one pass covers Np
+        const int P0 = kChunk * n0;  // first column of the last pass
         if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
-            int64_t lt = 0;
-            for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
-                if (lt > 0 && !mbar_wait(smem_u32(tmem_empty), (uint32_t)((lt - 1) & 1), a.err, 4, a.prof)) break;
-                tc_fence_after();
-                bool ok = true;
-                for (int c = 0; c < nc && ok; ++c) {
-                    const int64_t gc = lt * nc + c;
+            int64_t lt = 0, pass = 0;
+            bool ok = true;
+            for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++lt) {
+                for (int v = 0; v < nv; ++v) {
+                    const int64_t gc = lt * nv + v;
                     const int s = (int)(gc % S);
                     const uint32_t ph = (uint32_t)((gc / S) & 1);
+                    // output columns [lo, hi) of this chunk; TMEM column = output column - toff
+                    int c, lo, hi, toff;
+                    if (v < n0) { c = v; lo = kChunk * c; hi = P0; toff = 0; }
+                    else if (v < 2 * n0) { c = v - n0; lo = P0; hi = Np; toff = P0; }
+                    else { c = v - n0; lo = kChunk * c; hi = Np; toff = P0; }
+                    const bool first = (v == 0) || (v == n0);  // first chunk of a pass overwrites
+                    if (first) {
+                        // the epilogue has read every column of the previous pass
+                        if (pass > 0 &&
+                            !mbar_wait(smem_u32(tmem_empty), (uint32_t)((pass - 1) & 1), a.err, 4, a.prof)) {
+                            ok = false;
+                            break;
+                        }
+                        ++pass;
+                        tc_fence_after();
+                    }
                     if (!mbar_wait(smem_u32(full + s), ph, a.err, 5, a.prof)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
                     const uint32_t alo = ahi + kTileBytes;
-                    for (int col0 = kChunk * c; col0 < Np; col0 += 256) {
-                        const int n = (Np - col0 < 256) ? (Np - col0) : 256;
+                    for (int col0 = lo; col0 < hi; col0 += 256) {
+                        const int n = (hi - col0 < 256) ? (hi - col0) : 256;
                         const uint32_t id = idesc_f16(n, BF16);
                         const uint32_t jrow = (uint32_t)(col0 - kChunk * c);
+                        const uint32_t d = tmem + (uint32_t)(col0 - toff);
 #pragma unroll
                         for (int ks = 0; ks < 2; ++ks) {
+                            // K half ks: A columns [16 ks, 16 ks + 16); wide strip: row jrow, bytes
+                            // [32 ks, 32 ks + 32); narrow strip: rows from jrow + 16 - 16 ks
                             const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
-                            const uint64_t dbh = sdesc_sw64(strip_hi + jrow * 64 + 32 * ks);
-                            const uint64_t dbl = sdesc_sw64(strip_lo + jrow * 64 + 32 * ks);
-                            const uint32_t d = tmem + (uint32_t)col0;
-                            umma_f16(d, dah, dbh, id, (c > 0 || ks > 0) ? 1u : 0u);
+                            uint64_t dbh, dbl;
+                            if (wide) {
+                                dbh = sdesc_sw64(strip_hi + jrow * 64 + 32 * ks);
+                                dbl = sdesc_sw64(strip_lo + jrow * 64 + 32 * ks);
+                            } else {
+                                const uint32_t boff = (jrow + (uint32_t)(kStripK * (1 - ks))) * (kStripK * 2);
+                                dbh = sdesc_sw32(strip_hi + boff);
+                                dbl = sdesc_sw32(strip_lo + boff);
+                            }
+                            umma_f16(d, dah, dbh, id, (first && ks == 0) ? 0u : 1u);
                             umma_f16(d, dah, dbl, id, 1u);
                             umma_f16(d, dal, dbh, id, 1u);
                         }
@@ -576,7 +679,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     umma_commit(smem_u32(empty + s));
                     umma_commit(smem_u32(accf + s));
                 }
-                if (!ok) break;
             }
         }
         // drain every issued MMA before TMEM is released
@@ -712,15 +814,21 @@ float from_f16(uint16_t u)
     return __half2float(h);
 }
 
-// S[j'][k'] = Gamma[j' - k'] (j' >= k'), hi/lo 16-bit halves in the SW64
-// K-major image the MMA descriptors expect: row j' at j' * 64 bytes, 16-byte
-// chunk (k' / 8) XOR ((j' / 2) mod 4).
+// The strip image the MMA descriptors expect, hi/lo 16-bit halves:
+//   wide   S[j][k] = Gamma[j - k], rows j in [0, Np), SW64 K-major: row j at
+//          j * 64 bytes, 16-byte chunk (k / 8) XOR ((j / 2) mod 4);
+//   narrow P[r][k] = Gamma[r - 16 - k], rows r in [0, Np + 16), SW32 K-major:
+//          row r at r * 32 bytes, 16-byte chunk (k / 8) XOR ((r / 4) mod 2);
+// zero where the Gamma index is negative or >= N.
 void build_strip(const double* gamma, int N, int Np, int bf16, unsigned char* img)
 {
-    std::memset(img, 0, (size_t)2 * Np * 64);
-    for (int j = 0; j < Np; ++j)
-        for (int k = 0; k < kChunk; ++k) {
-            const int d = j - k;
+    const size_t half = (size_t)strip_bytes(Np) / 2;
+    std::memset(img, 0, 2 * half);
+    const bool wide = strip_k(Np) == kChunk;
+    const int rows = wide ? Np : Np + kStripK, kw = wide ? kChunk : kStripK, lead = wide ? 0 : kStripK;
+    for (int r = 0; r < rows; ++r)
+        for (int k = 0; k < kw; ++k) {
+            const int d = r - lead - k;
             const double gv = (d >= 0 && d < N) ? gamma[d] : 0.0;
             uint16_t hi, lo;
             if (bf16) {
@@ -730,9 +838,10 @@ void build_strip(const double* gamma, int N, int Np, int bf16, unsigned char* im
                 hi = to_f16((float)gv);
                 lo = to_f16((float)(gv - (double)from_f16(hi)));
             }
-            const size_t off = (size_t)j * 64 + ((((k >> 3) ^ ((j >> 1) & 3))) << 4) + (k & 7) * 2;
+            const int sw = wide ? ((r >> 1) & 3) : ((r >> 2) & 1);
+            const size_t off = (size_t)r * kw * 2 + ((((k >> 3) ^ sw)) << 4) + (k & 7) * 2;
             std::memcpy(img + off, &hi, 2);
-            std::memcpy(img + (size_t)Np * 64 + off, &lo, 2);
+            std::memcpy(img + half + off, &lo, 2);
         }
 }
 
@@ -743,7 +852,7 @@ void mixed_table_range(const MixedJob& job, int i, size_t* off, size_t* bytes)
     const MixedLaunch& r = job.launches[i];
     if (job.backend == RBG_CONV_GEMM) {
         *off = r.off_strip;
-        *bytes = (size_t)2 * r.args.Np * 64;
+        *bytes = (size_t)strip_bytes(r.args.Np);
     } else {
         *off = r.off_spec;
         *bytes = (size_t)r.args.L * 8;
@@ -780,7 +889,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     int backend = o.conv;
     if (backend == RBG_CONV_AUTO) backend = (Np <= kMaxNp) ? RBG_CONV_GEMM : RBG_CONV_FFT;
     if (backend == RBG_CONV_GEMM && Np > kMaxNp) {
-        err = "mixed GEMM form supports N <= 512 (TMEM holds 128 x 512 FP32); use the FFT backend";
+        err = "mixed GEMM form supports N <= 1024 (two passes over 128 x 512 FP32 TMEM columns); use the FFT backend";
         return RBG_ERR_UNSUPPORTED;
     }
     if (backend == RBG_CONV_FFT && N > 4096) {
@@ -797,21 +906,31 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     const int bf16 = (o.split == RBG_SPLIT_BF16X3) ? 1 : 0;
     const int optin = (int)prop.sharedMemPerBlockOptin;
     int tcols = 32;
-    while (tcols < Np) tcols <<= 1;
+    while (tcols < std::min(Np, kPassCols)) tcols <<= 1;
+    // variance groups per GEMM launch: as many as fit two pipeline stages
+    int ng_cap = kMaxG;
+    if (backend == RBG_CONV_GEMM) {
+        while (ng_cap > 1 && smem_layout(Np, 2, ng_cap, 0).total > optin) --ng_cap;
+        if (smem_layout(Np, 2, ng_cap, 0).total > optin) {
+            err = "mixed kernel shared memory does not fit";
+            return RBG_ERR_UNSUPPORTED;
+        }
+    }
 
     size_t off = 256;  // the error word lives at offset 0
     job.off_err = 0;
     const double log2e = 1.4426950408889634;
     for (int v = 0; v < job.n_vol; ++v) {
         const VolGroup& vol = plan.vols[v];
-        for (int g0 = vol.vg_begin; g0 < vol.vg_end; g0 += kMaxG) {
-            const int ng = std::min(kMaxG, vol.vg_end - g0);
+        for (int g0 = vol.vg_begin; g0 < vol.vg_end; g0 += ng_cap) {
+            const int ng = std::min(ng_cap, vol.vg_end - g0);
             MixedLaunch r;
             std::memset(&r.args, 0, sizeof(r.args));
             MixedArgs& A = r.args;
             A.N = N;
             A.Np = Np;
             A.nc = Np / kChunk;
+            A.n0 = (backend == RBG_CONV_GEMM && Np > kPassCols) ? (Np - kPassCols) / kChunk : 0;
             A.n_g = ng;
             A.g0 = g0;
             A.tmem_cols = tcols;
@@ -829,7 +948,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             }
             if (backend == RBG_CONV_GEMM) {
                 r.off_strip = off;
-                off += (size_t)2 * Np * 64;
+                off += (size_t)strip_bytes(Np);
                 off = (off + 255) / 256 * 256;
             } else {
                 A.logL = fft_log2_len(N);
@@ -865,7 +984,8 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     // epilogue warps are the kernel's critical path.
     job.fused = RBG_FUSE_PAYOFFS && (backend == RBG_CONV_GEMM);
     for (const MixedLaunch& r : job.launches)
-        if (r.args.n_o > kMixedMaxFused) job.fused = false;
+        if (r.args.n_o > kMixedMaxFused || smem_layout(Np, 2, r.args.n_g, r.args.n_o).total > optin)
+            job.fused = false;
     for (MixedLaunch& r : job.launches) {
         MixedArgs& A = r.args;
         const int no = job.fused ? A.n_o : 0;
@@ -970,12 +1090,12 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         cudaError_t e;
         if (job.backend == RBG_CONV_FFT) {
             e = launch_mixed_fft(A, job.sms, st);
-        } else if (job.split == RBG_SPLIT_BF16X3) {
-            e = cudaFuncSetAttribute(k_mixed_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            if (e == cudaSuccess) k_mixed_gemm<1><<<grid, kThreads, smem, st>>>(A);
         } else {
-            e = cudaFuncSetAttribute(k_mixed_gemm<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            if (e == cudaSuccess) k_mixed_gemm<0><<<grid, kThreads, smem, st>>>(A);
+            void (*kern)(MixedArgs);
+            if (job.split == RBG_SPLIT_BF16X3) kern = A.n0 > 0 ? k_mixed_gemm<1, true> : k_mixed_gemm<1, false>;
+            else kern = A.n0 > 0 ? k_mixed_gemm<0, true> : k_mixed_gemm<0, false>;
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e == cudaSuccess) kern<<<grid, kThreads, smem, st>>>(A);
         }
         if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) {

@@ -33,6 +33,7 @@ struct MixedArgs {
     uint64_t seed;
     int64_t path0, B;
     int N, Np, nc, n_g, g0, tmem_cols, stages;
+    int n0;                // GEMM backend, Np > 512: chunks of the first TMEM pass (0: one pass)
     int n_o, n_out_total;  // fused outputs of this launch; all outputs of the job
     int L, logL;  // FFT backend transform length
     float a1, a2, xi, sqrt_xi;

@@ -45,7 +45,7 @@ def fp64_x(W1, W1p, H, N):
     return Y + a1 * W1[:, :N] + a2 * W1p[:, :N], A
 
 
-@pytest.mark.parametrize("N,M", [(100, 300), (512, 256), (33, 129)])
+@pytest.mark.parametrize("N,M", [(100, 300), (512, 256), (33, 129), (700, 200), (1024, 130)])
 def test_fused_normals_are_the_exported_stream(R, N, M):
     w, _, _ = R.debug_mixed_paths(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], N, M, seed=11, path_offset=7)
     Z = R.generate_normals(11, M, N, precision=R.MIXED, path_offset=7)
@@ -54,8 +54,10 @@ def test_fused_normals_are_the_exported_stream(R, N, M):
 
 
 @pytest.mark.parametrize("split,tol", [(0, 4e-5), (1, 1e-6)])
-@pytest.mark.parametrize("N", [64, 100, 512])
+@pytest.mark.parametrize("N", [64, 100, 512, 513, 700, 1024])
 def test_toeplitz_gemm_columns(R, split, tol, N):
+    """Columns of one TMEM pass (N <= 512) and of two (512 < N <= 1024, the
+    second pass fed by redrawn A tiles) against the FP64 convolution."""
     H = 0.1
     M = 256
     w, x, _ = R.debug_mixed_paths(0.04, [H], [1.5], [-0.7], [1.0], [1.0], N, M, seed=3, split=split)
@@ -116,7 +118,34 @@ def test_mixed_grid_multi_pass(R):
 
 def test_gemm_backend_rejects_long_horizon(R):
     with pytest.raises(R.RbgError):
-        R.price_rt(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 1024, 256, precision=R.MIXED, conv=R.CONV_GEMM)
+        R.price_rt(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 1025, 256, precision=R.MIXED, conv=R.CONV_GEMM)
+
+
+@pytest.mark.parametrize("N", [544, 1024])
+def test_two_pass_gemm_prices_vs_fp64_identical_normals(R, N):
+    """Long-horizon shape on the two-pass GEMM: error vs the FP64 form on the
+    same FP32 normals <= 1e-4 relative and < 0.2 standard errors."""
+    H, eta, rho, xi, T = [0.1], [1.5], [-0.7], 0.04, 2.0
+    K = list(np.linspace(0.5, 1.5, 11))
+    M = 1 << 13
+    mp, ms, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=3, precision=R.MIXED, conv=R.CONV_GEMM)
+    fp, fs, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=3, normals=R.NORMALS_F32)
+    err = np.abs(mp - fp)
+    assert np.all(err <= 1e-4 * fp)
+    assert np.all(err < 0.2 * fs)
+
+
+def test_two_pass_gemm_multi_group_grid(R):
+    """Several variance groups and Volterra passes at N = 800 (two TMEM passes)."""
+    g = GRID
+    N, M = 800, 1 << 12
+    mp, ms, _ = R.price_rt(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, seed=23,
+                           precision=R.MIXED, split=1, conv=R.CONV_GEMM)
+    fp, fs, _ = R.price_rt(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, seed=23,
+                           normals=R.NORMALS_F32)
+    big = fp > 1e-4
+    assert np.all(np.abs(mp - fp)[big] <= 1e-4 * fp[big])
+    assert np.all(np.abs(mp - fp) < 0.2 * np.maximum(fs, 1e-12) + 1e-9)
 
 
 # ------------------------------------------------------------ FFT backend
@@ -133,9 +162,10 @@ def test_fft_backend_columns(R, N, M):
     assert np.max(err / (A + 1.0)) < 1e-5
 
 
-def test_fft_and_gemm_backends_agree(R):
+@pytest.mark.parametrize("N", [512, 1024])
+def test_fft_and_gemm_backends_agree(R, N):
     c = CFG2
-    N, M = 512, 1 << 14
+    M = 1 << 14
     pg, sg, _ = R.price_rt(c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], N, M, seed=5, precision=R.MIXED,
                            conv=R.CONV_GEMM, split=1)
     pf, sf, _ = R.price_rt(c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], N, M, seed=5, precision=R.MIXED,
@@ -148,7 +178,7 @@ def test_fft_prices_vs_fp64_identical_normals(R, N):
     H, eta, rho, xi, T = [0.1], [1.5], [-0.7], 0.04, 2.0
     K = list(np.linspace(0.5, 1.5, 11))
     M = 1 << 12
-    mp, ms, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=3, precision=R.MIXED)
+    mp, ms, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=3, precision=R.MIXED, conv=R.CONV_FFT)
     fp, fs, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=3, normals=R.NORMALS_F32)
     err = np.abs(mp - fp)
     assert np.all(err <= 1e-4 * fp)
