@@ -512,6 +512,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
 #pragma unroll 1
                 for (int hh = wg; hh < 2; hh += kEpiWGs) {
                     const int j0 = 16 * hh;
+                    // the producers' FP32 operands first: these shared-memory loads are
+                    // issued ahead of the TMEM load, so their latencies overlap
+                    float w1v[16], w1pv[16];
+#pragma unroll
+                    for (int jj = 0; jj < 16; ++jj) {
+                        w1v[jj] = w1s[(j0 + jj) * kTileM + p];
+                        w1pv[jj] = w1ps[(j0 + jj) * kTileM + p];
+                    }
+                    const float w_after = (hh == 0) ? w1s[16 * kTileM + p]
+                                                    : (!has_next ? 0.f
+                                                       : bnd     ? w1s[2 * kChunk * kTileM + p]
+                                                                 : ((const float*)(base + L.f0 + sn * kStageF))[p]);
                     float x[16];
                     tmem_ld16(tlane + (uint32_t)(kChunk * c + j0) - tcol0, x);
                     if (pass_end && hh + kEpiWGs >= 2) {
@@ -523,15 +535,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     float wn[16];
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj) {
-                        const float w1 = w1s[(j0 + jj) * kTileM + p];
-                        x[jj] = x[jj] + a.a1 * w1 + a.a2 * w1ps[(j0 + jj) * kTileM + p];
+                        const float w1 = w1v[jj];
+                        x[jj] = x[jj] + a.a1 * w1 + a.a2 * w1pv[jj];
                         if (jj > 0) wn[jj - 1] = w1;
                         if (jj == 0 && j0 == 0 && c == 0) w10_s[p] = w1;
                     }
-                    wn[15] = (hh == 0) ? w1s[16 * kTileM + p]
-                                       : (!has_next ? 0.f
-                                          : bnd     ? w1s[2 * kChunk * kTileM + p]
-                                                    : ((const float*)(base + L.f0 + sn * kStageF))[p]);
+                    wn[15] = w_after;
                     if (a.dbg_x && valid) {
 #pragma unroll
                         for (int jj = 0; jj < 16; ++jj) a.dbg_x[m * Np + kChunk * c + j0 + jj] = x[jj];
