@@ -203,6 +203,12 @@ int rbg_release(void);
  * after the reference's trigger chain) and outputs; vgroup_of_output
  * (length par_size*op_size, may be NULL) receives each output's group. */
 int rbg_plan_info(const rbg_params* p, int* n_vol, int* n_vgroups, int* n_out, int* vgroup_of_output);
+/* Host-only plan of the plain Monte Carlo estimator: as rbg_plan_info, plus
+ * the rho each output's S_T is computed with (the rho of the last
+ * H/T/eta/rho trigger, eps 1e-10). */
+int rbg_plan_info_mc(const rbg_params* p, int* n_vol, int* n_vgroups, int* vgroup_of_output, double* rho_of_output);
+/* Host-only plan of an unordered list: Volterra passes and variance groups. */
+int rbg_plan_info_unordered(const rbg_unordered* u, int* n_vol, int* n_vgroups, int* vgroup_of_output);
 
 /* Stage timing: when enabled, CUDA events bracket each stage on the stream
  * that launches it (stage 0 normals, 1 FP64 path pass, 2 mixed tcgen05 path

@@ -60,6 +60,7 @@ EXPORTS = [
     "rbg_debug_mixed_profile", "rbg_server_default_config", "rbg_server_create", "rbg_server_submit",
     "rbg_server_poll", "rbg_server_wait", "rbg_server_get_stats", "rbg_server_destroy", "rbg_server_last_error",
     "rbg_price_rt_unordered", "computeIV_tensor", "rbg_price_mc", "rbg_payoffs_mc", "rbg_generate_normals_streams",
+    "rbg_plan_info_mc", "rbg_plan_info_unordered",
 ]
 
 STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4
@@ -319,6 +320,27 @@ def plan_info(xi, H, eta, rho, T, K, N, M=1):
     nv, ng, no = C.c_int(), C.c_int(), C.c_int()
     groups = (C.c_int * p.out)()
     _check(lib().rbg_plan_info(C.byref(p.s), C.byref(nv), C.byref(ng), C.byref(no), groups))
+    return nv.value, ng.value, np.array(list(groups), dtype=np.int64)
+
+
+def plan_info_mc(xi, H, eta, rho, T, K, N, M=1):
+    """Host-only plain-MC plan: (n_passes, n_groups, group_of_output, rho_of_output)."""
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    nv, ng = C.c_int(), C.c_int()
+    groups = (C.c_int * p.out)()
+    rhos = np.empty(p.out)
+    _check(lib().rbg_plan_info_mc(C.byref(p.s), C.byref(nv), C.byref(ng), groups, rhos.ctypes.data_as(_dp)))
+    return nv.value, ng.value, np.array(list(groups), dtype=np.int64), rhos
+
+
+def plan_info_unordered(xi, H, eta, rho, T, K, N, M=1):
+    """Host-only unordered plan: (n_passes, n_groups, group_of_output)."""
+    arrs = [_arr(x) for x in (H, eta, rho, T, K)]
+    n = len(arrs[0])
+    u = RbgUnordered(float(xi), *[x.ctypes.data_as(_dp) for x in arrs], n, int(N), int(M))
+    nv, ng = C.c_int(), C.c_int()
+    groups = (C.c_int * n)()
+    _check(lib().rbg_plan_info_unordered(C.byref(u), C.byref(nv), C.byref(ng), groups))
     return nv.value, ng.value, np.array(list(groups), dtype=np.int64)
 
 

@@ -707,6 +707,34 @@ int rbg_plan_info(const rbg_params* p, int* n_vol, int* n_vgroups, int* n_out, i
     return RBG_OK;
 }
 
+int rbg_plan_info_mc(const rbg_params* p, int* n_vol, int* n_vgroups, int* vgroup_of_output, double* rho_of_output)
+{
+    if (!p) return fail(RBG_ERR_ARG, "null params");
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err, true)) return fail(RBG_ERR_ARG, err);
+    if (n_vol) *n_vol = (int)plan.vols.size();
+    if (n_vgroups) *n_vgroups = (int)plan.vgs.size();
+    for (size_t i = 0; i < plan.outs.size(); ++i) {
+        if (vgroup_of_output) vgroup_of_output[i] = plan.outs[i].vg;
+        if (rho_of_output) rho_of_output[i] = plan.outs[i].rho;
+    }
+    return RBG_OK;
+}
+
+int rbg_plan_info_unordered(const rbg_unordered* u, int* n_vol, int* n_vgroups, int* vgroup_of_output)
+{
+    if (!u) return fail(RBG_ERR_ARG, "null list");
+    Plan plan;
+    std::string err;
+    if (!build_plan_unordered(*u, plan, err)) return fail(RBG_ERR_ARG, err);
+    if (n_vol) *n_vol = (int)plan.vols.size();
+    if (n_vgroups) *n_vgroups = (int)plan.vgs.size();
+    if (vgroup_of_output)
+        for (size_t i = 0; i < plan.outs.size(); ++i) vgroup_of_output[i] = plan.outs[i].vg;
+    return RBG_OK;
+}
+
 // ------------------------------------------------------------- drop-in
 static void die_on(int rc)
 {

@@ -91,18 +91,19 @@ __device__ __forceinline__ void box_muller_f64(uint32_t a, uint32_t b, double& z
 }
 
 // FP32 Box-Muller on the same uniforms (mixed form), on the MUFU pipe:
-// r = sqrt(-2 ln 2 log2 u0) and the angle 2 pi u1 folded into (-pi, pi] so
-// sin/cos.approx stay in their accurate range (same sin and cos values).
+// r = sqrt(-2 ln 2 log2 u0); the angle is taken as t = 2 pi u1 - pi, which
+// lies in (-pi, pi) where sin/cos.approx are accurate, and
+// cos(2 pi u1) = -cos t, sin(2 pi u1) = -sin t.
 __device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float& z0, float& z1)
 {
     const float u0 = fmaf((float)a, 2.3283064e-10f, 1.1641532e-10f);
     const float u1 = fmaf((float)b, 2.3283064e-10f, 1.1641532e-10f);
-    const float r = sqrt_approx(-1.3862944f * lg2_approx(u0));
-    const float th = 6.2831853f * (u1 > 0.5f ? u1 - 1.0f : u1);
+    const float nr = -sqrt_approx(-1.3862944f * lg2_approx(u0));
+    const float th = fmaf(6.2831853f, u1, -3.14159265f);
     float s, c;
     sincos_approx(th, s, c);
-    z0 = r * c;
-    z1 = r * s;
+    z0 = nr * c;
+    z1 = nr * s;
 }
 
 // Normal CDF and BS call, rBergLib/BlackScholes.cpp:11-21 with tau = 1, r = 0

@@ -82,7 +82,7 @@ constexpr uint64_t kWaitNs = 2000000000ull;         // 2 s per wait
 // shared-memory layout (offsets from a 1024-aligned base):
 //   [strip hi | strip lo]            2 * Np * 64 B, SW64 (one pass), or 2 * (Np + 16) * 32 B, SW32
 //   A tiles, per stage [hi | lo]     16 KB per stage (1024-aligned)
-//   FP32 tiles, per stage            w1 [32][128], w1perp [32][128], W1 of step P0 [128]
+//   FP32 tiles, per stage            w1 [128][32], w1perp [128][32] (swizzled), W1 of step P0 [128]
 //   per-thread group sums            n_g * 2 * 128 floats
 //   beta tables                      n_g * Np floats
 //   fused outputs                    table n_o * 4 floats, FP32 Kahan sums [4 warps][n_o][4]
@@ -95,6 +95,11 @@ constexpr int kStageF = (2 * kChunk + 1) * kTileM * 4;                   // w1, 
 // column) where one TMEM pass covers Np; 16 (SW32, 16 leading zero rows)
 // for two-pass tiles, whose Np-row strip would not fit shared memory at 32.
 __host__ __device__ inline int strip_k(int Np) { return Np <= kPassCols ? kChunk : kStripK; }
+// FP32 tiles are path-major, [128 paths][32 steps], with the 16-byte chunk
+// index XORed by (path mod 8): a thread's 4 consecutive steps are one vector
+// access and the 8 threads of a vector phase hit distinct banks.
+__device__ __forceinline__ int ftile_at(int p, int s) { return p * kChunk + ((((s >> 2) ^ (p & 7))) << 2) + (s & 3); }
+
 __host__ __device__ inline int strip_bytes(int Np)
 {
     return strip_k(Np) == kChunk ? 2 * Np * kChunk * 2 : 2 * (Np + kStripK) * kStripK * 2;
@@ -331,9 +336,11 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
             box_muller_f32(x1.z, x1.w, wp[4 * q + 2], wp[4 * q + 3]);
         }
     }
+    if (!(valid && step0 + SPT <= a.N)) {  // only the last tile / chunk
 #pragma unroll
-    for (int q = 0; q < SPT; ++q) {
-        if (!valid || step0 + q >= a.N) { w[q] = 0.f; wp[q] = 0.f; }
+        for (int q = 0; q < SPT; ++q) {
+            if (!valid || step0 + q >= a.N) { w[q] = 0.f; wp[q] = 0.f; }
+        }
     }
     // A tile: row p, logical 16-byte chunks covering steps [SPT h, SPT h + SPT), SW64 swizzle
     uint32_t hi[SPT / 2], lo[SPT / 2];
@@ -347,9 +354,10 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
     }
     if (!REDRAW) {
 #pragma unroll
-        for (int q = 0; q < SPT; ++q) {
-            w1s[(SPT * h + q) * kTileM + p] = w[q];
-            w1ps[(SPT * h + q) * kTileM + p] = wp[q];
+        for (int q = 0; q < SPT; q += 4) {
+            const int at = ftile_at(p, SPT * h + q);
+            *(float4*)(w1s + at) = make_float4(w[q], w[q + 1], w[q + 2], w[q + 3]);
+            *(float4*)(w1ps + at) = make_float4(wp[q], wp[q + 1], wp[q + 2], wp[q + 3]);
         }
         // last chunk of the first pass: its successor (chunk n0) follows the
         // redrawn chunks, so W1 at step 32 n0 for the last column's sqrt(v) dW
@@ -516,14 +524,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     // issued ahead of the TMEM load, so their latencies overlap
                     float w1v[16], w1pv[16];
 #pragma unroll
-                    for (int jj = 0; jj < 16; ++jj) {
-                        w1v[jj] = w1s[(j0 + jj) * kTileM + p];
-                        w1pv[jj] = w1ps[(j0 + jj) * kTileM + p];
+                    for (int jj = 0; jj < 16; jj += 4) {
+                        const int at = ftile_at(p, j0 + jj);
+                        const float4 u = *(const float4*)(w1s + at), v = *(const float4*)(w1ps + at);
+                        w1v[jj] = u.x; w1v[jj + 1] = u.y; w1v[jj + 2] = u.z; w1v[jj + 3] = u.w;
+                        w1pv[jj] = v.x; w1pv[jj + 1] = v.y; w1pv[jj + 2] = v.z; w1pv[jj + 3] = v.w;
                     }
-                    const float w_after = (hh == 0) ? w1s[16 * kTileM + p]
-                                                    : (!has_next ? 0.f
-                                                       : bnd     ? w1s[2 * kChunk * kTileM + p]
-                                                                 : ((const float*)(base + L.f0 + sn * kStageF))[p]);
+                    const float w_after =
+                        (hh == 0) ? w1s[ftile_at(p, 16)]
+                                  : (!has_next ? 0.f
+                                     : bnd     ? w1s[2 * kChunk * kTileM + p]
+                                               : ((const float*)(base + L.f0 + sn * kStageF))[ftile_at(p, 0)]);
                     float x[16];
                     tmem_ld16(tlane + (uint32_t)(kChunk * c + j0) - tcol0, x);
                     if (pass_end && hh + kEpiWGs >= 2) {

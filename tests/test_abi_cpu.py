@@ -79,6 +79,57 @@ def test_plan_matches_trigger_chain(R, case):
     assert ng == len(set(states))
 
 
+def mc_rho_chain(H, eta, rho, T):
+    """The plain-MC rho each output prices S with: rho at the last
+    H/T/eta/rho trigger (rBergLib/rBergomiMT.cpp:239-262)."""
+    O, eps = len(T), 1e-10
+    out, cur = [], None
+    for i in range(len(H) * O):
+        q, t = i // O, i % O
+        upd = i == 0 or abs(H[q] - H[(i - 1) // O]) > eps or abs(T[t] - T[(i - 1) % O]) > eps \
+            or abs(eta[q] - eta[(i - 1) // O]) > eps or abs(rho[q] - rho[(i - 1) // O]) > eps
+        if upd:
+            cur = rho[q]
+        out.append(cur)
+    return out
+
+
+@pytest.mark.parametrize("case", [
+    ([0.1, 0.1], [1.5, 1.5], [-0.7, -0.7 + 5e-11], [1.0], [1.0]),          # stale rho kept
+    ([0.1, 0.1], [1.5, 1.5], [-0.7, -0.7 + 5e-11], [1.0, 2.0], [1.0, 1.1]),  # T wrap re-triggers
+    ([0.1, 0.1, 0.1], [1.5, 1.5, 1.5], [-0.7, -0.5, -0.5 - 2e-11], [0.5], [1.0]),
+])
+def test_mc_plan_rho_trigger(R, case):
+    H, eta, rho, T, K = case
+    _, _, groups, rhos = R.plan_info_mc(0.04, H, eta, rho, T, K, 64)
+    np.testing.assert_array_equal(rhos, mc_rho_chain(H, eta, rho, T))
+    _, _, groups_rt = R.plan_info(0.04, H, eta, rho, T, K, 64)
+    np.testing.assert_array_equal(groups, groups_rt)
+
+
+def test_unordered_plan_groups():
+    """Unordered lists share a Volterra pass per exact H and a variance group
+    per exact (H, T, eta) (rBergomi/rBergomiMT.cpp:940-957 recomputes every
+    tuple, so equal tuples reach equal states)."""
+    import rbergomi_gb300 as R
+    rng = np.random.default_rng(5)
+    n = 40
+    H = rng.choice([0.05, 0.1, 0.3], n)
+    eta = rng.choice([1.0, 2.0], n)
+    T = rng.choice([0.5, 1.0], n)
+    rho = rng.uniform(-0.9, -0.3, n)
+    K = rng.uniform(0.8, 1.2, n)
+    nv, ng, groups = R.plan_info_unordered(0.04, H, eta, rho, T, K, 64)
+    keys = list(zip(H, T, eta))
+    assert nv == len(set(H))
+    assert ng == len(set(keys))
+    for a in range(n):
+        for b in range(n):
+            assert (groups[a] == groups[b]) == (keys[a] == keys[b])
+    with pytest.raises(R.RbgError):
+        R.plan_info_unordered(0.04, [1.5], [1.0], [-0.5], [1.0], [1.0], 64)
+
+
 def test_plan_rejects_bad_input(R):
     with pytest.raises(R.RbgError):
         R.plan_info(0.04, [0.0], [1.0], [-0.5], [1.0], [1.0], 64)
@@ -90,12 +141,13 @@ def _run(code):
     return subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=120)
 
 
-def test_dropin_exit_codes():
+@pytest.mark.parametrize("fn", ["computeIVRT_tensor", "computeIV_tensor"])
+def test_dropin_exit_codes(fn):
     """Size mismatch -> exit 17, num_threads < 1 -> exit 21, before any GPU work
-    (rBergLib/cinterface.cpp:54-59, 76-81)."""
+    (rBergLib/cinterface.cpp:15-20, 38-42, 54-59)."""
     pre = ("import ctypes as C, numpy as np, rbergomi_gb300 as R\n"
            "L=R.lib(); d=lambda n: (C.c_double*n)(); s=(C.c_uint64*1)(1)\n")
-    call = ("L.computeIVRT_tensor(0.04, d(1), d(1), d(1), 1, d(2), d(2), 2, 8, 16, s, 1, {nt}, "
+    call = ("L." + fn + "(0.04, d(1), d(1), d(1), 1, d(2), d(2), 2, 8, 16, s, 1, {nt}, "
             "d(2), d(2), d(2), d(2), d(2), d(2), d(2), d(2), {out})\n")
     r = _run(pre + call.format(nt=1, out=3))
     assert r.returncode == 17 and "wrong size" in r.stderr
