@@ -10,10 +10,16 @@
 // IFFT(FFT(z) * G^) = (W1_a * Gamma) + i (W1_b * Gamma).  G^ = FFT(Gamma)/L
 // is computed once per (H, N) on the host in FP64 and stored as FP32.
 //
-// Transform: radix-4 Stockham auto-sort stages (a radix-2 first stage when
-// log2 L is odd) between two shared-memory buffers, twiddles from an FP32
-// table of exp(-2 pi i t / L) built on the host in FP64.  One CTA of 512
-// threads owns a pair of paths at a time and loops over pairs.
+// Transform: Stockham auto-sort passes held in registers, in place in one
+// shared-memory buffer: every thread loads its butterflies' inputs, the
+// block synchronises, then every thread writes its outputs.  Radix 16 (a
+// 4 x 4 decomposition with constant inner twiddles) for four bits of log2 L
+// at a time, one radix-2/4/8 pass first for the remainder, so L = 4096 takes
+// three passes per transform.  Pass twiddles come from an FP32 table of
+// exp(-2 pi i t / L) built on the host in FP64.  The buffer inserts one
+// padding element per 16, which keeps the strided writes of the first
+// passes off a single bank.  One CTA owns a pair of paths at a time and
+// loops over pairs; several CTAs share an SM.
 //
 // The epilogue is the GEMM kernel's: X = Y2 + a1 W1 + a2 W1perp,
 // sqrt(v_{j+1}) = 2^(alpha/2 X_j - beta_j/2), per-group sums of v and
@@ -31,8 +37,7 @@
 
 namespace rbg {
 
-constexpr int kFftThreads = 512;
-constexpr int kFftWarps = kFftThreads / 32;
+__host__ __device__ constexpr int fft_threads(int logL) { return 256; }
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -40,87 +45,230 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 }
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 mul_mi(float2 a) { return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x); }
 
-// One Stockham pass of radix R over L points, src -> dst, span Ns.
-template <int R, bool INV>
-__device__ __forceinline__ void stockham_pass(const float2* __restrict__ src, float2* __restrict__ dst, int L,
-                                              int lns, const float2* __restrict__ tw, int logL)
+// padded shared-memory index: one spare element after every 16
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+
+template <bool INV>
+__device__ __forceinline__ void dft2(float2& a, float2& b)
 {
-    const int nb = L / R;
-    const int Ns = 1 << lns;
-    const int lr = (R == 2) ? 1 : 2;
-    const int lstep = logL - lns - lr;  // log2(L / (Ns R))
-    for (int j = threadIdx.x; j < nb; j += kFftThreads) {
-        const int k = j & (Ns - 1);
-        float2 v[R];
+    const float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3)
+{
+    const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = mul_mi<INV>(csub(a1, a3));
+    a0 = cadd(t0, t2);
+    a2 = csub(t0, t2);
+    a1 = cadd(t1, t3);
+    a3 = csub(t1, t3);
+}
+
+// exp(-+ 2 pi i m / 16) for the inner twiddles of the 4 x 4 radix-16 DFT
+template <bool INV>
+__device__ __forceinline__ float2 w16(int m)
+{
+    constexpr float c1 = 0.92387953251128674f, s1 = 0.38268343236508977f, h = 0.70710678118654752f;
+    float2 w;
+    switch (m) {
+        case 1: w = make_float2(c1, s1); break;
+        case 2: w = make_float2(h, h); break;
+        case 3: w = make_float2(s1, c1); break;
+        case 6: w = make_float2(-h, h); break;
+        case 9: w = make_float2(-c1, -s1); break;
+        default: w = make_float2(1.f, 0.f); break;
+    }
+    if (!INV) w.y = -w.y;
+    return w;
+}
+
+// In-register DFT of radix R in {2, 4, 8, 16}; v[q'] holds input n = q' and,
+// on return, output k at position perm(k): R <= 4 natural order, R = 8, 16
+// transposed (k = k1 + A k2 sits at v[4 k1 + k2] with A = R / 4).
+template <int R, bool INV>
+__device__ __forceinline__ void dft_r(float2 (&v)[R])
+{
+    if (R == 2) {
+        dft2<INV>(v[0], v[1]);
+    } else if (R == 4) {
+        dft4<INV>(v[0], v[1], v[2], v[3]);
+    } else if (R == 8) {
+        // n = 4 n1 + n2 (n1 < 2, n2 < 4); k = k1 + 2 k2
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
-        if (Ns > 1) {
+        for (int n2 = 0; n2 < 4; ++n2) dft2<INV>(v[n2], v[4 + n2]);
+        // twiddle W8^(n2 k1) on (n2, k1 = 1): v[4 + n2]
+        constexpr float h = 0.70710678118654752f;
+        v[5] = cmul(v[5], make_float2(h, INV ? h : -h));
+        v[6] = mul_mi<INV>(v[6]);
+        v[7] = cmul(v[7], make_float2(-h, INV ? h : -h));
+        dft4<INV>(v[0], v[1], v[2], v[3]);
+        dft4<INV>(v[4], v[5], v[6], v[7]);
+    } else {
+        // n = 4 n1 + n2; k = k1 + 4 k2
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 t = __ldg(tw + ((k * r) << lstep));
-                if (INV) t.y = -t.y;
-                v[r] = cmul(v[r], t);
+        for (int n2 = 0; n2 < 4; ++n2) dft4<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+#pragma unroll
+        for (int k1 = 1; k1 < 4; ++k1)
+#pragma unroll
+            for (int n2 = 1; n2 < 4; ++n2) {
+                const int m = n2 * k1;
+                if (m == 4) v[4 * k1 + n2] = mul_mi<INV>(v[4 * k1 + n2]);
+                else v[4 * k1 + n2] = cmul(v[4 * k1 + n2], w16<INV>(m));
             }
-        }
-        const int d = ((j >> lns) << (lns + lr)) + k;
-        if (R == 2) {
-            dst[d] = cadd(v[0], v[1]);
-            dst[d + Ns] = csub(v[0], v[1]);
-        } else {
-            const float2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-            const float2 c = cadd(v[1], v[3]), e = csub(v[1], v[3]);
-            // forward: multiply e by -i; inverse: by +i
-            const float2 ie = INV ? make_float2(-e.y, e.x) : make_float2(e.y, -e.x);
-            dst[d] = cadd(a, c);
-            dst[d + Ns] = cadd(b, ie);
-            dst[d + 2 * Ns] = csub(a, c);
-            dst[d + 3 * Ns] = csub(b, ie);
-        }
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
     }
 }
 
-// Full transform; returns the buffer holding the result.
-template <bool INV>
-__device__ float2* fft_L(float2* a, float2* b, int L, int logL, const float2* __restrict__ tw)
+template <int R>
+__device__ __forceinline__ int out_slot(int k)
 {
-    int lns = 0;
-    if (logL & 1) {
-        stockham_pass<2, INV>(a, b, L, lns, tw, logL);
-        __syncthreads();
-        float2* t = a; a = b; b = t;
-        lns = 1;
+    return (R <= 4) ? k : 4 * (k % (R / 4)) + k / (R / 4);
+}
+
+// Where the first forward pass reads its input: the transform buffer, or the
+// generated normals directly, z[n] = W1_a[n] + i W1_b[n] for n < N and zero
+// above (SRC_WS), or the same sequence with every element doubled, which is
+// what a radix-2 first pass makes of a zero upper half (SRC_WS_DUP).
+enum { SRC_BUF = 0, SRC_WS = 1, SRC_WS_DUP = 2 };
+
+struct FftIn {
+    const float* w1a;  // W1 of the pair's first path; the second path's W1 is 2 W floats further
+    int W, N;
+};
+
+__device__ __forceinline__ float2 ws_z(const FftIn& in, int n)
+{
+    return n < in.N ? make_float2(in.w1a[n], in.w1a[2 * in.W + n]) : make_float2(0.f, 0.f);
+}
+
+// One in-place Stockham pass of radix R over L = 2^LOGL points, span 2^LNS.
+// ZHI: the upper half of the input is zero (the first forward pass: the
+// zero-padded sequence has N <= L / 2 entries), so those loads are skipped.
+// SPEC: multiply every output by the spectrum (the last forward pass).
+// HALF: store only outputs below L / 2 (the last inverse pass: the Volterra
+// sum needs N <= L / 2 of them).
+template <int R, int LOGL, int LNS, bool INV, int T, bool ZHI = false, int SRC = SRC_BUF, bool SPEC = false,
+          bool HALF = false>
+__device__ __forceinline__ void fft_pass(float2* __restrict__ buf, const float2* __restrict__ tw, const FftIn& in,
+                                         const float2* __restrict__ spec)
+{
+    constexpr int L = 1 << LOGL, NB = L / R, NS = 1 << LNS;
+    constexpr int LR = (R == 2) ? 1 : (R == 4) ? 2 : (R == 8) ? 3 : 4;
+    constexpr int LSTEP = LOGL - LNS - LR;
+    constexpr int BPT = (NB + T - 1) / T;  // butterflies per thread
+    // only the data stays live across the barrier; twiddles are read after it
+    float2 v[BPT][R];
+#pragma unroll
+    for (int b = 0; b < BPT; ++b) {
+        const int j = threadIdx.x + b * T;
+        if (NB % T == 0 || j < NB) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int n = j + r * NB;
+                if (ZHI && r >= R / 2) v[b][r] = make_float2(0.f, 0.f);
+                else if (SRC == SRC_WS) v[b][r] = ws_z(in, n);
+                else if (SRC == SRC_WS_DUP) v[b][r] = ws_z(in, n >> 1);
+                else v[b][r] = buf[pidx(n)];
+            }
+        }
     }
-    for (; lns < logL; lns += 2) {
-        stockham_pass<4, INV>(a, b, L, lns, tw, logL);
-        __syncthreads();
-        float2* t = a; a = b; b = t;
+    if (SRC == SRC_BUF) __syncthreads();  // reading the normals leaves the buffer free to write
+#pragma unroll
+    for (int b = 0; b < BPT; ++b) {
+        const int j = threadIdx.x + b * T;
+        if (NB % T == 0 || j < NB) {
+            const int k = j & (NS - 1);
+            if (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    if (ZHI && r >= R / 2) continue;
+                    float2 t = __ldg(tw + ((k * r) << LSTEP));
+                    if (INV) t.y = -t.y;
+                    v[b][r] = cmul(v[b][r], t);
+                }
+            }
+            dft_r<R, INV>(v[b]);
+            const int d = ((j >> LNS) << (LNS + LR)) + k;
+#pragma unroll
+            for (int q = 0; q < (HALF ? R / 2 : R); ++q) {
+                float2 y = v[b][out_slot<R>(q)];
+                if (SPEC) y = cmul(y, __ldg(spec + d + q * NS));
+                buf[pidx(d + q * NS)] = y;
+            }
+        }
     }
-    return a;
+    __syncthreads();
+}
+
+// Radix-16 passes from span 2^LNS up to L; FIRST marks the transform's first
+// pass (SRC and ZHI apply), the last pass gets SPEC (forward) or HALF (inverse).
+template <int LOGL, int LNS, bool INV, int T, bool ZHI, int SRC>
+__device__ __forceinline__ void fft_r16(float2* buf, const float2* tw, const FftIn& in, const float2* spec)
+{
+    if constexpr (LNS < LOGL) {
+        constexpr bool LAST = LNS + 4 == LOGL;
+        fft_pass<16, LOGL, LNS, INV, T, ZHI, SRC, LAST && !INV, LAST && INV>(buf, tw, in, spec);
+        fft_r16<LOGL, LNS + 4, INV, T, false, SRC_BUF>(buf, tw, in, spec);
+    }
+}
+
+// Forward transform of the pair's normals times the spectrum, or inverse
+// transform of the buffer.  L >= 16.  For odd log2 L the radix-2 first pass
+// of the forward transform is the SRC_WS_DUP read.
+template <int LOGL, bool INV, int T>
+__device__ __forceinline__ void fft_inplace(float2* buf, const float2* tw, const FftIn& in, const float2* spec)
+{
+    constexpr int REM = LOGL % 4;
+    if constexpr (INV) {
+        if constexpr (REM == 1) fft_pass<2, LOGL, 0, true, T>(buf, tw, in, spec);
+        if constexpr (REM == 2) fft_pass<4, LOGL, 0, true, T>(buf, tw, in, spec);
+        if constexpr (REM == 3) fft_pass<8, LOGL, 0, true, T>(buf, tw, in, spec);
+        fft_r16<LOGL, REM, true, T, false, SRC_BUF>(buf, tw, in, spec);
+    } else {
+        if constexpr (REM == 1) {
+            fft_r16<LOGL, 1, false, T, false, SRC_WS_DUP>(buf, tw, in, spec);
+        } else if constexpr (REM == 0) {
+            fft_r16<LOGL, 0, false, T, true, SRC_WS>(buf, tw, in, spec);
+        } else {
+            if constexpr (REM == 2) fft_pass<4, LOGL, 0, false, T, true, SRC_WS>(buf, tw, in, spec);
+            if constexpr (REM == 3) fft_pass<8, LOGL, 0, false, T, true, SRC_WS>(buf, tw, in, spec);
+            fft_r16<LOGL, REM, false, T, false, SRC_BUF>(buf, tw, in, spec);
+        }
+    }
 }
 
 struct FftSmem {
-    int buf0, buf1, w, red, total;
+    int buf, w, red, total;
 };
 
 __host__ __device__ inline FftSmem fft_smem(int L, int Np, int n_g)
 {
+    int logL = 0;
+    while ((1 << logL) < L) ++logL;
+    const int warps = fft_threads(logL) / 32;
     FftSmem S;
-    S.buf0 = 0;
-    S.buf1 = L * 8;
-    S.w = 2 * L * 8;                               // [2 paths][W1 | W1perp][Np + 1]
-    S.red = S.w + 2 * 2 * (Np + 4) * 4;
-    S.total = S.red + kFftWarps * n_g * 4 * 4 + 64;
+    S.buf = 0;
+    S.w = (L + L / 16) * 8;                        // padded transform buffer
+    S.red = S.w + 2 * 2 * (Np + 4) * 4;            // [2 paths][W1 | W1perp][Np + 4]
+    S.total = S.red + warps * n_g * 4 * 4 + 64;
     return S;
 }
 
-__global__ void __launch_bounds__(kFftThreads) k_mixed_fft(const __grid_constant__ MixedArgs a)
+template <int LOGL>
+__global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed_fft(const __grid_constant__ MixedArgs a)
 {
+    constexpr int T = fft_threads(LOGL), L = 1 << LOGL, WARPS = T / 32;
     extern __shared__ __align__(16) unsigned char smf[];
-    const int L = a.L, N = a.N, Np = a.Np;
+    const int N = a.N, Np = a.Np;
     const FftSmem S = fft_smem(L, Np, a.n_g);
-    float2* b0 = (float2*)(smf + S.buf0);
-    float2* b1 = (float2*)(smf + S.buf1);
+    float2* buf = (float2*)(smf + S.buf);
     float* ws = (float*)(smf + S.w);  // path q, stream s: ws + (2q + s) * (Np + 4)
     float* red = (float*)(smf + S.red);
     const int W = Np + 4;
@@ -131,7 +279,7 @@ __global__ void __launch_bounds__(kFftThreads) k_mixed_fft(const __grid_constant
 
     for (int64_t pr = blockIdx.x; pr < npairs; pr += gridDim.x) {
         // 1. normals of both paths, both streams (Np + 1 entries: W1[N] pairs with the last column)
-        for (int q = threadIdx.x; q < 4 * ngrp; q += kFftThreads) {
+        for (int q = threadIdx.x; q < 4 * ngrp; q += T) {
             const int g = q % ngrp, s = (q / ngrp) & 1, pth = q / (2 * ngrp);
             const int64_t m = 2 * pr + pth;
             float z[4] = {0.f, 0.f, 0.f, 0.f};
@@ -144,21 +292,15 @@ __global__ void __launch_bounds__(kFftThreads) k_mixed_fft(const __grid_constant
 #pragma unroll
             for (int e = 0; e < 4; ++e) o[e] = (4 * g + e < N) ? z[e] : 0.f;
         }
+        for (int n = N + threadIdx.x; n < W; n += T)  // tails of the four rows read as zeros
+#pragma unroll
+            for (int r = 0; r < 4; ++r) ws[r * W + n] = 0.f;
         __syncthreads();
-        // 2. z = W1_a + i W1_b, zero-padded to L
-        for (int n = threadIdx.x; n < L; n += kFftThreads)
-            b0[n] = (n < N) ? make_float2(ws[n], ws[2 * W + n]) : make_float2(0.f, 0.f);
-        if (threadIdx.x < 4) {
-            // padding entries [N, Np + 4) of the normal rows read as zeros below
-            for (int n = N; n < W; ++n) ws[threadIdx.x * W + n] = 0.f;
-        }
-        __syncthreads();
-        // 3. forward FFT, spectrum product (includes 1/L), inverse FFT
-        float2* f = fft_L<false>(b0, b1, L, a.logL, a.tw);
-        for (int n = threadIdx.x; n < L; n += kFftThreads) f[n] = cmul(f[n], __ldg(a.spec + n));
-        __syncthreads();
-        float2* g2 = (f == b0) ? b1 : b0;
-        float2* y = fft_L<true>(f, g2, L, a.logL, a.tw);
+        // 2-3. forward FFT of z = W1_a + i W1_b (zero-padded to L) times the
+        // spectrum (which includes 1/L), then the inverse FFT
+        const FftIn in{ws, W, N};
+        fft_inplace<LOGL, false, T>(buf, a.tw, in, a.spec);
+        fft_inplace<LOGL, true, T>(buf, a.tw, in, a.spec);
         // 4. epilogue: thread-strided columns for both paths
         const float* w1a = ws;
         const float* w1pa = ws + W;
@@ -169,8 +311,8 @@ __global__ void __launch_bounds__(kFftThreads) k_mixed_fft(const __grid_constant
             const float* bt = a.beta + (size_t)g * Np;
             const int lim = a.nsteps[g] - 1;
             float sva = 0.f, swa = 0.f, svb = 0.f, swb = 0.f;
-            for (int j = threadIdx.x; j < lim; j += kFftThreads) {
-                const float2 yj = y[j];
+            for (int j = threadIdx.x; j < lim; j += T) {
+                const float2 yj = buf[pidx(j)];
                 const float bj = __ldg(bt + j);
                 const float xa = yj.x + a.a1 * w1a[j] + a.a2 * w1pa[j];
                 const float xb = yj.y + a.a1 * w1b[j] + a.a2 * w1pb[j];
@@ -194,15 +336,15 @@ __global__ void __launch_bounds__(kFftThreads) k_mixed_fft(const __grid_constant
             }
         }
         if (a.dbg_x) {
-            for (int j = threadIdx.x; j < Np; j += kFftThreads) {
-                const float2 yj = y[j];
+            for (int j = threadIdx.x; j < Np; j += T) {
+                const float2 yj = (j < N) ? buf[pidx(j)] : make_float2(0.f, 0.f);
                 const int64_t ma = 2 * pr, mb = 2 * pr + 1;
                 if (ma < a.B) a.dbg_x[ma * Np + j] = (j < N) ? yj.x + a.a1 * w1a[j] + a.a2 * w1pa[j] : 0.f;
                 if (mb < a.B) a.dbg_x[mb * Np + j] = (j < N) ? yj.y + a.a1 * w1b[j] + a.a2 * w1pb[j] : 0.f;
             }
         }
         if (a.dbg_w) {
-            for (int j = threadIdx.x; j < Np; j += kFftThreads)
+            for (int j = threadIdx.x; j < Np; j += T)
                 for (int pth = 0; pth < 2; ++pth) {
                     const int64_t m = 2 * pr + pth;
                     if (m < a.B) {
@@ -215,7 +357,7 @@ __global__ void __launch_bounds__(kFftThreads) k_mixed_fft(const __grid_constant
         if (threadIdx.x < 2 * a.n_g) {
             const int g = threadIdx.x >> 1, pth = threadIdx.x & 1;
             float sv = 0.f, sw = 0.f;
-            for (int k = 0; k < kFftWarps; ++k) {
+            for (int k = 0; k < WARPS; ++k) {
                 const float* r = red + (k * a.n_g + g) * 4 + 2 * pth;
                 sv += r[0];
                 sw += r[1];
@@ -259,9 +401,10 @@ void fft_host(std::vector<std::complex<double>>& x, bool inverse)
 
 }  // namespace
 
+// L = 2^ceil(log2 2N), at least 16 so that every transform has a radix-16 pass
 int fft_log2_len(int N)
 {
-    int logL = 1;
+    int logL = 4;
     while ((1 << logL) < 2 * N) ++logL;
     return logL;
 }
@@ -291,18 +434,36 @@ void fft_tables(const double* gamma, int N, int logL, float* spec, float* tw)
     }
 }
 
-cudaError_t launch_mixed_fft(const MixedArgs& A, int sms, cudaStream_t st)
+template <int LOGL>
+static cudaError_t launch_fft_l(const MixedArgs& A, int sms, cudaStream_t st)
 {
-    const int smem = fft_smem(A.L, A.Np, A.n_g).total;
-    cudaError_t e = cudaFuncSetAttribute(k_mixed_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int smem = fft_smem(1 << LOGL, A.Np, A.n_g).total;
+    cudaError_t e = cudaFuncSetAttribute(k_mixed_fft<LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_fft, kFftThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_fft<LOGL>, fft_threads(LOGL), smem);
     if (per_sm < 1) per_sm = 1;
     const int64_t npairs = (A.B + 1) / 2;
     const int grid = (int)std::min<int64_t>(npairs, (int64_t)sms * per_sm);
-    k_mixed_fft<<<grid, kFftThreads, smem, st>>>(A);
+    k_mixed_fft<LOGL><<<grid, fft_threads(LOGL), smem, st>>>(A);
     return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_fft(const MixedArgs& A, int sms, cudaStream_t st)
+{
+    switch (A.logL) {
+        case 4: return launch_fft_l<4>(A, sms, st);
+        case 5: return launch_fft_l<5>(A, sms, st);
+        case 6: return launch_fft_l<6>(A, sms, st);
+        case 7: return launch_fft_l<7>(A, sms, st);
+        case 8: return launch_fft_l<8>(A, sms, st);
+        case 9: return launch_fft_l<9>(A, sms, st);
+        case 10: return launch_fft_l<10>(A, sms, st);
+        case 11: return launch_fft_l<11>(A, sms, st);
+        case 12: return launch_fft_l<12>(A, sms, st);
+        case 13: return launch_fft_l<13>(A, sms, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace rbg
