@@ -1062,10 +1062,11 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     return RBG_OK;
 }
 
+// The image is pageable host memory: the copy stages it before returning, so
+// the caller may release it at once.
 int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& err)
 {
-    if (cudaMemcpyAsync(ws, job.host_ws.data(), job.host_ws.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) {
+    if (cudaMemcpyAsync(ws, job.host_ws.data(), job.host_ws.size(), cudaMemcpyHostToDevice, st) != cudaSuccess) {
         cudaGetLastError();
         err = "mixed workspace upload failed";
         return RBG_ERR_CUDA;
