@@ -150,20 +150,23 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
+// One wait attempt; the hardware may suspend the thread for up to 20 us
+// (the suspend-time hint) until the phase completes, so waiting warps do not
+// spin on the issue slots the working roles need.
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(20000u)
         : "memory");
     return ok != 0;
 }
 
 // Bounded wait for the phase of the given parity; false on timeout or when
 // another role already failed (then the caller winds down).  The error word
-// and the clock are polled every 64 tries only.  With `prof` set (diagnostic
+// and the clock are polled every 64 tries only (at most 64 x 20 us apart).  With `prof` set (diagnostic
 // runs), lane 0 adds the cycles it waited to prof[site].
 __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site,
                                        unsigned long long* prof = nullptr)
