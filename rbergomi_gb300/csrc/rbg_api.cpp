@@ -811,6 +811,7 @@ void computeIV_tensor(double xi, double* H, double* eta, double* rho, int par_si
                       double* K_tot, int out_size)
 {
     check_dropin_sizes(par_size, op_size, num_threads, out_size);
+    if (out_size == 0) return;  // an empty grid: the reference's loops run zero times
     rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
     rbg_options o;
     rbg_default_options(&o);
@@ -825,6 +826,7 @@ void computeIVRT_tensor(double xi, double* H, double* eta, double* rho, int par_
                         double* K_tot, int out_size)
 {
     check_dropin_sizes(par_size, op_size, num_threads, out_size);
+    if (out_size == 0) return;  // an empty grid: the reference's loops run zero times
     rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
     rbg_options o;
     rbg_default_options(&o);
@@ -840,7 +842,7 @@ void computeIVRT_tensor_quadrature(double xi, double* H, double* eta, double* rh
                                    double* payoff)
 {
     (void)num_threads;
-    if (M <= 0) return;
+    if (M <= 0 || (long)par_size * op_size == 0) return;  // nothing to price: no payoffs written
     rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
     die_on(rbg_payoffs_rt(&p, nullptr, Z, payoff, 0));
 }

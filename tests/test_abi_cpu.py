@@ -153,3 +153,17 @@ def test_dropin_exit_codes(fn):
     assert r.returncode == 17 and "wrong size" in r.stderr
     r = _run(pre + call.format(nt=0, out=2))
     assert r.returncode == 21 and "positive integer" in r.stderr
+
+
+@pytest.mark.parametrize("fn", ["computeIVRT_tensor", "computeIV_tensor"])
+def test_dropin_empty_grid_returns(fn):
+    """par_size * op_size == out_size == 0: the reference's loops run zero
+    times and the call returns normally; so does the drop-in, without a GPU."""
+    code = ("import ctypes as C, rbergomi_gb300 as R\n"
+            "L=R.lib(); d=lambda n: (C.c_double*max(n,1))(); s=(C.c_uint64*1)(1)\n"
+            "L." + fn + "(0.04, d(0), d(0), d(0), 0, d(2), d(2), 2, 8, 16, s, 1, 1, "
+            "d(0), d(0), d(0), d(0), d(0), d(0), d(0), d(0), 0)\n"
+            "L.computeIVRT_tensor_quadrature(0.04, d(1), d(1), d(1), 1, d(0), d(0), 0, 8, 16, d(256), 1, d(0))\n"
+            "print('returned')\n")
+    r = _run(code)
+    assert r.returncode == 0 and "returned" in r.stdout, r.stderr
