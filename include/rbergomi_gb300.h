@@ -42,9 +42,10 @@ extern "C" {
  * stream Wperp per path, S_T = exp(sum sqrt(v) sqrt(dt) Z - dt/2 sum v) with
  * Z = rho W1 + sqrt(1 - rho^2) Wperp, payoff max(S_T - K, 0); S is
  * recomputed on the reference's rho trigger (eps 1e-10).  Same size checks,
- * exit codes and seed folding as computeIVRT_tensor.  Always FP64.  Like the
- * reference (cinterface.cpp:45), eta_tot receives the rho values and
- * rho_tot the eta values. */
+ * exit codes and seed folding as computeIVRT_tensor.  FP64 unless the
+ * environment sets RBG_PRECISION=mixed (then N <= 1024).  Like the reference
+ * (cinterface.cpp:45), eta_tot receives the rho values and rho_tot the eta
+ * values. */
 void computeIV_tensor(double xi, double* H, double* eta, double* rho, int par_size, double* T, double* K,
                       int op_size, int N, long M, uint64_t* seed, int seed_size, int num_threads, double* price,
                       double* iv, double* stat, double* H_tot, double* eta_tot, double* rho_tot, double* T_tot,
@@ -165,7 +166,8 @@ int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, do
 int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs);
 
 /* Plain Monte Carlo on the Philox stream (streams W1, W1perp, Wperp): the
- * estimator of computeIV_tensor with status codes.  FP64 form only. */
+ * estimator of computeIV_tensor with status codes.  FP64, or the mixed form
+ * (tcgen05 GEMM, N <= 1024; RBG_ERR_UNSUPPORTED above). */
 int rbg_price_mc(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv);
 
 /* Plain Monte Carlo per-path payoffs for caller-supplied normals: Z holds

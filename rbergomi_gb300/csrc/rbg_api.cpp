@@ -297,20 +297,22 @@ static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M,
 // Mixed form: tcgen05 fused path kernel writes FP32 (Ivdt, IsvdW) per
 // (variance group, path); the FP64 payoff/sum kernels finish.
 static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M, cudaStream_t st,
-                       double* host_res)
+                       double* host_res, bool mc = false)
 {
     TableSet ts;
     int rc = upload_tables(c, plan, st, ts);
     if (rc) return rc;
     const int no = (int)plan.outs.size();
     MixedJob job;
-    if ((rc = mixed_prepare(plan, o, M, job, g_err))) return rc;
+    if ((rc = mixed_prepare(plan, o, M, job, g_err, 0, mc))) return rc;
     const int64_t B = job.batch;
     if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
     const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
     const int64_t max_chunks = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
     if (!job.fused && (rc = ensure(c.ivb, sizeof(float) * 2 * plan.vgs.size() * (size_t)B, "variance sums")))
         return rc;
+    if (mc && (rc = ensure(c.ivp, sizeof(float) * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    float* ivq = mc ? c.ivp.as<float>() : nullptr;
     if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
     if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
     if ((rc = ensure(c.res, sizeof(double) * 5 * no, "results"))) return rc;
@@ -341,13 +343,14 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
         } else {
             {
                 ProfScope ps(kStageMixed, st, (int)job.launches.size());
-                if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, c.ivb.p, st, g_err)))
+                if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, c.ivb.p, st, g_err, nullptr,
+                                       nullptr, nullptr, nullptr, ivq)))
                     return rc;
             }
             const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
             {
                 ProfScope ps(kStagePayoff, st);
-                launch_payoff_sums_f32(ts.t.outs, no, c.ivb.p, b, G, c.part.as<double>(), nchunks, st);
+                launch_payoff_sums_f32(ts.t.outs, no, c.ivb.p, b, G, c.part.as<double>(), nchunks, st, ivq);
             }
             {
                 ProfScope ps(kStageReduce, st);
@@ -380,8 +383,7 @@ static int price_plan(const Plan& plan, int64_t M, const rbg_options* o, std::ve
             return fail(RBG_ERR_UNSUPPORTED, "FP64 form uses the direct Volterra sum");
         return price_fp64(*c, plan, *o, M, st, res.data(), mc);
     }
-    if (mc) return fail(RBG_ERR_UNSUPPORTED, "the plain Monte Carlo estimator runs in the FP64 form");
-    if (o->precision == RBG_MIXED) return price_mixed(*c, plan, *o, M, st, res.data());
+    if (o->precision == RBG_MIXED) return price_mixed(*c, plan, *o, M, st, res.data(), mc);
     return fail(RBG_ERR_ARG, "unknown precision");
 }
 
@@ -815,6 +817,8 @@ void computeIV_tensor(double xi, double* H, double* eta, double* rho, int par_si
     rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
     rbg_options o;
     rbg_default_options(&o);
+    const char* prec = std::getenv("RBG_PRECISION");
+    if (prec && std::strcmp(prec, "mixed") == 0) o.precision = RBG_MIXED;
     o.seed = fold_seed(seed, seed_size);
     die_on(rbg_price_mc(&p, &o, price, stat, iv));
     fill_tot(H, eta, rho, par_size, T, K, op_size, H_tot, rho_tot, eta_tot, T_tot, K_tot);

@@ -17,7 +17,8 @@
 // Toeplitz structure.  Time steps are cut into K-chunks of 32.  Chunk c
 // multiplies the A tile W1[:, 32c, 32c+32) into output columns [32c, Np):
 //   D[:, 32c + j'] += sum_{k'<32} A_c[:, k'] * S[j'][k'],  S[j'][k'] = Gamma[j' - k'],
-// and S does not depend on c.  So one Np x 32 strip S (hi and lo halves,
+// and S does not depend on c.  Its diagonal holds a1 instead of Gamma[0] = 0,
+// so the MMAs also add the hybrid scheme's near-field term a1 W1_j.  So one Np x 32 strip S (hi and lo halves,
 // 64 KB at N = 512) stays resident in shared memory for the whole kernel,
 // loaded once by a bulk async copy; only A tiles stream.  Two-pass tiles
 // (below) use a narrow strip instead: the two K = 16 halves of a chunk read
@@ -89,7 +90,11 @@ constexpr uint64_t kWaitNs = 2000000000ull;         // 2 s per wait
 //   mbarriers + TMEM address
 constexpr int kTileBytes = kTileM * kChunk * 2;                          // one 16-bit 128 x 32 tile, 8 KB
 constexpr int kStageA = 2 * kTileBytes;                                  // hi + lo
-constexpr int kStageF = (2 * kChunk + 1) * kTileM * 4;                   // w1, w1perp, boundary W1
+// FP32 stage: W1 tile, W1perp tile, W1 boundary row; plain Monte Carlo adds
+// a Wperp tile and its boundary row (offsets in floats)
+constexpr int kFW1p = kChunk * kTileM, kFBnd = 2 * kChunk * kTileM, kFWq = kFBnd + kTileM;
+constexpr int kFWqBnd = kFWq + kChunk * kTileM;
+__host__ __device__ constexpr int stage_f_bytes(int ns) { return (ns == 3 ? kFWqBnd + kTileM : kFWq) * 4; }
 
 // Strip width in K: the full chunk (32, SW64 rows, one row per output
 // column) where one TMEM pass covers Np; 16 (SW32, 16 leading zero rows)
@@ -109,15 +114,16 @@ struct SmemLayout {
     int strip, a0, f0, stages, acc, beta, otab, osum, bars, total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, int n_o)
+// ns: normal streams per path, 2 (RT) or 3 (plain Monte Carlo: ns sums per group)
+__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, int n_o, int ns = 2)
 {
     SmemLayout L;
     L.strip = 0;
     L.a0 = (strip_bytes(Np) + 1023) / 1024 * 1024;
     L.stages = stages;
     L.f0 = L.a0 + stages * kStageA;
-    L.acc = L.f0 + stages * kStageF;
-    L.beta = L.acc + 2 * n_g * 2 * kTileM * 4 + kTileM * 4;  // per warpgroup, then W1_0 per path
+    L.acc = L.f0 + stages * stage_f_bytes(ns);
+    L.beta = L.acc + 2 * n_g * ns * kTileM * 4 + (ns - 1) * kTileM * 4;  // per warpgroup, then W1_0 (Wperp_0)
     L.otab = L.beta + n_g * Np * 4;
     L.osum = (L.otab + n_o * 16 + 15) / 16 * 16;
     L.bars = L.osum + kEpiWarps * n_o * 16;
@@ -316,7 +322,7 @@ __device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rh
 // REDRAW (a first-pass chunk drawn again for the second pass), the FP32 W1 /
 // W1perp tiles the epilogue reads.  Compiled per REDRAW so that the W1 and
 // W1perp Philox streams stay interleaved in the common case.
-template <int BF16, bool REDRAW>
+template <int BF16, bool REDRAW, bool MC>
 __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKeys& keys, uint64_t gpath, bool valid,
                                               int64_t m, int p, int h, int c, int n0, unsigned char* st,
                                               float* w1s)
@@ -324,9 +330,9 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
     constexpr int SPT = kStepsPerThread;
     const int Np = a.Np;
     const int sw = (p >> 1) & 3;
-    float* w1ps = w1s + kChunk * kTileM;
+    float* w1ps = w1s + kFW1p;
     const int step0 = kChunk * c + SPT * h;
-    float w[SPT], wp[SPT];
+    float w[SPT], wp[SPT], wq[MC ? SPT : 1];
 #pragma unroll
     for (int q = 0; q < SPT / 4; ++q) {
         const uint32_t g = (uint32_t)((step0 >> 2) + q);
@@ -338,11 +344,20 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
             box_muller_f32(x1.x, x1.y, wp[4 * q], wp[4 * q + 1]);
             box_muller_f32(x1.z, x1.w, wp[4 * q + 2], wp[4 * q + 3]);
         }
+        if (MC && !REDRAW) {  // plain Monte Carlo: Wperp on stream 2
+            const uint4 x2 = philox_group(keys, gpath, g, 2);
+            box_muller_f32(x2.x, x2.y, wq[4 * q], wq[4 * q + 1]);
+            box_muller_f32(x2.z, x2.w, wq[4 * q + 2], wq[4 * q + 3]);
+        }
     }
     if (!(valid && step0 + SPT <= a.N)) {  // only the last tile / chunk
 #pragma unroll
         for (int q = 0; q < SPT; ++q) {
-            if (!valid || step0 + q >= a.N) { w[q] = 0.f; wp[q] = 0.f; }
+            if (!valid || step0 + q >= a.N) {
+                w[q] = 0.f;
+                wp[q] = 0.f;
+                if (MC) wq[q] = 0.f;
+            }
         }
     }
     // A tile: row p, logical 16-byte chunks covering steps [SPT h, SPT h + SPT), SW64 swizzle
@@ -361,6 +376,7 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
             const int at = ftile_at(p, SPT * h + q);
             *(float4*)(w1s + at) = make_float4(w[q], w[q + 1], w[q + 2], w[q + 3]);
             *(float4*)(w1ps + at) = make_float4(wp[q], wp[q + 1], wp[q + 2], wp[q + 3]);
+            if (MC) *(float4*)(w1s + kFWq + at) = make_float4(wq[q], wq[q + 1], wq[q + 2], wq[q + 3]);
         }
         // last chunk of the first pass: its successor (chunk n0) follows the
         // redrawn chunks, so W1 at step 32 n0 for the last column's sqrt(v) dW
@@ -369,7 +385,12 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
             const uint4 xb = philox_group(keys, gpath, (uint32_t)(8 * n0), 0);
             float b0, b1;
             box_muller_f32(xb.x, xb.y, b0, b1);
-            w1s[2 * kChunk * kTileM + p] = valid ? b0 : 0.f;
+            w1s[kFBnd + p] = valid ? b0 : 0.f;
+            if (MC) {
+                const uint4 xq = philox_group(keys, gpath, (uint32_t)(8 * n0), 2);
+                box_muller_f32(xq.x, xq.y, b0, b1);
+                w1s[kFWqBnd + p] = valid ? b0 : 0.f;
+            }
         }
         if (a.dbg_w && valid) {
 #pragma unroll
@@ -384,13 +405,15 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
 // TWO: two TMEM passes per tile (512 < Np <= 1024).  The one-pass
 // instantiation has n0 = 0 at compile time, so the virtual-chunk bookkeeping
 // folds away there.
-template <int BF16, bool TWO>
+template <int BF16, bool TWO, bool MC>
 __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
+    constexpr int NS = MC ? 3 : 2;  // normal streams per path = sums per variance group
+    constexpr int kStageFB = stage_f_bytes(NS);
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g, a.n_o);
+    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g, a.n_o, NS);
     unsigned char* strip = base + L.strip;
     float* acc_s = (float*)(base + L.acc);
     float* beta_s = (float*)(base + L.beta);
@@ -465,11 +488,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 const int c = (v < n0) ? v : v - n0;
                 if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
                 unsigned char* st = base + L.a0 + s * kStageA;
-                float* w1s = (float*)(base + L.f0 + s * kStageF);
+                float* w1s = (float*)(base + L.f0 + s * kStageFB);
                 if (TWO && redraw)
-                    produce_chunk<BF16, true>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+                    produce_chunk<BF16, true, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
                 else
-                    produce_chunk<BF16, false>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+                    produce_chunk<BF16, false, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
                 fence_proxy_async();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(full + s));
@@ -482,16 +505,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         const int quad = warp & 3;        // TMEM lane quadrant
         const int p = quad * 32 + lane;
         const uint32_t tlane = tmem + ((uint32_t)(quad * 32) << 16);
-        float* my_acc = acc_s + (size_t)wg * a.n_g * 2 * kTileM;
-        float* w10_s = acc_s + (size_t)2 * a.n_g * 2 * kTileM;  // W1_0 per path
+        // per warpgroup [group][NS sums][path]: sum v, sum sqrt(v) W1 (, sum sqrt(v) Wperp)
+        float* my_acc = acc_s + (size_t)wg * a.n_g * NS * kTileM;
+        float* w10_s = acc_s + (size_t)2 * a.n_g * NS * kTileM;  // W1_0 per path
+        float* wq0_s = w10_s + kTileM;                          // Wperp_0 per path (plain Monte Carlo)
         int64_t lt = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
             const int64_t m = tile * kTileM + p;
             const bool valid = m < a.B;
-            for (int g = 0; g < a.n_g; ++g) {
-                my_acc[(2 * g) * kTileM + p] = 0.f;
-                my_acc[(2 * g + 1) * kTileM + p] = 0.f;
-            }
+            for (int g = 0; g < a.n_g; ++g)
+#pragma unroll
+                for (int t = 0; t < NS; ++t) my_acc[(NS * g + t) * kTileM + p] = 0.f;
             for (int v = 0; v < nv; ++v) {
                 const int64_t gc = lt * nv + v;
                 const int s = (int)(gc % S);
@@ -518,8 +542,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     goto done;
                 if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
                 tc_fence_after();
-                const float* w1s = (const float*)(base + L.f0 + s * kStageF);
-                const float* w1ps = w1s + kChunk * kTileM;
+                const float* w1s = (const float*)(base + L.f0 + s * kStageFB);
+                const float* w1ps = w1s + kFW1p;
+                const float* wqs = w1s + kFWq;  // plain Monte Carlo only
 #pragma unroll 1
                 for (int hh = wg; hh < 2; hh += kEpiWGs) {
                     const int j0 = 16 * hh;
@@ -533,11 +558,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                         w1v[jj] = u.x; w1v[jj + 1] = u.y; w1v[jj + 2] = u.z; w1v[jj + 3] = u.w;
                         w1pv[jj] = v.x; w1pv[jj + 1] = v.y; w1pv[jj + 2] = v.z; w1pv[jj + 3] = v.w;
                     }
-                    const float w_after =
-                        (hh == 0) ? w1s[ftile_at(p, 16)]
-                                  : (!has_next ? 0.f
-                                     : bnd     ? w1s[2 * kChunk * kTileM + p]
-                                               : ((const float*)(base + L.f0 + sn * kStageF))[ftile_at(p, 0)]);
+                    const float* nexts = (const float*)(base + L.f0 + sn * kStageFB);
+                    const float w_after = (hh == 0) ? w1s[ftile_at(p, 16)]
+                                                    : (!has_next ? 0.f
+                                                       : bnd     ? w1s[kFBnd + p]
+                                                                 : nexts[ftile_at(p, 0)]);
+                    float wqv[MC ? 16 : 1], wq_after = 0.f;
+                    if (MC) {
+#pragma unroll
+                        for (int jj = 0; jj < 16; jj += 4) {
+                            const float4 u = *(const float4*)(wqs + ftile_at(p, j0 + jj));
+                            wqv[jj] = u.x; wqv[jj + 1] = u.y; wqv[jj + 2] = u.z; wqv[jj + 3] = u.w;
+                        }
+                        wq_after = (hh == 0) ? wqs[ftile_at(p, 16)]
+                                             : (!has_next ? 0.f
+                                                : bnd     ? w1s[kFWqBnd + p]
+                                                          : nexts[kFWq + ftile_at(p, 0)]);
+                    }
                     float x[16];
                     tmem_ld16(tlane + (uint32_t)(kChunk * c + j0) - tcol0, x);
                     if (pass_end && hh + kEpiWGs >= 2) {
@@ -550,11 +587,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj) {
                         const float w1 = w1v[jj];
-                        x[jj] = x[jj] + a.a1 * w1 + a.a2 * w1pv[jj];
+                        x[jj] = fmaf(a.a2, w1pv[jj], x[jj]);  // Y2 + a1 W1 came out of the MMA
                         if (jj > 0) wn[jj - 1] = w1;
-                        if (jj == 0 && j0 == 0 && c == 0) w10_s[p] = w1;
+                        if (jj == 0 && j0 == 0 && c == 0) {
+                            w10_s[p] = w1;
+                            if (MC) wq0_s[p] = wqv[0];
+                        }
                     }
                     wn[15] = w_after;
+                    float wqn[MC ? 16 : 1];  // Wperp one step ahead
+                    if (MC) {
+#pragma unroll
+                        for (int jj = 0; jj < 15; ++jj) wqn[jj] = wqv[jj + 1];
+                        wqn[15] = wq_after;
+                    }
                     if (a.dbg_x && valid) {
 #pragma unroll
                         for (int jj = 0; jj < 16; ++jj) a.dbg_x[m * Np + kChunk * c + j0 + jj] = x[jj];
@@ -563,15 +609,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     // one MUFU ex2 per element and group, v = su * su
                     for (int g = 0; g < a.n_g; ++g) {
                         const float ah = a.alpha[g];
-                        const float* bt = beta_s + g * Np + kChunk * c + j0;
+                        const float* btp = beta_s + g * Np + kChunk * c + j0;
+                        float bt[16];
+#pragma unroll
+                        for (int jj = 0; jj < 16; jj += 4) {
+                            const float4 u = *(const float4*)(btp + jj);  // 16-byte aligned: Np, j0 are multiples of 16
+                            bt[jj] = u.x; bt[jj + 1] = u.y; bt[jj + 2] = u.z; bt[jj + 3] = u.w;
+                        }
                         const int lim = a.nsteps[g] - 1 - kChunk * c - j0;
-                        float sv = 0.f, swv = 0.f;
+                        float sv = 0.f, swv = 0.f, swq = 0.f;
                         if (lim >= 16) {
 #pragma unroll
                             for (int jj = 0; jj < 16; ++jj) {
                                 const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
                                 sv = fmaf(su, su, sv);
                                 swv = fmaf(su, wn[jj], swv);
+                                if (MC) swq = fmaf(su, wqn[jj], swq);
                             }
                         } else {
 #pragma unroll
@@ -580,11 +633,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                                     const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
                                     sv = fmaf(su, su, sv);
                                     swv = fmaf(su, wn[jj], swv);
+                                    if (MC) swq = fmaf(su, wqn[jj], swq);
                                 }
                             }
                         }
-                        my_acc[(2 * g) * kTileM + p] += sv;
-                        my_acc[(2 * g + 1) * kTileM + p] += swv;
+                        my_acc[(NS * g) * kTileM + p] += sv;
+                        my_acc[(NS * g + 1) * kTileM + p] += swv;
+                        if (MC) my_acc[(NS * g + 2) * kTileM + p] += swq;
                     }
                 }
                 __syncwarp();
@@ -603,10 +658,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 const int g = (int)o.w;
                 if (g != g_last) {
                     g_last = g;
-                    float sv = acc_s[(2 * g) * kTileM + p], sw2 = acc_s[(2 * g + 1) * kTileM + p];
+                    float sv = acc_s[(NS * g) * kTileM + p], sw2 = acc_s[(NS * g + 1) * kTileM + p];
                     if (kEpiWGs == 2) {
-                        sv += acc_s[((size_t)a.n_g * 2 + 2 * g) * kTileM + p];
-                        sw2 += acc_s[((size_t)a.n_g * 2 + 2 * g + 1) * kTileM + p];
+                        sv += acc_s[((size_t)a.n_g * NS + NS * g) * kTileM + p];
+                        sw2 += acc_s[((size_t)a.n_g * NS + NS * g + 1) * kTileM + p];
                     }
                     iv_last = a.dt[g] * (a.xi + sv);
                     iw_last = a.sdt[g] * fmaf(a.sqrt_xi, w1_0, sw2);
@@ -628,13 +683,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
             }
             if (wg == 0 && valid && a.ivb) {
                 for (int g = 0; g < a.n_g; ++g) {
-                    float sv = acc_s[(2 * g) * kTileM + p], sw2 = acc_s[(2 * g + 1) * kTileM + p];
+                    float sv = acc_s[(NS * g) * kTileM + p], sw2 = acc_s[(NS * g + 1) * kTileM + p];
                     if (kEpiWGs == 2) {
-                        sv += acc_s[((size_t)a.n_g * 2 + 2 * g) * kTileM + p];
-                        sw2 += acc_s[((size_t)a.n_g * 2 + 2 * g + 1) * kTileM + p];
+                        sv += acc_s[((size_t)a.n_g * NS + NS * g) * kTileM + p];
+                        sw2 += acc_s[((size_t)a.n_g * NS + NS * g + 1) * kTileM + p];
                     }
                     a.ivb[(size_t)(a.g0 + g) * a.B + m] =
                         make_float2(a.dt[g] * (a.xi + sv), a.sdt[g] * fmaf(a.sqrt_xi, w1_0, sw2));
+                    if (MC) {
+                        // IsvdWp = sdt (sqrt(xi) Wperp_0 + sum sqrt(v_j) Wperp_j)
+                        float sq = acc_s[(NS * g + 2) * kTileM + p];
+                        if (kEpiWGs == 2) sq += acc_s[((size_t)a.n_g * NS + NS * g + 2) * kTileM + p];
+                        a.ivq[(size_t)(a.g0 + g) * a.B + m] = a.sdt[g] * fmaf(a.sqrt_xi, wq0_s[p], sq);
+                    }
                 }
             }
             if (a.prof && lane == 0) atomicAdd(a.prof + 20, (unsigned long long)(clock64() - bs_t0));
@@ -740,9 +801,18 @@ done:
 // ----------------------------------------------- FP32 payoffs, FP64 sums
 constexpr int kOPB32 = 8;
 
+// Plain Monte Carlo payoff in FP32: S_T = exp(rho IsvdW + sqrt(1 - rho^2) IsvdWp
+// - Ivdt / 2) (the FP64 form's mc_payoff), payoff max(S_T - K, 0).
+__device__ __forceinline__ float mc_payoff_f32(float Ivdt, float IsvdW, float IsvdWp, float rho, float K)
+{
+    const float lnS = fmaf(rho, IsvdW, fmaf(sqrtf(fmaxf(1.0f - rho * rho, 0.0f)), IsvdWp, -0.5f * Ivdt));
+    return fmaxf(ex2_approx(1.4426950408889634f * lnS) - K, 0.0f);
+}
+
+template <bool MC>
 __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restrict__ outs, int n_out,
                                                          const float2* __restrict__ ivb, int64_t B, int G,
-                                                         double* __restrict__ part)
+                                                         double* __restrict__ part, const float* __restrict__ ivq)
 {
     __shared__ double red[8][kOPB32][2];
     const int c = blockIdx.x;
@@ -765,11 +835,16 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
         if (m >= B) break;
         int cur = -1;
         float2 iv = make_float2(0.f, 0.f);
+        float ip = 0.f;
 #pragma unroll
         for (int q = 0; q < kOPB32; ++q) {
             if (vg[q] < 0) continue;
-            if (vg[q] != cur) { cur = vg[q]; iv = ivb[(size_t)cur * B + m]; }
-            const float x = rt_payoff_f32(iv.x, iv.y, rho[q], K[q], lnK[q]);
+            if (vg[q] != cur) {
+                cur = vg[q];
+                iv = ivb[(size_t)cur * B + m];
+                if (MC) ip = ivq[(size_t)cur * B + m];
+            }
+            const float x = MC ? mc_payoff_f32(iv.x, iv.y, ip, rho[q], K[q]) : rt_payoff_f32(iv.x, iv.y, rho[q], K[q], lnK[q]);
             s1[q] += x;
             s2[q] = fmaf(x, x, s2[q]);
         }
@@ -800,10 +875,11 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
 }
 
 void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int64_t B, int G, double* part,
-                            int nchunks, cudaStream_t st)
+                            int nchunks, cudaStream_t st, const float* ivq)
 {
     dim3 grid(nchunks, (n_out + kOPB32 - 1) / kOPB32);
-    k_payoff_sums_f32<<<grid, 256, 0, st>>>(outs, n_out, (const float2*)ivb, B, G, part);
+    if (ivq) k_payoff_sums_f32<true><<<grid, 256, 0, st>>>(outs, n_out, (const float2*)ivb, B, G, part, ivq);
+    else k_payoff_sums_f32<false><<<grid, 256, 0, st>>>(outs, n_out, (const float2*)ivb, B, G, part, ivq);
     count_launch();
 }
 
@@ -838,12 +914,12 @@ float from_f16(uint16_t u)
 }
 
 // The strip image the MMA descriptors expect, hi/lo 16-bit halves:
-//   wide   S[j][k] = Gamma[j - k], rows j in [0, Np), SW64 K-major: row j at
+//   wide   S[j][k] = Gamma[j - k] (a1 at j = k), rows j in [0, Np), SW64 K-major: row j at
 //          j * 64 bytes, 16-byte chunk (k / 8) XOR ((j / 2) mod 4);
-//   narrow P[r][k] = Gamma[r - 16 - k], rows r in [0, Np + 16), SW32 K-major:
+//   narrow P[r][k] = Gamma[r - 16 - k] (a1 at r - 16 = k), rows r in [0, Np + 16), SW32 K-major:
 //          row r at r * 32 bytes, 16-byte chunk (k / 8) XOR ((r / 4) mod 2);
 // zero where the Gamma index is negative or >= N.
-void build_strip(const double* gamma, int N, int Np, int bf16, unsigned char* img)
+void build_strip(const double* gamma, int N, int Np, int bf16, double a1, unsigned char* img)
 {
     const size_t half = (size_t)strip_bytes(Np) / 2;
     std::memset(img, 0, 2 * half);
@@ -852,7 +928,9 @@ void build_strip(const double* gamma, int N, int Np, int bf16, unsigned char* im
     for (int r = 0; r < rows; ++r)
         for (int k = 0; k < kw; ++k) {
             const int d = r - lead - k;
-            const double gv = (d >= 0 && d < N) ? gamma[d] : 0.0;
+            // the diagonal carries a1 (Gamma[0] = 0 otherwise), so the MMA also adds the
+            // near-field term a1 W1_j to column j
+            const double gv = (d == 0) ? a1 : (d > 0 && d < N) ? gamma[d] : 0.0;
             uint16_t hi, lo;
             if (bf16) {
                 hi = to_bf16((float)gv);
@@ -889,7 +967,7 @@ void mixed_twiddle_range(const MixedJob& job, size_t* off, size_t* bytes)
 }
 
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
-                  int64_t max_batch)
+                  int64_t max_batch, bool mc)
 {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -915,11 +993,17 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         err = "mixed GEMM form supports N <= 1024 (two passes over 128 x 512 FP32 TMEM columns); use the FFT backend";
         return RBG_ERR_UNSUPPORTED;
     }
+    if (mc && backend != RBG_CONV_GEMM) {
+        err = "mixed plain Monte Carlo runs on the GEMM backend (N <= 1024)";
+        return RBG_ERR_UNSUPPORTED;
+    }
     if (backend == RBG_CONV_FFT && N > 4096) {
         err = "mixed FFT backend supports N <= 4096 (two 8192-point buffers in shared memory)";
         return RBG_ERR_UNSUPPORTED;
     }
     job = MixedJob();
+    job.mc = mc;
+    const int ns = mc ? 3 : 2;
     job.backend = backend;
     job.N = N;
     job.n_vol = (int)plan.vols.size();
@@ -933,8 +1017,8 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     // variance groups per GEMM launch: as many as fit two pipeline stages
     int ng_cap = kMaxG;
     if (backend == RBG_CONV_GEMM) {
-        while (ng_cap > 1 && smem_layout(Np, 2, ng_cap, 0).total > optin) --ng_cap;
-        if (smem_layout(Np, 2, ng_cap, 0).total > optin) {
+        while (ng_cap > 1 && smem_layout(Np, 2, ng_cap, 0, ns).total > optin) --ng_cap;
+        if (smem_layout(Np, 2, ng_cap, 0, ns).total > optin) {
             err = "mixed kernel shared memory does not fit";
             return RBG_ERR_UNSUPPORTED;
         }
@@ -1005,15 +1089,15 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     // Pricing the payoffs inside the path kernel's epilogue (RBG_FUSE_PAYOFFS)
     // measured slower than the separate FP32 payoff kernel on GB300: the
     // epilogue warps are the kernel's critical path.
-    job.fused = RBG_FUSE_PAYOFFS && (backend == RBG_CONV_GEMM);
+    job.fused = RBG_FUSE_PAYOFFS && (backend == RBG_CONV_GEMM) && !mc;
     for (const MixedLaunch& r : job.launches)
         if (r.args.n_o > kMixedMaxFused || smem_layout(Np, 2, r.args.n_g, r.args.n_o).total > optin)
             job.fused = false;
     for (MixedLaunch& r : job.launches) {
         MixedArgs& A = r.args;
         const int no = job.fused ? A.n_o : 0;
-        A.stages = (smem_layout(Np, 3, A.n_g, no).total <= optin) ? 3 : 2;
-        if (backend == RBG_CONV_GEMM && smem_layout(Np, A.stages, A.n_g, no).total > optin) {
+        A.stages = (smem_layout(Np, 3, A.n_g, no, ns).total <= optin) ? 3 : 2;
+        if (backend == RBG_CONV_GEMM && smem_layout(Np, A.stages, A.n_g, no, ns).total > optin) {
             err = "mixed kernel shared memory does not fit";
             return RBG_ERR_UNSUPPORTED;
         }
@@ -1030,7 +1114,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         const MixedArgs& A = r.args;
         const int vol = plan.vgs[A.g0].vol;
         if (backend == RBG_CONV_GEMM)
-            build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, bf16, ws.data() + r.off_strip);
+            build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, bf16, plan.vols[vol].a1, ws.data() + r.off_strip);
         else
             fft_tables(plan.gamma.data() + (size_t)vol * N, N, A.logL, (float*)(ws.data() + r.off_spec),
                        (float*)(ws.data() + job.off_tw));
@@ -1085,8 +1169,12 @@ int mixed_part_rows(const MixedJob& job, int64_t B)
 
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
                  cudaStream_t st, std::string& err, float* dbg_w, float* dbg_x, double* part,
-                 unsigned long long* prof)
+                 unsigned long long* prof, float* ivq)
 {
+    if (job.mc && !ivq) {
+        err = "plain Monte Carlo launch without an IsvdWp buffer";
+        return RBG_ERR_ARG;
+    }
     unsigned char* base = (unsigned char*)ws;
     for (const MixedLaunch& r : job.launches) {
         MixedArgs A = r.args;
@@ -1102,13 +1190,14 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         if (!job.fused || !part) A.n_o = 0;
         A.tw = (const float2*)(base + job.off_tw);
         A.ivb = (float2*)ivb;
+        A.ivq = ivq;
         A.err = (unsigned int*)(base + job.off_err);
         A.dbg_w = dbg_w;
         A.dbg_x = dbg_x;
         A.seed = seed;
         A.path0 = path0;
         A.B = B;
-        const int smem = smem_layout(A.Np, A.stages, A.n_g, A.n_o).total;
+        const int smem = smem_layout(A.Np, A.stages, A.n_g, A.n_o, job.mc ? 3 : 2).total;
         const int64_t ntiles = (B + kTileM - 1) / kTileM;
         const int grid = (int)std::min<int64_t>(ntiles, job.sms);
         cudaError_t e;
@@ -1116,8 +1205,13 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
             e = launch_mixed_fft(A, job.sms, st);
         } else {
             void (*kern)(MixedArgs);
-            if (job.split == RBG_SPLIT_BF16X3) kern = A.n0 > 0 ? k_mixed_gemm<1, true> : k_mixed_gemm<1, false>;
-            else kern = A.n0 > 0 ? k_mixed_gemm<0, true> : k_mixed_gemm<0, false>;
+            const bool two = A.n0 > 0;
+            if (job.split == RBG_SPLIT_BF16X3)
+                kern = job.mc ? (two ? k_mixed_gemm<1, true, true> : k_mixed_gemm<1, false, true>)
+                              : (two ? k_mixed_gemm<1, true, false> : k_mixed_gemm<1, false, false>);
+            else
+                kern = job.mc ? (two ? k_mixed_gemm<0, true, true> : k_mixed_gemm<0, false, true>)
+                              : (two ? k_mixed_gemm<0, true, false> : k_mixed_gemm<0, false, false>);
             e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e == cudaSuccess) kern<<<grid, kThreads, smem, st>>>(A);
         }

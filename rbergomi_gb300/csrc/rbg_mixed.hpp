@@ -21,6 +21,7 @@ struct MixedArgs {
     const unsigned char* strip;  // [hi | lo], each Np*64 bytes, SW64 K-major image
     const float* beta;           // [n_g][Np] (log2 compensator - log2 xi) / 2
     float2* ivb;                 // [n_vg_total][B] (Ivdt, IsvdW)
+    float* ivq;                  // plain Monte Carlo: [n_vg_total][B] IsvdWp = sum sqrt(v) sdt Wperp
     unsigned int* err;           // 0, or the id of the wait that expired
     float* dbg_w;                // optional [B][2][Np] normals the producers drew
     float* dbg_x;                // optional [B][Np] X = Y2 + a1 W1 + a2 W1perp
@@ -54,14 +55,16 @@ struct MixedJob {
     int N = 0, n_vol = 0, n_vg = 0, split = 0, sms = 0;
     int backend = RBG_CONV_GEMM;  // RBG_CONV_GEMM or RBG_CONV_FFT
     bool fused = false;           // payoffs priced inside the path kernel (GEMM backend, <= 64 per launch)
+    bool mc = false;              // plain Monte Carlo: third normal stream Wperp and IsvdWp per (group, path)
     size_t off_tw = 0;
     std::vector<MixedLaunch> launches;   // one per (Volterra pass, <= 16 groups)
     std::vector<const void*> table_dev;  // optional device copies of each launch's strip / spectrum
     std::vector<unsigned char> host_ws;  // image uploaded by mixed_upload
 };
 
+// mc: the plain Monte Carlo estimator (GEMM backend, N <= 1024).
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
-                  int64_t max_batch = 0);
+                  int64_t max_batch = 0, bool mc = false);
 // Byte range of launch i's strip (GEMM) or spectrum (FFT) inside host_ws, and
 // of the shared FFT twiddle table (empty for the GEMM backend).
 void mixed_table_range(const MixedJob& job, int i, size_t* off, size_t* bytes);
@@ -71,9 +74,10 @@ int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& er
 // write (Ivdt, IsvdW) to ivb; fused jobs add their payoff sums to `part`
 // (rows = mixed_part_rows(job, B), zeroed by the caller) and write ivb only
 // when it is non-null.
+// Plain Monte Carlo jobs also write IsvdWp per (group, path) to ivq.
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
                  cudaStream_t st, std::string& err, float* dbg_w = nullptr, float* dbg_x = nullptr,
-                 double* part = nullptr, unsigned long long* prof = nullptr);
+                 double* part = nullptr, unsigned long long* prof = nullptr, float* ivq = nullptr);
 int mixed_part_rows(const MixedJob& job, int64_t B);
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
 // FFT backend (rbg_fft.cu)
@@ -82,7 +86,8 @@ size_t fft_smem_bytes(int N, int n_g);
 void fft_tables(const double* gamma, int N, int logL, float* spec, float* tw);
 cudaError_t launch_mixed_fft(const MixedArgs& A, int sms, cudaStream_t st);
 
+// ivq non-null: plain Monte Carlo payoffs max(S_T - K, 0) from (Ivdt, IsvdW, IsvdWp)
 void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int64_t B, int G, double* part,
-                            int nchunks, cudaStream_t st);
+                            int nchunks, cudaStream_t st, const float* ivq = nullptr);
 
 }  // namespace rbg

@@ -2,7 +2,8 @@
 computeIV_tensor, rBergLib/cinterface.cpp:10-46 over rBergomiMT.cpp:174-289):
 third normal stream, S_T from the log-Euler sum, payoff max(S_T - K, 0), S
 recomputed only on the rho trigger.  FP64 form: 1e-12 relative on prices
-against the reference's own output and the oracle on identical normals."""
+against the reference's own output and the oracle on identical normals.
+Mixed form: against the FP64 form on identical FP32 normals."""
 import numpy as np
 import pytest
 
@@ -83,6 +84,30 @@ def test_mc_and_rt_estimate_the_same_price(R):
     assert np.all(sr < sm)  # conditioning on W1 reduces the variance
 
 
-def test_mc_mixed_precision_is_rejected(R):
+@pytest.mark.parametrize("N", [100, 512, 700])
+def test_mc_mixed_vs_fp64_identical_normals(R, N):
+    """Mixed plain MC (third Philox stream in the fused tcgen05 kernel, FP32
+    payoffs) against the FP64 form on the same FP32 normals: <= 1e-4
+    relative and < 0.2 standard errors; one- and two-pass GEMM."""
+    xi, H, eta, rho = 0.235 ** 2, [0.07, 0.2], [1.9, 1.2], [-0.9, -0.6]
+    T, K = [0.5, 0.5, 1.5], [0.9, 1.1, 1.0]
+    M = 1 << 15
+    mp, ms, _ = R.price_mc(xi, H, eta, rho, T, K, N, M, seed=9, precision=R.MIXED)
+    fp, fs, _ = R.price_mc(xi, H, eta, rho, T, K, N, M, seed=9, normals=R.NORMALS_F32)
+    err = np.abs(mp - fp)
+    assert np.all(err <= 1e-4 * fp)
+    assert np.all(err < 0.2 * fs)
+    assert np.all(np.abs(ms / fs - 1) < 1e-3)
+
+
+def test_mc_mixed_rejects_fft_range(R):
     with pytest.raises(R.RbgError):
-        R.price_mc(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 64, 256, precision=R.MIXED)
+        R.price_mc(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 2048, 256, precision=R.MIXED)
+
+
+def test_computeIV_tensor_mixed_env(R, monkeypatch):
+    monkeypatch.setenv("RBG_PRECISION", "mixed")
+    xi, H, eta, rho, T, K = 0.05, [0.1], [1.5], [-0.7], [1.0], [1.0]
+    res = R.computeIV_tensor(xi, H, eta, rho, T, K, 128, 1 << 14, [5])
+    p, s, _ = R.price_mc(xi, H, eta, rho, T, K, 128, 1 << 14, seed=5, precision=R.MIXED)
+    np.testing.assert_array_equal(res.price, p)
