@@ -311,6 +311,68 @@ def run_gpu(args, w):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------- ParamTot grid arm
+GRID_H, GRID_ETA, GRID_RHO = [0.05, 0.1, 0.2, 0.3], [1.0, 1.5, 2.0, 2.5], [-0.95, -0.7, -0.5]
+GRID_T = [0.25, 0.5, 1.0, 2.0]
+GRID_K = [round(0.7 + 0.06 * i, 10) for i in range(11)]
+
+
+def run_grid(args):
+    """The full ParamTot grid sharing one Gaussian draw: 48 (H, eta, rho) tuples
+    (H slowest, rho fastest) x 4 maturities x 11 strikes, 256 steps per unit
+    time, M = 2^20, seed 7.  One call per maturity with N_T = 256 T steps:
+    the shorter maturities price on prefixes of the same Philox paths.  One
+    step = the four calls."""
+    import torch
+
+    import rbergomi_gb300 as R
+
+    torch.cuda.set_device(0)
+    R.lib()
+    stream = torch.cuda.current_stream()
+    prec = R.MIXED if args.precision == "mixed" else R.FP64
+    M = int(args.paths or (1 << 20))
+    H = [h for h in GRID_H for _ in GRID_ETA for _ in GRID_RHO]
+    eta = [e for _ in GRID_H for e in GRID_ETA for _ in GRID_RHO]
+    rho = [r for _ in GRID_H for _ in GRID_ETA for r in GRID_RHO]
+    flush = torch.empty((256 << 20) // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        out = []
+        for T in GRID_T:
+            out.append(R.price_rt(0.235 ** 2, H, eta, rho, [T] * len(GRID_K), GRID_K, int(256 * T), M, seed=7,
+                                  precision=prec, stream=stream.cuda_stream))
+        return out
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    n0 = R.launch_count()
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    psteps = M * sum(int(256 * T) for T in GRID_T) * len(GRID_H)
+    prices = len(H) * len(GRID_K) * len(GRID_T)
+    print(json.dumps({
+        "metric": METRIC, "value": psteps / (ms / 1e3), "unit": "path-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == R.FP64 else "bf16x3+f32+f64", "data": "synthetic (Philox4x32-10 normals)",
+        "config": {"workload": "paramtot-grid-m1m", "M": M, "tuples": len(H), "maturities": GRID_T,
+                   "strikes": len(GRID_K), "steps_per_unit_time": 256, "seed": 7, "precision": args.precision,
+                   "l2": "flushed (256 MiB write) before each step"},
+        "prices_per_s": prices / (ms / 1e3), "clocks": clk.summary(), "gpu_launches": R.launch_count() - n0,
+    }))
+
+
 # ------------------------------------------------------------ serving arm
 def serving_requests(n: int, rate: float, seed: int = 20261203):
     """Calibration-style traffic: Poisson arrivals at `rate`/s; H ~ U[.03,.45],
@@ -411,7 +473,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS) + ["serving-poisson"])
+    ap.add_argument("--workload", default=DEFAULT,
+                    choices=sorted(WORKLOADS) + ["serving-poisson", "paramtot-grid-m1m"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
     ap.add_argument("--split", type=int, default=0, help="0 = BF16x3, 1 = FP16x3")
     ap.add_argument("--cpu-paths", type=int, default=1 << 17)
@@ -427,6 +490,10 @@ def main():
     args = ap.parse_args()
     if args.workload == "serving-poisson":
         run_serving(args)
+        return
+    if args.workload == "paramtot-grid-m1m":
+        args.precision = args.precision or "fp64"
+        run_grid(args)
         return
     w = dict(WORKLOADS[args.workload])
     if args.paths:

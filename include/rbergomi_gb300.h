@@ -43,7 +43,7 @@ extern "C" {
  * Z = rho W1 + sqrt(1 - rho^2) Wperp, payoff max(S_T - K, 0); S is
  * recomputed on the reference's rho trigger (eps 1e-10).  Same size checks,
  * exit codes and seed folding as computeIVRT_tensor.  FP64 unless the
- * environment sets RBG_PRECISION=mixed (then N <= 1024).  Like the reference
+ * environment sets RBG_PRECISION=mixed.  Like the reference
  * (cinterface.cpp:45), eta_tot receives the rho values and rho_tot the eta
  * values. */
 void computeIV_tensor(double xi, double* H, double* eta, double* rho, int par_size, double* T, double* K,
@@ -167,7 +167,7 @@ int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, d
 
 /* Plain Monte Carlo on the Philox stream (streams W1, W1perp, Wperp): the
  * estimator of computeIV_tensor with status codes.  FP64, or the mixed form
- * (tcgen05 GEMM, N <= 1024; RBG_ERR_UNSUPPORTED above). */
+ * (tcgen05 GEMM for N <= 1024, batched FFT above). */
 int rbg_price_mc(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv);
 
 /* Plain Monte Carlo per-path payoffs for caller-supplied normals: Z holds

@@ -139,13 +139,14 @@ __device__ __forceinline__ int out_slot(int k)
 enum { SRC_BUF = 0, SRC_WS = 1, SRC_WS_DUP = 2 };
 
 struct FftIn {
-    const float* w1a;  // W1 of the pair's first path; the second path's W1 is 2 W floats further
-    int W, N;
+    const float* w1a;  // W1 of the pair's first path
+    const float* w1b;  // W1 of the second path
+    int N;
 };
 
 __device__ __forceinline__ float2 ws_z(const FftIn& in, int n)
 {
-    return n < in.N ? make_float2(in.w1a[n], in.w1a[2 * in.W + n]) : make_float2(0.f, 0.f);
+    return n < in.N ? make_float2(in.w1a[n], in.w1b[n]) : make_float2(0.f, 0.f);
 }
 
 // One in-place Stockham pass of radix R over L = 2^LOGL points, span 2^LNS.
@@ -248,7 +249,8 @@ struct FftSmem {
     int buf, w, red, total;
 };
 
-__host__ __device__ inline FftSmem fft_smem(int L, int Np, int n_g)
+// ns normal streams per path: 2 (RT) or 3 (plain Monte Carlo adds Wperp)
+__host__ __device__ inline FftSmem fft_smem(int L, int Np, int n_g, int ns = 2)
 {
     int logL = 0;
     while ((1 << logL) < L) ++logL;
@@ -256,20 +258,21 @@ __host__ __device__ inline FftSmem fft_smem(int L, int Np, int n_g)
     FftSmem S;
     S.buf = 0;
     S.w = (L + L / 16) * 8;                        // padded transform buffer
-    S.red = S.w + 2 * 2 * (Np + 4) * 4;            // [2 paths][W1 | W1perp][Np + 4]
-    S.total = S.red + warps * n_g * 4 * 4 + 64;
+    S.red = S.w + 2 * ns * (Np + 4) * 4;           // [2 paths][W1 | W1perp (| Wperp)][Np + 4]
+    S.total = S.red + warps * n_g * 2 * ns * 4 + 64;
     return S;
 }
 
-template <int LOGL>
+// MC: plain Monte Carlo, a third normal stream (Wperp) and IsvdWp per path.
+template <int LOGL, bool MC>
 __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed_fft(const __grid_constant__ MixedArgs a)
 {
-    constexpr int T = fft_threads(LOGL), L = 1 << LOGL, WARPS = T / 32;
+    constexpr int T = fft_threads(LOGL), L = 1 << LOGL, WARPS = T / 32, NS = MC ? 3 : 2;
     extern __shared__ __align__(16) unsigned char smf[];
     const int N = a.N, Np = a.Np;
-    const FftSmem S = fft_smem(L, Np, a.n_g);
+    const FftSmem S = fft_smem(L, Np, a.n_g, NS);
     float2* buf = (float2*)(smf + S.buf);
-    float* ws = (float*)(smf + S.w);  // path q, stream s: ws + (2q + s) * (Np + 4)
+    float* ws = (float*)(smf + S.w);  // path q, stream s: ws + (NS q + s) * (Np + 4)
     float* red = (float*)(smf + S.red);
     const int W = Np + 4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -279,8 +282,8 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
 
     for (int64_t pr = blockIdx.x; pr < npairs; pr += gridDim.x) {
         // 1. normals of both paths, both streams (Np + 1 entries: W1[N] pairs with the last column)
-        for (int q = threadIdx.x; q < 4 * ngrp; q += T) {
-            const int g = q % ngrp, s = (q / ngrp) & 1, pth = q / (2 * ngrp);
+        for (int q = threadIdx.x; q < 2 * NS * ngrp; q += T) {
+            const int g = q % ngrp, s = (q / ngrp) % NS, pth = q / (NS * ngrp);
             const int64_t m = 2 * pr + pth;
             float z[4] = {0.f, 0.f, 0.f, 0.f};
             if (m < a.B) {
@@ -288,29 +291,31 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
                 box_muller_f32(x.x, x.y, z[0], z[1]);
                 box_muller_f32(x.z, x.w, z[2], z[3]);
             }
-            float* o = ws + (2 * pth + s) * W + 4 * g;
+            float* o = ws + (NS * pth + s) * W + 4 * g;
 #pragma unroll
             for (int e = 0; e < 4; ++e) o[e] = (4 * g + e < N) ? z[e] : 0.f;
         }
-        for (int n = N + threadIdx.x; n < W; n += T)  // tails of the four rows read as zeros
+        for (int n = N + threadIdx.x; n < W; n += T)  // tails of the rows read as zeros
 #pragma unroll
-            for (int r = 0; r < 4; ++r) ws[r * W + n] = 0.f;
+            for (int r = 0; r < 2 * NS; ++r) ws[r * W + n] = 0.f;
         __syncthreads();
         // 2-3. forward FFT of z = W1_a + i W1_b (zero-padded to L) times the
         // spectrum (which includes 1/L), then the inverse FFT
-        const FftIn in{ws, W, N};
+        const FftIn in{ws, ws + NS * W, N};
         fft_inplace<LOGL, false, T>(buf, a.tw, in, a.spec);
         fft_inplace<LOGL, true, T>(buf, a.tw, in, a.spec);
         // 4. epilogue: thread-strided columns for both paths
         const float* w1a = ws;
         const float* w1pa = ws + W;
-        const float* w1b = ws + 2 * W;
-        const float* w1pb = ws + 3 * W;
+        const float* w1b = ws + NS * W;
+        const float* w1pb = ws + (NS + 1) * W;
+        const float* wqa = ws + 2 * W;         // plain Monte Carlo only
+        const float* wqb = ws + (NS + 2) * W;
         for (int g = 0; g < a.n_g; ++g) {
             const float ah = a.alpha[g];
             const float* bt = a.beta + (size_t)g * Np;
             const int lim = a.nsteps[g] - 1;
-            float sva = 0.f, swa = 0.f, svb = 0.f, swb = 0.f;
+            float sva = 0.f, swa = 0.f, svb = 0.f, swb = 0.f, sqa = 0.f, sqb = 0.f;
             for (int j = threadIdx.x; j < lim; j += T) {
                 const float2 yj = buf[pidx(j)];
                 const float bj = __ldg(bt + j);
@@ -322,6 +327,10 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
                 swa = fmaf(sua, w1a[j + 1], swa);
                 svb = fmaf(sub, sub, svb);
                 swb = fmaf(sub, w1b[j + 1], swb);
+                if (MC) {
+                    sqa = fmaf(sua, wqa[j + 1], sqa);
+                    sqb = fmaf(sub, wqb[j + 1], sqb);
+                }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -329,10 +338,15 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
                 swa += __shfl_xor_sync(0xffffffffu, swa, o);
                 svb += __shfl_xor_sync(0xffffffffu, svb, o);
                 swb += __shfl_xor_sync(0xffffffffu, swb, o);
+                if (MC) {
+                    sqa += __shfl_xor_sync(0xffffffffu, sqa, o);
+                    sqb += __shfl_xor_sync(0xffffffffu, sqb, o);
+                }
             }
             if (lane == 0) {
-                float* r = red + (warp * a.n_g + g) * 4;
+                float* r = red + (warp * a.n_g + g) * 2 * NS;
                 r[0] = sva; r[1] = swa; r[2] = svb; r[3] = swb;
+                if (MC) { r[4] = sqa; r[5] = sqb; }
             }
         }
         if (a.dbg_x) {
@@ -348,26 +362,28 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
                 for (int pth = 0; pth < 2; ++pth) {
                     const int64_t m = 2 * pr + pth;
                     if (m < a.B) {
-                        a.dbg_w[(m * 2 + 0) * Np + j] = ws[(2 * pth) * W + j];
-                        a.dbg_w[(m * 2 + 1) * Np + j] = ws[(2 * pth + 1) * W + j];
+                        a.dbg_w[(m * 2 + 0) * Np + j] = ws[(NS * pth) * W + j];
+                        a.dbg_w[(m * 2 + 1) * Np + j] = ws[(NS * pth + 1) * W + j];
                     }
                 }
         }
         __syncthreads();
         if (threadIdx.x < 2 * a.n_g) {
             const int g = threadIdx.x >> 1, pth = threadIdx.x & 1;
-            float sv = 0.f, sw = 0.f;
+            float sv = 0.f, sw = 0.f, sq = 0.f;
             for (int k = 0; k < WARPS; ++k) {
-                const float* r = red + (k * a.n_g + g) * 4 + 2 * pth;
-                sv += r[0];
-                sw += r[1];
+                const float* r = red + (k * a.n_g + g) * 2 * NS;
+                sv += r[2 * pth];
+                sw += r[2 * pth + 1];
+                if (MC) sq += r[4 + pth];
             }
             const int64_t m = 2 * pr + pth;
             if (m < a.B) {
-                const float w10 = ws[(2 * pth) * W];
+                const float w10 = ws[(NS * pth) * W];
                 const float Ivdt = a.dt[g] * (a.xi + sv);
                 const float IsvdW = a.sdt[g] * fmaf(a.sqrt_xi, w10, sw);
                 a.ivb[(size_t)(a.g0 + g) * a.B + m] = make_float2(Ivdt, IsvdW);
+                if (MC) a.ivq[(size_t)(a.g0 + g) * a.B + m] = a.sdt[g] * fmaf(a.sqrt_xi, ws[(NS * pth + 2) * W], sq);
             }
         }
         __syncthreads();
@@ -409,11 +425,11 @@ int fft_log2_len(int N)
     return logL;
 }
 
-size_t fft_smem_bytes(int N, int n_g)
+size_t fft_smem_bytes(int N, int n_g, int ns)
 {
     const int L = 1 << fft_log2_len(N);
     const int Np = (N + 31) / 32 * 32;
-    return (size_t)fft_smem(L, Np, n_g).total;
+    return (size_t)fft_smem(L, Np, n_g, ns).total;
 }
 
 // spectrum G^ = FFT(Gamma zero-padded to L) / L, FP32; twiddles exp(-2 pi i t / L)
@@ -434,19 +450,25 @@ void fft_tables(const double* gamma, int N, int logL, float* spec, float* tw)
     }
 }
 
-template <int LOGL>
-static cudaError_t launch_fft_l(const MixedArgs& A, int sms, cudaStream_t st)
+template <int LOGL, bool MC>
+static cudaError_t launch_fft_lm(const MixedArgs& A, int sms, cudaStream_t st)
 {
-    const int smem = fft_smem(1 << LOGL, A.Np, A.n_g).total;
-    cudaError_t e = cudaFuncSetAttribute(k_mixed_fft<LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int smem = fft_smem(1 << LOGL, A.Np, A.n_g, MC ? 3 : 2).total;
+    cudaError_t e = cudaFuncSetAttribute(k_mixed_fft<LOGL, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_fft<LOGL>, fft_threads(LOGL), smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_fft<LOGL, MC>, fft_threads(LOGL), smem);
     if (per_sm < 1) per_sm = 1;
     const int64_t npairs = (A.B + 1) / 2;
     const int grid = (int)std::min<int64_t>(npairs, (int64_t)sms * per_sm);
-    k_mixed_fft<LOGL><<<grid, fft_threads(LOGL), smem, st>>>(A);
+    k_mixed_fft<LOGL, MC><<<grid, fft_threads(LOGL), smem, st>>>(A);
     return cudaGetLastError();
+}
+
+template <int LOGL>
+static cudaError_t launch_fft_l(const MixedArgs& A, int sms, cudaStream_t st)
+{
+    return A.ivq ? launch_fft_lm<LOGL, true>(A, sms, st) : launch_fft_lm<LOGL, false>(A, sms, st);
 }
 
 cudaError_t launch_mixed_fft(const MixedArgs& A, int sms, cudaStream_t st)

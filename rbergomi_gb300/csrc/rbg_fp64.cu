@@ -342,7 +342,9 @@ __global__ void k_finalize(const double* __restrict__ acc, int n_out, int64_t M,
 void launch_finalize(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,
                      int compute_iv, double* res, void* stream)
 {
-    const int threads = 128;
+    // one output (one warp) per block: the implied-vol search is FP64-bound,
+    // and GB300's FP64 pipe is per SM, so the outputs spread over the SMs
+    const int threads = 32;
     const int blocks = (int)(((int64_t)n_out * 32 + threads - 1) / threads);
     k_finalize<<<blocks, threads, 0, (cudaStream_t)stream>>>(acc, n_out, M, outs, Tvals, compute_iv, res);
     count_launch();
@@ -358,8 +360,7 @@ __global__ void k_implied_vol(int n, const double* price, const double* K, const
 
 void launch_implied_vol(int n, const double* price, const double* K, const double* T, double* iv, void* stream)
 {
-    const int blocks = (int)(((int64_t)n * 32 + 127) / 128);
-    k_implied_vol<<<blocks, 128, 0, (cudaStream_t)stream>>>(n, price, K, T, iv);
+    k_implied_vol<<<n, 32, 0, (cudaStream_t)stream>>>(n, price, K, T, iv);  // one warp (output) per block
     count_launch();
 }
 

@@ -17,8 +17,7 @@
 // Toeplitz structure.  Time steps are cut into K-chunks of 32.  Chunk c
 // multiplies the A tile W1[:, 32c, 32c+32) into output columns [32c, Np):
 //   D[:, 32c + j'] += sum_{k'<32} A_c[:, k'] * S[j'][k'],  S[j'][k'] = Gamma[j' - k'],
-// and S does not depend on c.  Its diagonal holds a1 instead of Gamma[0] = 0,
-// so the MMAs also add the hybrid scheme's near-field term a1 W1_j.  So one Np x 32 strip S (hi and lo halves,
+// and S does not depend on c.  So one Np x 32 strip S (hi and lo halves,
 // 64 KB at N = 512) stays resident in shared memory for the whole kernel,
 // loaded once by a bulk async copy; only A tiles stream.  Two-pass tiles
 // (below) use a narrow strip instead: the two K = 16 halves of a chunk read
@@ -303,18 +302,36 @@ __device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_
 // (rBergLib/rBergomiMT.cpp:598-602 with BlackScholes.cpp:16-21).  ITM strikes
 // go through put-call parity, (S - K) + put, so both wings are computed from
 // small tail probabilities that keep their relative accuracy.
+// The strike-independent part: conditional spot, log-spot, vol and 1 / vol.
+struct RtSpot {
+    float lnS, spot, rv, vol;
+    bool deg;  // zero conditional variance: the payoff is intrinsic
+};
+
+__device__ __forceinline__ RtSpot rt_spot_f32(float Ivdt, float IsvdW, float rho)
+{
+    RtSpot r;
+    const float v2 = (1.0f - rho * rho) * Ivdt;
+    r.lnS = -0.5f * rho * rho * Ivdt + rho * IsvdW;
+    r.spot = ex2_approx(1.4426950408889634f * r.lnS);
+    r.deg = !(v2 > 0.0f);
+    r.rv = rsqrt_approx(v2);
+    r.vol = v2 * r.rv;
+    return r;
+}
+
+__device__ __forceinline__ float rt_payoff_f32(const RtSpot& r, float K, float lnK)
+{
+    if (r.deg) return fmaxf(r.spot - K, 0.0f);
+    const float d1 = fmaf(r.lnS - lnK, r.rv, 0.5f * r.vol);
+    const float d2 = d1 - r.vol;
+    if (r.spot > K) return (r.spot - K) + (K * phi_f32(-d2) - r.spot * phi_f32(-d1));
+    return r.spot * phi_f32(d1) - K * phi_f32(d2);
+}
+
 __device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rho, float K, float lnK)
 {
-    const float v2 = (1.0f - rho * rho) * Ivdt;
-    const float lnS = -0.5f * rho * rho * Ivdt + rho * IsvdW;
-    const float spot = ex2_approx(1.4426950408889634f * lnS);
-    if (!(v2 > 0.0f)) return fmaxf(spot - K, 0.0f);
-    const float rv = rsqrt_approx(v2);
-    const float vol = v2 * rv;
-    const float d1 = fmaf(lnS - lnK, rv, 0.5f * vol);
-    const float d2 = d1 - vol;
-    if (spot > K) return (spot - K) + (K * phi_f32(-d2) - spot * phi_f32(-d1));
-    return spot * phi_f32(d1) - K * phi_f32(d2);
+    return rt_payoff_f32(rt_spot_f32(Ivdt, IsvdW, rho), K, lnK);
 }
 
 // One producer thread's share of a chunk: Philox -> FP32 normals for steps
@@ -587,7 +604,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj) {
                         const float w1 = w1v[jj];
-                        x[jj] = fmaf(a.a2, w1pv[jj], x[jj]);  // Y2 + a1 W1 came out of the MMA
+                        x[jj] = x[jj] + a.a1 * w1 + a.a2 * w1pv[jj];
                         if (jj > 0) wn[jj - 1] = w1;
                         if (jj == 0 && j0 == 0 && c == 0) {
                             w10_s[p] = w1;
@@ -835,7 +852,8 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
         if (m >= B) break;
         int cur = -1;
         float2 iv = make_float2(0.f, 0.f);
-        float ip = 0.f;
+        float ip = 0.f, rho_cur = 2.0f;
+        RtSpot sp{};
 #pragma unroll
         for (int q = 0; q < kOPB32; ++q) {
             if (vg[q] < 0) continue;
@@ -843,8 +861,16 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
                 cur = vg[q];
                 iv = ivb[(size_t)cur * B + m];
                 if (MC) ip = ivq[(size_t)cur * B + m];
+                rho_cur = 2.0f;
             }
-            const float x = MC ? mc_payoff_f32(iv.x, iv.y, ip, rho[q], K[q]) : rt_payoff_f32(iv.x, iv.y, rho[q], K[q], lnK[q]);
+            float x;
+            if (MC) {
+                x = mc_payoff_f32(iv.x, iv.y, ip, rho[q], K[q]);
+            } else {
+                // strikes of one (group, rho) share the conditional spot and vol
+                if (rho[q] != rho_cur) { rho_cur = rho[q]; sp = rt_spot_f32(iv.x, iv.y, rho_cur); }
+                x = rt_payoff_f32(sp, K[q], lnK[q]);
+            }
             s1[q] += x;
             s2[q] = fmaf(x, x, s2[q]);
         }
@@ -914,12 +940,15 @@ float from_f16(uint16_t u)
 }
 
 // The strip image the MMA descriptors expect, hi/lo 16-bit halves:
-//   wide   S[j][k] = Gamma[j - k] (a1 at j = k), rows j in [0, Np), SW64 K-major: row j at
+//   wide   S[j][k] = Gamma[j - k], rows j in [0, Np), SW64 K-major: row j at
 //          j * 64 bytes, 16-byte chunk (k / 8) XOR ((j / 2) mod 4);
-//   narrow P[r][k] = Gamma[r - 16 - k] (a1 at r - 16 = k), rows r in [0, Np + 16), SW32 K-major:
+//   narrow P[r][k] = Gamma[r - 16 - k], rows r in [0, Np + 16), SW32 K-major:
 //          row r at r * 32 bytes, 16-byte chunk (k / 8) XOR ((r / 4) mod 2);
 // zero where the Gamma index is negative or >= N.
-void build_strip(const double* gamma, int N, int Np, int bf16, double a1, unsigned char* img)
+// The near-field term a1 W1_j stays out of the split products: the epilogue
+// adds it from the FP32 normal, which keeps X an order of magnitude closer
+// to FP64 than folding a1 into the strip's diagonal (measured; no speed-up).
+void build_strip(const double* gamma, int N, int Np, int bf16, unsigned char* img)
 {
     const size_t half = (size_t)strip_bytes(Np) / 2;
     std::memset(img, 0, 2 * half);
@@ -928,9 +957,7 @@ void build_strip(const double* gamma, int N, int Np, int bf16, double a1, unsign
     for (int r = 0; r < rows; ++r)
         for (int k = 0; k < kw; ++k) {
             const int d = r - lead - k;
-            // the diagonal carries a1 (Gamma[0] = 0 otherwise), so the MMA also adds the
-            // near-field term a1 W1_j to column j
-            const double gv = (d == 0) ? a1 : (d > 0 && d < N) ? gamma[d] : 0.0;
+            const double gv = (d >= 0 && d < N) ? gamma[d] : 0.0;
             uint16_t hi, lo;
             if (bf16) {
                 hi = to_bf16((float)gv);
@@ -991,10 +1018,6 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     if (backend == RBG_CONV_AUTO) backend = (Np <= kMaxNp) ? RBG_CONV_GEMM : RBG_CONV_FFT;
     if (backend == RBG_CONV_GEMM && Np > kMaxNp) {
         err = "mixed GEMM form supports N <= 1024 (two passes over 128 x 512 FP32 TMEM columns); use the FFT backend";
-        return RBG_ERR_UNSUPPORTED;
-    }
-    if (mc && backend != RBG_CONV_GEMM) {
-        err = "mixed plain Monte Carlo runs on the GEMM backend (N <= 1024)";
         return RBG_ERR_UNSUPPORTED;
     }
     if (backend == RBG_CONV_FFT && N > 4096) {
@@ -1060,7 +1083,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             } else {
                 A.logL = fft_log2_len(N);
                 A.L = 1 << A.logL;
-                if (fft_smem_bytes(N, ng) > (size_t)optin) {
+                if (fft_smem_bytes(N, ng, ns) > (size_t)optin) {
                     err = "mixed FFT kernel shared memory does not fit";
                     return RBG_ERR_UNSUPPORTED;
                 }
@@ -1114,7 +1137,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         const MixedArgs& A = r.args;
         const int vol = plan.vgs[A.g0].vol;
         if (backend == RBG_CONV_GEMM)
-            build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, bf16, plan.vols[vol].a1, ws.data() + r.off_strip);
+            build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, bf16, ws.data() + r.off_strip);
         else
             fft_tables(plan.gamma.data() + (size_t)vol * N, N, A.logL, (float*)(ws.data() + r.off_spec),
                        (float*)(ws.data() + job.off_tw));

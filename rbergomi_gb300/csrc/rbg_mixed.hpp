@@ -82,7 +82,7 @@ int mixed_part_rows(const MixedJob& job, int64_t B);
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
 // FFT backend (rbg_fft.cu)
 int fft_log2_len(int N);
-size_t fft_smem_bytes(int N, int n_g);
+size_t fft_smem_bytes(int N, int n_g, int ns = 2);
 void fft_tables(const double* gamma, int N, int logL, float* spec, float* tw);
 cudaError_t launch_mixed_fft(const MixedArgs& A, int sms, cudaStream_t st);
 

@@ -100,9 +100,18 @@ def test_mc_mixed_vs_fp64_identical_normals(R, N):
     assert np.all(np.abs(ms / fs - 1) < 1e-3)
 
 
-def test_mc_mixed_rejects_fft_range(R):
-    with pytest.raises(R.RbgError):
-        R.price_mc(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 2048, 256, precision=R.MIXED)
+@pytest.mark.parametrize("N,conv", [(1500, "auto"), (700, "fft")])
+def test_mc_mixed_fft_backend_vs_fp64(R, N, conv):
+    """Mixed plain MC on the batched-FFT backend (automatic above N = 1024)."""
+    xi, H, eta, rho = 0.05, [0.1], [1.5], [-0.7]
+    T, K = [2.0, 2.0], [0.9, 1.2]
+    M = 1 << 13
+    cv = R.CONV_FFT if conv == "fft" else R.CONV_AUTO
+    mp, ms, _ = R.price_mc(xi, H, eta, rho, T, K, N, M, seed=4, precision=R.MIXED, conv=cv)
+    fp, fs, _ = R.price_mc(xi, H, eta, rho, T, K, N, M, seed=4, normals=R.NORMALS_F32)
+    err = np.abs(mp - fp)
+    assert np.all(err <= 1e-4 * fp)
+    assert np.all(err < 0.2 * fs)
 
 
 def test_computeIV_tensor_mixed_env(R, monkeypatch):

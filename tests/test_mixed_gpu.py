@@ -30,9 +30,7 @@ GRID = dict(xi=0.04, H=[0.05, 0.1, 0.1, 0.3, 0.1], eta=[1.0, 1.5, 1.5, 2.5, 1.5]
 
 def fp64_x(W1, W1p, H, N):
     """X_j = sum_{k<j} W1_k Gamma_{j-k} + a1 W1_j + a2 W1perp_j in FP64 and
-    the magnitude of the split-product terms, sum_{k<j} |W1_k Gamma_{j-k}| +
-    a1 |W1_j| (the GEMM's strip carries a1 on its diagonal)
-    (rBergLib/rBergomiMT.cpp:83-109)."""
+    the magnitude sum_{k<j} |W1_k Gamma_{j-k}| (rBergLib/rBergomiMT.cpp:83-109)."""
     from oracle import oracle as O
     G = O.gamma(H, N)
     s2H = np.sqrt(2 * H)
@@ -44,7 +42,7 @@ def fp64_x(W1, W1p, H, N):
     for k in range(N):
         Y[:, k + 1:] += W1[:, k:k + 1] * G[None, 1:N - k]
         A[:, k + 1:] += np.abs(W1[:, k:k + 1] * G[None, 1:N - k])
-    return Y + a1 * W1[:, :N] + a2 * W1p[:, :N], A + a1 * np.abs(W1[:, :N])
+    return Y + a1 * W1[:, :N] + a2 * W1p[:, :N], A
 
 
 @pytest.mark.parametrize("N,M", [(100, 300), (512, 256), (33, 129), (700, 200), (1024, 130)])
