@@ -852,8 +852,7 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
         if (m >= B) break;
         int cur = -1;
         float2 iv = make_float2(0.f, 0.f);
-        float ip = 0.f, rho_cur = 2.0f;
-        RtSpot sp{};
+        float ip = 0.f;
 #pragma unroll
         for (int q = 0; q < kOPB32; ++q) {
             if (vg[q] < 0) continue;
@@ -861,16 +860,11 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
                 cur = vg[q];
                 iv = ivb[(size_t)cur * B + m];
                 if (MC) ip = ivq[(size_t)cur * B + m];
-                rho_cur = 2.0f;
             }
-            float x;
-            if (MC) {
-                x = mc_payoff_f32(iv.x, iv.y, ip, rho[q], K[q]);
-            } else {
-                // strikes of one (group, rho) share the conditional spot and vol
-                if (rho[q] != rho_cur) { rho_cur = rho[q]; sp = rt_spot_f32(iv.x, iv.y, rho_cur); }
-                x = rt_payoff_f32(sp, K[q], lnK[q]);
-            }
+            // every output's payoff independently: the eight chains overlap (sharing the
+            // strike-independent terms across outputs measured slower)
+            const float x = MC ? mc_payoff_f32(iv.x, iv.y, ip, rho[q], K[q])
+                               : rt_payoff_f32(iv.x, iv.y, rho[q], K[q], lnK[q]);
             s1[q] += x;
             s2[q] = fmaf(x, x, s2[q]);
         }
