@@ -156,6 +156,36 @@ typedef struct rbg_unordered {
  * equal H share one Volterra pass and equal (H, T, eta) one variance path. */
 int rbg_price_rt_unordered(const rbg_unordered* u, const rbg_options* o, double* price, double* stat, double* iv);
 
+/* Romano-Touzi prices with the control variate of McCrickerd and Pakkanen
+ * and antithetic paths, as ML_console_ST's RBergomi::ComputeIVRTVarRed does
+ * it (ML_console_ST/RBergomi.cpp:218-306, 478-540), over an unordered list
+ * with one xi per tuple and that code's (i dt)^{2H} compensator:
+ *   pilot: M_control paths give Q_i = max 2 Ivdt and alpha_i = -cov(X, Y) /
+ *   var(Y), X the RT payoff, Y = BS(S, K, 1, sqrt(rho^2 (Q - Ivdt)));
+ *   main: M paths, each the mean of X + alpha Y at W and at -W (Q_max where
+ *   Q <= Ivdt), then price -= alpha E[Y] in closed form.
+ * FP64.  Pilot normals come from Philox paths 2^62 + path_offset + m, main
+ * normals from paths path_offset + m. */
+typedef struct rbg_cv_params {
+    const double* xi;
+    const double* H;
+    const double* eta;
+    const double* rho;
+    const double* T;
+    const double* K;
+    long size;
+    int N;
+    int64_t M;          /* main paths (each also priced antithetically) */
+    int64_t M_control;  /* pilot paths (the reference uses 10000) */
+    double Q_max;       /* the reference uses 10000 */
+} rbg_cv_params;
+
+int rbg_price_rt_cv(const rbg_cv_params* p, const rbg_options* o, double* price, double* stat, double* iv);
+/* Same on caller normals (host pointers): Zc holds 2*N*M_control doubles for
+ * the pilot, Z 2*N*M for the main paths, W1 then W1perp per path. */
+int rbg_price_rt_cv_normals(const rbg_cv_params* p, const double* Zc, const double* Z, double* price, double* stat,
+                            double* iv);
+
 /* Same, with the raw sums instead of finished moments: sum[i] = sum_m x,
  * sum2[i] = sum_m x^2 over this call's paths (for merging shards/replicas). */
 int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, double* sum2);

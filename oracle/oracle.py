@@ -20,6 +20,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "librbg_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "librbergomi_ref.so")
+ML_REF_SO = os.path.join(HERE, "_ref", "libml_ref.so")
 REF_SRC_DIR = "/root/reference"
 
 _dp = C.POINTER(C.c_double)
@@ -65,12 +66,60 @@ def lib():
                                            C.c_int64, C.c_uint64, C.c_int, _dp, _dp, _dp, _dp]
         L.rbgo_price_rt_philox.restype = C.c_int
         L.rbgo_max_threads.restype = C.c_int
+        L.rbgo_price_rt_cv.argtypes = [C.c_long] + [_dp] * 6 + [C.c_int, C.c_int64, _dp, C.c_int64, _dp,
+                                                                  C.c_double, C.c_int, _dp, _dp, _dp, _dp,
+                                                                  C.POINTER(C.c_int64)]
+        L.rbgo_price_rt_cv.restype = C.c_int
         _lib = L
     return _lib
 
 
 def ref_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+def price_rt_cv(xi, H, eta, rho, T, K, Zc, Z, Qmax=10000.0, nthreads: int = 0):
+    """The control-variate Romano-Touzi estimator (ML_console_ST) on the
+    pilot normals Zc [Mc, 2, N] and main normals Z [M, 2, N]: per tuple
+    (price, stat, alpha, Q, exception count)."""
+    arrs = [np.ascontiguousarray(np.atleast_1d(np.asarray(a, dtype=np.float64))) for a in (xi, H, eta, rho, T, K)]
+    n = len(arrs[0])
+    Zc = np.ascontiguousarray(Zc, dtype=np.float64)
+    Z = np.ascontiguousarray(Z, dtype=np.float64)
+    Mc, two, N = Zc.shape
+    M = Z.shape[0]
+    price, stat, alpha, Q = (np.empty(n) for _ in range(4))
+    cnt = np.empty(n, dtype=np.int64)
+    rc = lib().rbgo_price_rt_cv(n, *[a.ctypes.data_as(_dp) for a in arrs], N, Mc, Zc.ctypes.data_as(_dp), M,
+                                Z.ctypes.data_as(_dp), float(Qmax), nthreads, price.ctypes.data_as(_dp),
+                                stat.ctypes.data_as(_dp), alpha.ctypes.data_as(_dp), Q.ctypes.data_as(_dp),
+                                cnt.ctypes.data_as(C.POINTER(C.c_int64)))
+    if rc:
+        raise MemoryError("oracle allocation failed")
+    return price, stat, alpha, Q, cnt
+
+
+def ml_ref_available() -> bool:
+    return os.path.exists(ML_REF_SO)
+
+
+def ml_ref_price_rt_cv(xi, H, eta, rho, T, K, N, M, Mc, seed):
+    """ComputeIVRTVarRed of the compiled reference (ML_console_ST) with a
+    Mc-path pilot: (price, stat, iv) per tuple, and the normals it drew,
+    pilot [Mc, 2, N] and main [M, 2, N]."""
+    R = C.CDLL(ML_REF_SO)
+    R.mlglue_price_rt_varred.argtypes = [_dp] * 6 + [C.c_long, C.c_int, C.c_long, C.c_long, _u64p, C.c_int,
+                                                     _dp, _dp, _dp]
+    R.mlglue_normals.argtypes = [_u64p, C.c_int, C.c_long, _dp]
+    arrs = [np.ascontiguousarray(np.atleast_1d(np.asarray(a, dtype=np.float64))) for a in (xi, H, eta, rho, T, K)]
+    n = len(arrs[0])
+    price, stat, iv = np.empty(n), np.empty(n), np.empty(n)
+    sd = (C.c_uint64 * len(seed))(*[int(x) for x in seed])
+    R.mlglue_price_rt_varred(*[a.ctypes.data_as(_dp) for a in arrs], n, N, M, Mc, sd, len(seed),
+                             price.ctypes.data_as(_dp), stat.ctypes.data_as(_dp), iv.ctypes.data_as(_dp))
+    Zall = np.empty((Mc + M, 2, N))
+    R.mlglue_normals(sd, len(seed), (Mc + M) * 2 * N, Zall.ctypes.data_as(_dp))
+    return price, stat, iv, Zall[:Mc], Zall[Mc:]
 
 
 def ref():

@@ -439,3 +439,161 @@ int rbgo_max_threads(void)
     return 1;
 #endif
 }
+
+/* ---------------------------------------------------------------------------
+ * Romano-Touzi estimator with the control variate of McCrickerd & Pakkanen
+ * and antithetic paths, as ML_console_ST implements it for an unordered
+ * parameter list (xi, H, eta, rho, T, K per tuple):
+ *   computeIvdtIsvdW         ML_console_ST/RBergomi.cpp:464-476, with updateV's
+ *                            (i dt)^{2H} compensator (:365-372; rBergLib uses i-1)
+ *   estimateControlVariate   :493-540 -- pilot paths: Q_i = max_m 2 Ivdt_im,
+ *                            X = BS(S, K, 1, sqrt((1-rho^2) Ivdt)),
+ *                            Y = BS(S, K, 1, sqrt(rho^2 (Q - Ivdt))),
+ *                            alpha_i = -cov(X, Y) / cov(Y, Y) (aux.h:206-220)
+ *   ComputePriceRTVarRed     :218-289 -- per main path the mean of the payoff
+ *                            X + alpha Y at W and at -W; Y takes Qmax where
+ *                            Q <= Ivdt (counted, over both halves, and
+ *                            divided by M); price -= alpha ((1 - p) BS(1, K, 1,
+ *                            sqrt(rho^2 Q)) + p BS(1, K, 1, sqrt(rho^2 Qmax)))
+ * Normals: Zc [Mc][2][N] pilot, Z [M][2][N] main.  Outputs per tuple: the
+ * adjusted price, stat (of the unadjusted payoffs, as the reference), alpha,
+ * Q and the exception count.
+ * ------------------------------------------------------------------------- */
+static void ivdt_isvdw_ml(double xi, double H, double eta, double T, int N, const double* W1,
+                          const double* W1perp, const double* G, double sgn, double* buf, double* Ivdt,
+                          double* IsvdW)
+{
+    double *w1 = buf, *w1p = buf + N, *Wt = buf + 2 * N, *Y2 = buf + 3 * N, *v = buf + 4 * N;
+    for (int j = 0; j < N; ++j) { w1[j] = sgn * W1[j]; w1p[j] = sgn * W1perp[j]; }
+    wtilde(Wt, w1, w1p, G, H, N, Y2);
+    const double dt = T / N, sdt = sqrt(dt), tH = pow(T, H);
+    v[0] = xi;
+    for (int i = 1; i < N; ++i)
+        v[i] = xi * exp(eta * (tH * Wt[i - 1]) - 0.5 * eta * eta * pow(i * dt, 2 * H));
+    double a = 0.0, b = 0.0;
+    for (int j = 0; j < N; ++j) a += v[j];
+    for (int j = 0; j < N; ++j) b += sqrt(v[j]) * sdt * w1[j];
+    *Ivdt = dt * a;
+    *IsvdW = b;
+}
+
+static double rt_spot(double rho, double Ivdt, double IsvdW)
+{
+    return exp(-0.5 * rho * rho * Ivdt + rho * IsvdW);
+}
+
+int rbgo_price_rt_cv(long n, const double* xi, const double* H, const double* eta, const double* rho,
+                     const double* T, const double* K, int N, int64_t Mc, const double* Zc, int64_t M,
+                     const double* Z, double Qmax, int nthreads, double* price, double* stat, double* alpha,
+                     double* Q, int64_t* count)
+{
+    double* G = (double*)malloc(sizeof(double) * (size_t)N * (size_t)n);
+    double* piv = (double*)malloc(sizeof(double) * 2 * (size_t)n * (size_t)Mc);
+    if (!G || !piv) { free(G); free(piv); return -1; }
+    for (long i = 0; i < n; ++i) rbgo_gamma(H[i], N, G + (size_t)i * N);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    int fail = 0;
+    /* pilot integrals */
+#pragma omp parallel
+    {
+        double* buf = (double*)malloc(sizeof(double) * 5 * (size_t)N);
+        if (!buf) {
+#pragma omp atomic write
+            fail = 1;
+        } else {
+#pragma omp for schedule(static)
+            for (int64_t m = 0; m < Mc; ++m)
+                for (long i = 0; i < n; ++i) {
+                    const double* z = Zc + (size_t)m * 2 * N;
+                    ivdt_isvdw_ml(xi[i], H[i], eta[i], T[i], N, z, z + N, G + (size_t)i * N, 1.0, buf,
+                                  &piv[((size_t)i * Mc + m) * 2], &piv[((size_t)i * Mc + m) * 2 + 1]);
+                }
+            free(buf);
+        }
+    }
+    if (fail) { free(G); free(piv); return -1; }
+    for (long i = 0; i < n; ++i) {
+        const double* pv = piv + (size_t)i * Mc * 2;
+        double q = 0.0;
+        for (int64_t m = 0; m < Mc; ++m) q = fmax(q, 2 * pv[2 * m]);
+        Q[i] = q;
+        double r = rho[i], mx = 0.0, my = 0.0;
+        double* X = (double*)malloc(sizeof(double) * 2 * (size_t)Mc);
+        if (!X) { free(G); free(piv); return -1; }
+        double* Y = X + Mc;
+        for (int64_t m = 0; m < Mc; ++m) {
+            const double iv = pv[2 * m], iw = pv[2 * m + 1], s = rt_spot(r, iv, iw);
+            X[m] = rbgo_bs_call(s, K[i], 1.0, sqrt((1.0 - r * r) * iv));
+            Y[m] = rbgo_bs_call(s, K[i], 1.0, sqrt(r * r * (q - iv)));
+            mx += X[m];
+            my += Y[m];
+        }
+        mx /= (double)Mc;
+        my /= (double)Mc;
+        double cxy = 0.0, cyy = 0.0;
+        for (int64_t m = 0; m < Mc; ++m) {
+            cxy += (X[m] - mx) * (Y[m] - my);
+            cyy += (Y[m] - my) * (Y[m] - my);
+        }
+        alpha[i] = -(cxy / (double)(Mc - 1)) / (cyy / (double)(Mc - 1));
+        free(X);
+    }
+    free(piv);
+    /* main paths, antithetic pairs */
+    double* s1 = (double*)calloc((size_t)n, sizeof(double));
+    double* s2 = (double*)calloc((size_t)n, sizeof(double));
+    int64_t* cnt = (int64_t*)calloc((size_t)n, sizeof(int64_t));
+    if (!s1 || !s2 || !cnt) { free(G); free(s1); free(s2); free(cnt); return -1; }
+#pragma omp parallel
+    {
+        double* buf = (double*)malloc(sizeof(double) * 5 * (size_t)N);
+        double* l1 = (double*)calloc((size_t)n, sizeof(double));
+        double* l2 = (double*)calloc((size_t)n, sizeof(double));
+        int64_t* lc = (int64_t*)calloc((size_t)n, sizeof(int64_t));
+        if (!buf || !l1 || !l2 || !lc) {
+#pragma omp atomic write
+            fail = 1;
+        } else {
+#pragma omp for schedule(static)
+            for (int64_t m = 0; m < M; ++m) {
+                const double* z = Z + (size_t)m * 2 * N;
+                for (long i = 0; i < n; ++i) {
+                    double pay = 0.0;
+                    for (int h = 0; h < 2; ++h) {
+                        double iv, iw;
+                        ivdt_isvdw_ml(xi[i], H[i], eta[i], T[i], N, z, z + N, G + (size_t)i * N, h ? -1.0 : 1.0, buf,
+                                      &iv, &iw);
+                        const double r = rho[i], s = rt_spot(r, iv, iw);
+                        const double x = rbgo_bs_call(s, K[i], 1.0, sqrt((1.0 - r * r) * iv));
+                        const double vy = Q[i] > iv ? sqrt(r * r * (Q[i] - iv)) : sqrt(r * r * (Qmax - iv));
+                        if (Q[i] <= iv) lc[i]++;
+                        pay += 0.5 * (x + alpha[i] * rbgo_bs_call(s, K[i], 1.0, vy));
+                    }
+                    l1[i] += pay;
+                    l2[i] += pay * pay;
+                }
+            }
+#pragma omp critical
+            for (long i = 0; i < n; ++i) { s1[i] += l1[i]; s2[i] += l2[i]; cnt[i] += lc[i]; }
+        }
+        free(buf); free(l1); free(l2); free(lc);
+    }
+    if (!fail) {
+        for (long i = 0; i < n; ++i) {
+            const double p = s1[i] * (1.0 / (double)M);
+            const double var = 1.0 * (s2[i] * (1.0 / (double)M)) + -1.0 * (p * p);
+            stat[i] = sqrt(var) * (1.0 / sqrt((double)M));
+            const double pex = (double)cnt[i] / (double)M, r = rho[i];
+            const double adj = (1.0 - pex) * rbgo_bs_call(1.0, K[i], 1.0, sqrt(r * r * Q[i])) +
+                               pex * rbgo_bs_call(1.0, K[i], 1.0, sqrt(r * r * Qmax));
+            price[i] = p - alpha[i] * adj;
+            count[i] = cnt[i];
+        }
+    }
+    free(G); free(s1); free(s2); free(cnt);
+    return fail ? -1 : 0;
+}

@@ -1,6 +1,7 @@
-// roots.hpp -- from-scratch stand-in for the two Boost.Math root-finding names
-// the reference's BlackScholes.cpp uses (eps_tolerance, bracket_and_solve_root)
-// plus boost::uintmax_t.  TEST INFRASTRUCTURE for oracle/build_ref.sh only.
+// roots.hpp -- from-scratch stand-in for the Boost.Math root-finding names the
+// reference's BlackScholes.cpp files use (eps_tolerance, bracket_and_solve_root,
+// newton_raphson_iterate) plus boost::uintmax_t.  TEST INFRASTRUCTURE for the
+// oracle's reference build only.
 //
 // Follows Boost's documented contract: bracket_and_solve_root(f, guess, factor,
 // rising, tol, max_iter) walks guess*factor^k (or guess/factor^k) until f
@@ -14,6 +15,7 @@
 #include <cstdint>
 #include <limits>
 #include <stdexcept>
+#include <tuple>
 #include <utility>
 
 namespace boost {
@@ -68,6 +70,46 @@ std::pair<T, T> bracket_and_solve_root(F f, const T& guess, T factor, bool risin
     }
     max_iter = used;
     return std::make_pair(a, b);
+}
+
+// newton_raphson_iterate(f, guess, min, max, digits, max_iter), Boost's
+// documented contract: f returns (f(x), f'(x)); Newton steps
+// x -= f(x) / f'(x); a step that would leave [min, max] (or a zero
+// derivative) is replaced by bisection towards the violated bound; the
+// iteration stops once the step is below |x| 2^(1-digits) or after max_iter
+// evaluations, and returns x.
+template <class F, class T>
+T newton_raphson_iterate(F f, T guess, T min, T max, int digits, boost::uintmax_t& max_iter)
+{
+    const T factor = static_cast<T>(std::ldexp(1.0, 1 - digits));
+    T x = guess, delta = (std::numeric_limits<T>::max)();
+    boost::uintmax_t count = max_iter, used = 0;
+    while (used < count) {
+        const auto r = f(x);
+        ++used;
+        const T f0 = std::get<0>(r), f1 = std::get<1>(r);
+        if (f0 == 0) break;
+        T next;
+        if (f1 == 0) {
+            next = (f0 > 0) == (delta > 0) ? (x + min) / 2 : (x + max) / 2;
+        } else {
+            next = x - f0 / f1;
+            if (next < min) next = (x + min) / 2;
+            if (next > max) next = (x + max) / 2;
+        }
+        delta = x - next;
+        x = next;
+        if (std::fabs(delta) <= std::fabs(x) * factor) break;
+    }
+    max_iter = used;
+    return x;
+}
+
+template <class F, class T>
+T newton_raphson_iterate(F f, T guess, T min, T max, int digits)
+{
+    boost::uintmax_t it = (std::numeric_limits<boost::uintmax_t>::max)();
+    return newton_raphson_iterate(f, guess, min, max, digits, it);
 }
 
 }  // namespace tools

@@ -40,6 +40,11 @@ class RbgUnordered(C.Structure):
                 ("size", C.c_long), ("N", C.c_int), ("M", C.c_int64)]
 
 
+class RbgCvParams(C.Structure):
+    _fields_ = [("xi", _dp), ("H", _dp), ("eta", _dp), ("rho", _dp), ("T", _dp), ("K", _dp), ("size", C.c_long),
+                ("N", C.c_int), ("M", C.c_int64), ("M_control", C.c_int64), ("Q_max", C.c_double)]
+
+
 class RbgOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("conv", C.c_int), ("normals", C.c_int), ("split", C.c_int),
                 ("compute_iv", C.c_int), ("seed", C.c_uint64), ("path_offset", C.c_int64),
@@ -60,7 +65,7 @@ EXPORTS = [
     "rbg_debug_mixed_profile", "rbg_server_default_config", "rbg_server_create", "rbg_server_submit",
     "rbg_server_poll", "rbg_server_wait", "rbg_server_get_stats", "rbg_server_destroy", "rbg_server_last_error",
     "rbg_price_rt_unordered", "computeIV_tensor", "rbg_price_mc", "rbg_payoffs_mc", "rbg_generate_normals_streams",
-    "rbg_plan_info_mc", "rbg_plan_info_unordered",
+    "rbg_plan_info_mc", "rbg_plan_info_unordered", "rbg_price_rt_cv", "rbg_price_rt_cv_normals",
 ]
 
 STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4
@@ -244,6 +249,43 @@ def price_rt_unordered(xi, H, eta, rho, T, K, N, M, **opts):
     price, stat, iv = np.empty(n), np.empty(n), np.empty(n)
     _check(lib().rbg_price_rt_unordered(C.byref(u), C.byref(o), price.ctypes.data_as(_dp),
                                         stat.ctypes.data_as(_dp), iv.ctypes.data_as(_dp)))
+    return price, stat, iv
+
+
+def _cv_params(xi, H, eta, rho, T, K, N, M, M_control, Q_max):
+    arrs = [_arr(x) for x in (H, eta, rho, T, K)]
+    n = len(arrs[0])
+    xis = np.full(n, float(xi)) if np.ndim(xi) == 0 else _arr(xi)
+    if any(len(x) != n for x in arrs + [xis]):
+        raise ValueError("xi, H, eta, rho, T, K must have the same length")
+    p = RbgCvParams(xis.ctypes.data_as(_dp), *[x.ctypes.data_as(_dp) for x in arrs], n, int(N), int(M),
+                    int(M_control), float(Q_max))
+    return p, n, (xis, arrs)
+
+
+def price_rt_cv(xi, H, eta, rho, T, K, N, M, M_control=10000, Q_max=10000.0, **opts):
+    """Romano-Touzi with the McCrickerd-Pakkanen control variate and
+    antithetic paths (ML_console_ST's ComputeIVRTVarRed), one tuple per
+    output, xi per tuple (scalar or array), FP64: (price, stat, iv)."""
+    p, n, keep = _cv_params(xi, H, eta, rho, T, K, N, M, M_control, Q_max)
+    o = options(**opts)
+    price, stat, iv = np.empty(n), np.empty(n), np.empty(n)
+    _check(lib().rbg_price_rt_cv(C.byref(p), C.byref(o), price.ctypes.data_as(_dp), stat.ctypes.data_as(_dp),
+                                 iv.ctypes.data_as(_dp)))
+    return price, stat, iv
+
+
+def price_rt_cv_normals(xi, H, eta, rho, T, K, Zc, Z, Q_max=10000.0):
+    """The control-variate estimator on caller normals: pilot Zc [Mc, 2, N],
+    main Z [M, 2, N]."""
+    Zc = np.ascontiguousarray(Zc, dtype=np.float64)
+    Z = np.ascontiguousarray(Z, dtype=np.float64)
+    Mc, two, N = Zc.shape
+    p, n, keep = _cv_params(xi, H, eta, rho, T, K, N, Z.shape[0], Mc, Q_max)
+    price, stat, iv = np.empty(n), np.empty(n), np.empty(n)
+    _check(lib().rbg_price_rt_cv_normals(C.byref(p), Zc.ctypes.data_as(_dp), Z.ctypes.data_as(_dp),
+                                         price.ctypes.data_as(_dp), stat.ctypes.data_as(_dp),
+                                         iv.ctypes.data_as(_dp)))
     return price, stat, iv
 
 

@@ -136,7 +136,7 @@ struct Ctx {
     int dev = -1;
     cudaStream_t stream = nullptr;
     std::mutex mu;
-    DevBuf z, ivb, ivp, part, acc, tabs, res, pay, mixed_ws;
+    DevBuf z, ivb, ivp, part, acc, tabs, res, pay, mixed_ws, cv;
     // host images of what `tabs` and `mixed_ws` hold, so that a call with
     // the same tables (a calibration loop, a benchmark) uploads nothing
     std::vector<unsigned char> tabs_img, mixed_img;
@@ -184,7 +184,7 @@ static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts
     std::vector<VGDev> vgs(ng);
     for (int g = 0; g < ng; ++g) {
         const VGroup& G = plan.vgs[g];
-        vgs[g] = VGDev{G.scale, G.eta, G.dt, G.sdt, plan.xi, G.nsteps, G.vol};
+        vgs[g] = VGDev{G.scale, G.eta, G.dt, G.sdt, G.xi, G.nsteps, G.vol};
     }
     std::vector<OutDev> outs(no);
     std::vector<double> Tv(no);
@@ -397,6 +397,91 @@ static int price_any(const rbg_params* p, const rbg_options* o, std::vector<doub
     return price_plan(plan, p->M, o, res, mc);
 }
 
+// Control-variate Romano-Touzi estimator (ML_console_ST), FP64.  Zc / Z: host
+// normals, or null for the Philox stream (pilot paths 2^62 + path_offset + m).
+static const int64_t kCvPilotPath0 = (int64_t)1 << 62;
+
+static int price_cv(Ctx& c, const Plan& plan, const rbg_cv_params& p, const rbg_options& o, const double* Zc,
+                    const double* Z, cudaStream_t st, double* host_res)
+{
+    TableSet ts;
+    int rc = upload_tables(c, plan, st, ts);
+    if (rc) return rc;
+    const int no = (int)plan.outs.size(), N = plan.N, ng = (int)plan.vgs.size();
+    const int64_t Mc = p.M_control, M = p.M;
+    const int64_t B = fp64_batch(plan, M, 4);  // normals plus two (Ivdt, IsvdW) sets per path
+    if (Mc > fp64_batch(plan, Mc, 2)) return fail(RBG_ERR_ARG, "M_control too large for one pilot batch");
+    const int64_t zpaths = std::max(B, Mc);
+    if ((rc = ensure(c.z, sizeof(double) * 2 * N * (size_t)zpaths, "normals"))) return rc;
+    if ((rc = ensure(c.ivb, sizeof(double) * 2 * ng * (size_t)zpaths, "variance sums"))) return rc;
+    if ((rc = ensure(c.ivp, sizeof(double) * 2 * ng * (size_t)B, "antithetic sums"))) return rc;
+    const size_t cv_bytes = sizeof(double) * (size_t)no * (2 * (size_t)Mc + 2) + sizeof(unsigned long long) * no;
+    if ((rc = ensure(c.cv, cv_bytes, "control-variate scratch"))) return rc;
+    double* alpha = c.cv.as<double>();
+    double* Q = alpha + no;
+    unsigned long long* count = (unsigned long long*)(Q + no);
+    double* xy = (double*)(count + no);
+    const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
+    const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+    if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
+    if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
+    if ((rc = ensure(c.res, sizeof(double) * 5 * no, "results"))) return rc;
+    // pilot: one batch of Mc paths
+    if (Zc) {
+        RBG_CUDA(cudaMemcpyAsync(c.z.p, Zc, sizeof(double) * 2 * N * Mc, cudaMemcpyHostToDevice, st));
+    } else {
+        launch_normals(o.seed, kCvPilotPath0 + o.path_offset, Mc, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st);
+    }
+    launch_path_fp64(ts.t, c.z.as<double>(), Mc, c.ivb.as<double>(), st);
+    launch_cv_pilot(ts.t, c.ivb.as<double>(), Mc, xy, alpha, Q, st);
+    RBG_CUDA(cudaMemsetAsync(count, 0, sizeof(unsigned long long) * no, st));
+    RBG_CUDA(cudaMemsetAsync(c.acc.p, 0, sizeof(double) * 4 * no, st));
+    // main paths, antithetic pairs
+    for (int64_t m0 = 0; m0 < M; m0 += B) {
+        const int64_t b = std::min(B, M - m0);
+        if (Z) {
+            RBG_CUDA(cudaMemcpyAsync(c.z.p, Z + (size_t)m0 * 2 * N, sizeof(double) * 2 * N * b, cudaMemcpyHostToDevice,
+                                     st));
+        } else {
+            launch_normals(o.seed, o.path_offset + m0, b, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st);
+        }
+        launch_path_fp64(ts.t, c.z.as<double>(), b, c.ivb.as<double>(), st, nullptr, c.ivp.as<double>());
+        const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
+        launch_payoff_sums_cv(ts.t, c.ivb.as<double>(), c.ivp.as<double>(), b, alpha, Q, p.Q_max, G,
+                              c.part.as<double>(), count, nchunks, st);
+        launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+        RBG_CUDA(cudaGetLastError());
+    }
+    launch_finalize_cv(c.acc.as<double>(), no, M, ts.t.outs, ts.Tvals, alpha, Q, count, p.Q_max, o.compute_iv,
+                       c.res.as<double>(), st);
+    RBG_CUDA(cudaGetLastError());
+    RBG_CUDA(cudaMemcpyAsync(host_res, c.res.p, sizeof(double) * 5 * no, cudaMemcpyDeviceToHost, st));
+    RBG_CUDA(cudaStreamSynchronize(st));
+    return RBG_OK;
+}
+
+static int price_cv_any(const rbg_cv_params* p, const rbg_options* o, const double* Zc, const double* Z,
+                        std::vector<double>& res)
+{
+    if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
+    if (!p->xi) return fail(RBG_ERR_ARG, "null xi array");
+    if (p->M_control < 2) return fail(RBG_ERR_ARG, "M_control must be >= 2");
+    if (o->precision != RBG_FP64) return fail(RBG_ERR_UNSUPPORTED, "the control-variate estimator runs in FP64");
+    g_h2d = g_d2h = 0;
+    rbg_unordered u{p->xi[0], p->H, p->eta, p->rho, p->T, p->K, p->size, p->N, p->M};
+    Plan plan;
+    std::string err;
+    if (p->size > 0 && !build_plan_unordered(u, plan, err, p->xi, 1)) return fail(RBG_ERR_ARG, err);
+    if (p->size <= 0) return fail(RBG_ERR_ARG, "size must be positive");
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
+    res.assign(5 * plan.outs.size(), 0.0);
+    return price_cv(*c, plan, *p, *o, Zc, Z, st, res.data());
+}
+
 static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payoff, int device_ptrs,
                               cudaStream_t user_stream, bool mc = false)
 {
@@ -489,6 +574,34 @@ int rbg_price_rt_unordered(const rbg_unordered* u, const rbg_options* o, double*
     if (!build_plan_unordered(*u, plan, err)) return fail(RBG_ERR_ARG, err);
     std::vector<double> res;
     int rc = price_plan(plan, u->M, o, res);
+    if (rc) return rc;
+    const size_t no = res.size() / 5;
+    if (price) std::memcpy(price, res.data(), no * sizeof(double));
+    if (stat) std::memcpy(stat, res.data() + no, no * sizeof(double));
+    if (iv) std::memcpy(iv, res.data() + 2 * no, no * sizeof(double));
+    return RBG_OK;
+}
+
+int rbg_price_rt_cv(const rbg_cv_params* p, const rbg_options* o, double* price, double* stat, double* iv)
+{
+    std::vector<double> res;
+    int rc = price_cv_any(p, o, nullptr, nullptr, res);
+    if (rc) return rc;
+    const size_t no = res.size() / 5;
+    if (price) std::memcpy(price, res.data(), no * sizeof(double));
+    if (stat) std::memcpy(stat, res.data() + no, no * sizeof(double));
+    if (iv) std::memcpy(iv, res.data() + 2 * no, no * sizeof(double));
+    return RBG_OK;
+}
+
+int rbg_price_rt_cv_normals(const rbg_cv_params* p, const double* Zc, const double* Z, double* price, double* stat,
+                            double* iv)
+{
+    if (!Zc || !Z) return fail(RBG_ERR_ARG, "null normals");
+    rbg_options o;
+    rbg_default_options(&o);
+    std::vector<double> res;
+    int rc = price_cv_any(p, &o, Zc, Z, res);
     if (rc) return rc;
     const size_t no = res.size() / 5;
     if (price) std::memcpy(price, res.data(), no * sizeof(double));
@@ -598,7 +711,7 @@ int rbg_release(void)
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     RBG_CUDA(cudaStreamSynchronize(c->stream));
-    for (DevBuf* b : {&c->z, &c->ivb, &c->ivp, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws})
+    for (DevBuf* b : {&c->z, &c->ivb, &c->ivp, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws, &c->cv})
         b->release();
     c->tabs_img.clear();
     c->mixed_img.clear();

@@ -71,9 +71,12 @@ void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, dou
 // One warp per path.  Shared memory: Gamma of the current pass (N doubles),
 // then per warp W1 (N) and X (N).  NS = 3 (plain MC) also sums
 // IsvdWp = sum sqrt(v) sdt Wperp into ivp.
-template <int NS>
+// ANTI (control-variate form): also the antithetic path -W1, -W1perp.  The
+// Volterra sum is linear, so its X is exactly -X; ivn[g][B] gets its
+// (Ivdt, IsvdW).
+template <int NS, bool ANTI>
 __global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t B, double2* __restrict__ ivb,
-                            double* __restrict__ ivp)
+                            double* __restrict__ ivp, double2* __restrict__ ivn)
 {
     extern __shared__ double sm[];
     const int N = t.N;
@@ -106,23 +109,33 @@ __global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t 
         for (int g = vol.vg_begin; g < vol.vg_end; ++g) {
             const VGDev vg = t.vgs[g];
             const double* comp = t.comp + (size_t)g * N;
-            double sv = 0.0, sw = 0.0, sp = 0.0;
+            double sv = 0.0, sw = 0.0, sp = 0.0, nv = 0.0, nw = 0.0;
             for (int j = lane; j < vg.nsteps; j += 32) {
                 const double vj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * X[j - 1]) - comp[j - 1]);
                 sv += vj;
                 const double sq = sqrt(vj) * vg.sdt;
                 sw += sq * W1s[j];
                 if (NS == 3) sp += sq * Wperp[j];
+                if (ANTI) {
+                    const double uj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * -X[j - 1]) - comp[j - 1]);
+                    nv += uj;
+                    nw += sqrt(uj) * vg.sdt * -W1s[j];
+                }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 sv += __shfl_xor_sync(0xffffffffu, sv, o);
                 sw += __shfl_xor_sync(0xffffffffu, sw, o);
                 if (NS == 3) sp += __shfl_xor_sync(0xffffffffu, sp, o);
+                if (ANTI) {
+                    nv += __shfl_xor_sync(0xffffffffu, nv, o);
+                    nw += __shfl_xor_sync(0xffffffffu, nw, o);
+                }
             }
             if (lane == 0) {
                 ivb[(size_t)g * B + m] = make_double2(vg.dt * sv, sw);
                 if (NS == 3) ivp[(size_t)g * B + m] = sp;
+                if (ANTI) ivn[(size_t)g * B + m] = make_double2(vg.dt * nv, nw);
             }
         }
         __syncwarp();
@@ -141,21 +154,27 @@ int path_fp64_warps(int N)
 
 size_t path_fp64_smem(int N, int warps) { return 8 * (size_t)N + (size_t)warps * 16 * N; }
 
-void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream, double* ivp)
+void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream, double* ivp,
+                      double* ivn)
 {
     const int warps = path_fp64_warps(t.N);
     const size_t smem = path_fp64_smem(t.N, warps);
     static size_t configured = 0;
     if (smem > configured) {
-        cudaFuncSetAttribute(k_path_fp64<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_path_fp64<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_path_fp64<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_path_fp64<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_path_fp64<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = smem;
     }
     const int64_t blocks = (B + warps - 1) / warps;
-    if (ivp)
-        k_path_fp64<3><<<(unsigned)blocks, warps * 32, smem, (cudaStream_t)stream>>>(t, Z, B, (double2*)ivb, ivp);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (ivn)
+        k_path_fp64<2, true><<<(unsigned)blocks, warps * 32, smem, st>>>(t, Z, B, (double2*)ivb, nullptr,
+                                                                         (double2*)ivn);
+    else if (ivp)
+        k_path_fp64<3, false><<<(unsigned)blocks, warps * 32, smem, st>>>(t, Z, B, (double2*)ivb, ivp, nullptr);
     else
-        k_path_fp64<2><<<(unsigned)blocks, warps * 32, smem, (cudaStream_t)stream>>>(t, Z, B, (double2*)ivb, ivp);
+        k_path_fp64<2, false><<<(unsigned)blocks, warps * 32, smem, st>>>(t, Z, B, (double2*)ivb, nullptr, nullptr);
     count_launch();
 }
 
@@ -393,6 +412,204 @@ void launch_payoff_store(const Fp64Tables& t, const double* ivb, int64_t B, int6
     else
         k_payoff_store<0><<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, B, stride,
                                                                              payoff, ivp);
+    count_launch();
+}
+
+// ------------------------------------------------------- control variate
+// The Romano-Touzi estimator with the control variate of McCrickerd and
+// Pakkanen and antithetic paths, as ML_console_ST/RBergomi.cpp implements it
+// (estimateControlVariate :493-540, ComputePriceRTVarRed :218-289,
+// updatePayoffControlVariate :478-491).
+//   X = BS(S, K, 1, sqrt((1 - rho^2) Ivdt)),  S = exp(-rho^2 Ivdt / 2 + rho IsvdW)
+//   Y = BS(S, K, 1, sqrt(rho^2 (Q - Ivdt)))   (Qmax in place of Q where Q <= Ivdt)
+
+// Fixed-shape block sum (256 threads): the same order on every run.
+__device__ double block_sum_256(double x, double* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    double t = 0.0;
+    for (int k = 0; k < 8; ++k) t += red[k];
+    return t;
+}
+
+// One block of 256 threads per output: Q = max_m 2 Ivdt_m; X_m, Y_m on the
+// pilot paths (stored in xy); means; centred covariance sums (two passes, as
+// aux.h:206-220 computes them); alpha = -cov(X, Y) / cov(Y, Y).
+__global__ void __launch_bounds__(256) k_cv_pilot(Fp64Tables t, const double2* __restrict__ ivb, int64_t Mc,
+                                                  double* __restrict__ xy, double* __restrict__ alpha,
+                                                  double* __restrict__ Qout)
+{
+    __shared__ double red[8];
+    const int i = blockIdx.x;
+    const OutDev od = t.outs[i];
+    const double2* iv = ivb + (size_t)od.vg * Mc;
+    double* X = xy + (size_t)i * 2 * Mc;
+    double* Y = X + Mc;
+    double q = 0.0;
+    for (int64_t m = threadIdx.x; m < Mc; m += 256) q = fmax(q, 2 * iv[m].x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) q = fmax(q, __shfl_xor_sync(0xffffffffu, q, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = q;
+    __syncthreads();
+    q = 0.0;
+    for (int k = 0; k < 8; ++k) q = fmax(q, red[k]);
+    const double r = od.rho;
+    double sx = 0.0, sy = 0.0;
+    for (int64_t m = threadIdx.x; m < Mc; m += 256) {
+        const double a = iv[m].x, b = iv[m].y;
+        const double spot = exp(-0.5 * r * r * a + r * b);
+        X[m] = bs_call_tau1(spot, od.K, sqrt((1.0 - r * r) * a));
+        Y[m] = bs_call_tau1(spot, od.K, sqrt(r * r * (q - a)));
+        sx += X[m];
+        sy += Y[m];
+    }
+    const double mx = block_sum_256(sx, red) / (double)Mc;
+    const double my = block_sum_256(sy, red) / (double)Mc;
+    double cxy = 0.0, cyy = 0.0;
+    for (int64_t m = threadIdx.x; m < Mc; m += 256) {
+        const double dy = Y[m] - my;
+        cxy += (X[m] - mx) * dy;
+        cyy += dy * dy;
+    }
+    cxy = block_sum_256(cxy, red);
+    cyy = block_sum_256(cyy, red);
+    if (threadIdx.x == 0) {
+        alpha[i] = -(cxy / (double)(Mc - 1)) / (cyy / (double)(Mc - 1));
+        Qout[i] = q;
+    }
+}
+
+void launch_cv_pilot(const Fp64Tables& t, const double* ivb, int64_t Mc, double* xy, double* alpha, double* Q,
+                     void* stream)
+{
+    k_cv_pilot<<<t.n_out, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, Mc, xy, alpha, Q);
+    count_launch();
+}
+
+__device__ __forceinline__ double cv_half(double2 iv, double rho, double K, double alpha, double Q, double Qmax,
+                                          unsigned& exc)
+{
+    const double spot = exp(-0.5 * rho * rho * iv.x + rho * iv.y);
+    const double x = bs_call_tau1(spot, K, sqrt((1.0 - rho * rho) * iv.x));
+    const bool inside = Q > iv.x;
+    if (!inside) ++exc;
+    const double y = bs_call_tau1(spot, K, inside ? sqrt(rho * rho * (Q - iv.x)) : sqrt(rho * rho * (Qmax - iv.x)));
+    return x + alpha * y;
+}
+
+// grid (nchunks, ceil(n_out / kOPB)), as k_payoff_sums: per path the
+// antithetic mean 0.5 (f(W) + f(-W)).
+__global__ void __launch_bounds__(256) k_payoff_sums_cv(Fp64Tables t, const double2* __restrict__ ivb,
+                                                        const double2* __restrict__ ivn, int64_t B,
+                                                        const double* __restrict__ alpha,
+                                                        const double* __restrict__ Q, double Qmax, int G,
+                                                        double* __restrict__ part,
+                                                        unsigned long long* __restrict__ count)
+{
+    __shared__ double red[8][kOPB][2];
+    const int c = blockIdx.x;
+    const int o0 = blockIdx.y * kOPB;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double S = 0, CS = 0, S2 = 0, CS2 = 0;
+    OutDev od[kOPB];
+    double al[kOPB], qq[kOPB];
+    unsigned exc[kOPB];
+#pragma unroll
+    for (int q = 0; q < kOPB; ++q) {
+        const int i = o0 + q;
+        od[q] = (i < t.n_out) ? t.outs[i] : OutDev{0.0, 1.0, -1, 0};
+        al[q] = (i < t.n_out) ? alpha[i] : 0.0;
+        qq[q] = (i < t.n_out) ? Q[i] : 0.0;
+        exc[q] = 0;
+    }
+    for (int sub = 0; sub < G; ++sub) {
+        const int64_t m = ((int64_t)c * G + sub) * 256 + threadIdx.x;
+#pragma unroll
+        for (int q = 0; q < kOPB; ++q) {
+            double x = 0.0;
+            if (m < B && od[q].vg >= 0) {
+                const size_t at = (size_t)od[q].vg * B + m;
+                x = 0.5 * cv_half(ivb[at], od[q].rho, od[q].K, al[q], qq[q], Qmax, exc[q]);
+                x += 0.5 * cv_half(ivn[at], od[q].rho, od[q].K, al[q], qq[q], Qmax, exc[q]);
+            }
+            double x2 = x * x;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+                x2 += __shfl_xor_sync(0xffffffffu, x2, o);
+            }
+            if (lane == 0) { red[w][q][0] = x; red[w][q][1] = x2; }
+        }
+        __syncthreads();
+        if (threadIdx.x < kOPB) {
+            const int q = threadIdx.x;
+            double a = 0, a2 = 0;
+            for (int k = 0; k < 8; ++k) { a += red[k][q][0]; a2 += red[k][q][1]; }
+            neumaier_add(S, CS, a);
+            neumaier_add(S2, CS2, a2);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < kOPB; ++q) {
+        unsigned e = exc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+        if (lane == 0 && e && o0 + q < t.n_out) atomicAdd(count + o0 + q, (unsigned long long)e);
+    }
+    if (threadIdx.x < kOPB && o0 + (int)threadIdx.x < t.n_out) {
+        double* p = part + ((size_t)c * t.n_out + o0 + threadIdx.x) * 4;
+        p[0] = S; p[1] = CS; p[2] = S2; p[3] = CS2;
+    }
+}
+
+void launch_payoff_sums_cv(const Fp64Tables& t, const double* ivb, const double* ivn, int64_t B, const double* alpha,
+                           const double* Q, double Qmax, int G, double* part, unsigned long long* count, int nchunks,
+                           void* stream)
+{
+    dim3 grid(nchunks, (t.n_out + kOPB - 1) / kOPB);
+    k_payoff_sums_cv<<<grid, 256, 0, (cudaStream_t)stream>>>(t, (const double2*)ivb, (const double2*)ivn, B, alpha,
+                                                             Q, Qmax, G, part, count);
+    count_launch();
+}
+
+// price = mean - alpha ((1 - p) BS(1, K, 1, sqrt(rho^2 Q)) + p BS(1, K, 1, sqrt(rho^2 Qmax))),
+// p = exceptions / M; stat from the unadjusted payoffs (RBergomi.cpp:266-284).
+__global__ void k_finalize_cv(const double* __restrict__ acc, int n_out, int64_t M, const OutDev* __restrict__ outs,
+                              const double* __restrict__ Tv, const double* __restrict__ alpha,
+                              const double* __restrict__ Q, const unsigned long long* __restrict__ count,
+                              double Qmax, int compute_iv, double* __restrict__ res)
+{
+    const int i = blockIdx.x;
+    if (i >= n_out) return;
+    const double S = acc[i * 4 + 0] + acc[i * 4 + 1];
+    const double S2 = acc[i * 4 + 2] + acc[i * 4 + 3];
+    const double mean = S * (1.0 / (double)M);
+    const double var = 1.0 * (S2 * (1.0 / (double)M)) + -1.0 * (mean * mean);
+    const double stat = sqrt(var) * (1.0 / sqrt((double)M));
+    const double p = (double)count[i] / (double)M, r = outs[i].rho, K = outs[i].K;
+    const double adj = (1.0 - p) * bs_call_tau1(1.0, K, sqrt(r * r * Q[i])) + p * bs_call_tau1(1.0, K, sqrt(r * r * Qmax));
+    const double price = mean - alpha[i] * adj;
+    const double iv = compute_iv ? implied_vol_warp(price, K, Tv[i]) : 0.0;
+    if ((threadIdx.x & 31) == 0) {
+        res[i] = price;
+        res[n_out + i] = stat;
+        res[2 * n_out + i] = iv;
+        res[3 * n_out + i] = S;
+        res[4 * n_out + i] = S2;
+    }
+}
+
+void launch_finalize_cv(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,
+                        const double* alpha, const double* Q, const unsigned long long* count, double Qmax,
+                        int compute_iv, double* res, void* stream)
+{
+    k_finalize_cv<<<n_out, 32, 0, (cudaStream_t)stream>>>(acc, n_out, M, outs, Tvals, alpha, Q, count, Qmax,
+                                                          compute_iv, res);
     count_launch();
 }
 

@@ -29,6 +29,7 @@ struct VGroup {
     double Hs, Ts;  // H and T at the last H-or-T trigger (scaleWtilde)
     double Hv, eta; // H and eta at the last H-or-T-or-eta trigger (updateV)
     double scale, dt, sdt;
+    double xi;  // forward variance (per tuple in the control-variate form, else the plan's)
     int nsteps;
 };
 
@@ -40,6 +41,9 @@ struct OutMap {
 struct Plan {
     double xi = 0;
     int N = 0;
+    // compensator index: v_i = xi exp(eta WS_{i-1} - eta^2/2 ((i - 1 + comp_shift) dt)^{2H});
+    // 0 for rBergLib (rBergomiMT.cpp:73-80), 1 for ML_console_ST (RBergomi.cpp:365-372)
+    int comp_shift = 0;
     std::vector<VolGroup> vols;
     std::vector<VGroup> vgs;
     std::vector<OutMap> outs;
@@ -56,7 +60,10 @@ struct Plan {
 bool build_plan(const rbg_params& p, Plan& plan, std::string& err, bool plain_mc = false);
 // The unordered form: one output per tuple, every tuple's chain recomputed
 // as the reference's updatePayoffUnordered does (equal tuples share state).
-bool build_plan_unordered(const rbg_unordered& u, Plan& plan, std::string& err);
+// xi_per: optional per-tuple forward variances (groups then split by xi);
+// comp_shift as in Plan.
+bool build_plan_unordered(const rbg_unordered& u, Plan& plan, std::string& err, const double* xi_per = nullptr,
+                          int comp_shift = 0);
 
 // ---- device-side views -------------------------------------------------
 struct VolDev {
@@ -89,7 +96,20 @@ int path_fp64_warps(int N);
 size_t path_fp64_smem(int N, int warps);
 // ivp non-null: Z has three streams per path (plain MC) and ivp[g][B] gets IsvdWp
 void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, void* stream,
-                      double* ivp = nullptr);
+                      double* ivp = nullptr, double* ivn = nullptr);
+// control-variate form (ML_console_ST): pilot statistics per output -- Q = max
+// 2 Ivdt over the pilot, alpha = -cov(X, Y) / var(Y) -- from the pilot's
+// (Ivdt, IsvdW) [group][Mc]; xy scratch holds 2 Mc doubles per output
+void launch_cv_pilot(const Fp64Tables& t, const double* ivb, int64_t Mc, double* xy, double* alpha, double* Q,
+                     void* stream);
+// per chunk (S, C, S2, C2) of the antithetic control-variate payoffs, and the
+// Qmax-exception count per output (atomically added, integer)
+void launch_payoff_sums_cv(const Fp64Tables& t, const double* ivb, const double* ivn, int64_t B, const double* alpha,
+                           const double* Q, double Qmax, int G, double* part, unsigned long long* count, int nchunks,
+                           void* stream);
+void launch_finalize_cv(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,
+                        const double* alpha, const double* Q, const unsigned long long* count, double Qmax,
+                        int compute_iv, double* res, void* stream);
 void launch_payoff_sums(const Fp64Tables& t, const double* ivb, int64_t B, int64_t ivb_stride, int G,
                         double* part, int nchunks, void* stream, const double* ivp = nullptr);
 void launch_accumulate(const double* part, int nchunks, int n_out, double* acc, void* stream);

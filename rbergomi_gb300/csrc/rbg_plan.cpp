@@ -65,6 +65,7 @@ VGroup make_vgroup(const Plan& plan, int vol, double Hs, double Ts, double Hv, d
     g.dt = Ts / N;
     g.sdt = std::sqrt(g.dt);
     g.scale = plan.vols[vol].c * std::pow(Ts, Hs);
+    g.xi = plan.xi;
     g.nsteps = N;
     return g;
 }
@@ -98,8 +99,9 @@ void fill_tables(Plan& plan)
         const VGroup& G = plan.vgs[g];
         double* c = plan.comp.data() + g * N;
         // updateV's compensator, evaluated as the reference writes it:
-        // 0.5 * eta * eta * pow((i - 1) * dt, 2 * H) with j = i - 1
-        for (int j = 0; j + 1 < N; ++j) c[j] = 0.5 * G.eta * G.eta * std::pow(j * G.dt, 2 * G.Hv);
+        // 0.5 * eta * eta * pow((i - 1 + comp_shift) * dt, 2 * H) with j = i - 1
+        for (int j = 0; j + 1 < N; ++j)
+            c[j] = 0.5 * G.eta * G.eta * std::pow((j + plan.comp_shift) * G.dt, 2 * G.Hv);
     }
 }
 }  // namespace
@@ -175,7 +177,8 @@ bool build_plan(const rbg_params& p, Plan& plan, std::string& err, bool plain_mc
     return true;
 }
 
-bool build_plan_unordered(const rbg_unordered& u, Plan& plan, std::string& err)
+bool build_plan_unordered(const rbg_unordered& u, Plan& plan, std::string& err, const double* xi_per,
+                          int comp_shift)
 {
     if (u.size <= 0) { err = "size must be positive"; return false; }
     if (!u.H || !u.eta || !u.rho || !u.T || !u.K) { err = "null parameter array"; return false; }
@@ -186,14 +189,15 @@ bool build_plan_unordered(const rbg_unordered& u, Plan& plan, std::string& err)
         if (!(u.H[i] > 0.0 && u.H[i] < 1.0)) { err = "H must lie in (0, 1)"; return false; }
 
     plan = Plan();
-    plan.xi = u.xi;
+    plan.xi = xi_per ? xi_per[0] : u.xi;
     plan.N = u.N;
+    plan.comp_shift = comp_shift;
     // updatePayoffUnordered (rBergomi/rBergomiMT.cpp:940-957) recomputes the
     // whole chain for every index: Volterra pass by H(i), WS = T(i)^H(i) Wtilde,
     // dt = T(i)/N, v from (H(i), eta(i)).  Equal tuples give equal states, so
     // passes are shared by exact H and variance groups by exact (H, T, eta).
     std::map<double, int> vol_of_H;
-    std::map<std::tuple<double, double, double>, int> vg_of_key;
+    std::map<std::tuple<double, double, double, double>, int> vg_of_key;
     std::vector<VGroup> vgs;
     std::vector<int> out_vg(u.size);
     for (long i = 0; i < u.size; ++i) {
@@ -203,11 +207,13 @@ bool build_plan_unordered(const rbg_unordered& u, Plan& plan, std::string& err)
             it = vol_of_H.emplace(H, (int)plan.vols.size()).first;
             plan.vols.push_back(make_vol(H, u.N));
         }
-        auto key = std::make_tuple(H, T, eta);
+        const double xi = xi_per ? xi_per[i] : u.xi;
+        auto key = std::make_tuple(H, T, eta, xi);
         auto jt = vg_of_key.find(key);
         if (jt == vg_of_key.end()) {
             jt = vg_of_key.emplace(key, (int)vgs.size()).first;
             vgs.push_back(make_vgroup(plan, it->second, H, T, H, eta, u.N));
+            vgs.back().xi = xi;
         }
         out_vg[i] = jt->second;
     }

@@ -19,6 +19,11 @@ def dropin(name):
     return {k: d[k] for k in d.files}
 
 
+def dropin_cv(name):
+    d = np.load(os.path.join(GOLDEN, f"cv_{name}.npz"))
+    return {k: d[k] for k in d.files}
+
+
 def debug8():
     with open(os.path.join(GOLDEN, "debug8.json")) as f:
         return json.load(f)

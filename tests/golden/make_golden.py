@@ -13,6 +13,9 @@ Outputs (all small, committed):
   dropin_rt.npz        computeIVRT_tensor(num_threads = 1) of the compiled
                        reference plus the mt19937_64 normals it drew
   dropin_mc.npz        computeIV_tensor(num_threads = 1), same
+  cv_*.npz             RBergomi::ComputeIVRTVarRed of ML_console_ST (the
+                       control-variate Romano-Touzi estimator) with a small
+                       pilot, plus the pilot and main normals it drew
 The GPU machine has no reference; tests read only these files there.
 """
 from __future__ import annotations
@@ -63,6 +66,14 @@ def dropin_case(name, fn, nstreams, xi, H, eta, rho, T, K, N, M, seed):
                         **{f"ref_{k}": v for k, v in r.items()})
 
 
+def cv_case(name, xi, H, eta, rho, T, K, N, M, Mc, seed):
+    p, s, iv, Zc, Z = O.ml_ref_price_rt_cv(xi, H, eta, rho, T, K, N, M, Mc, seed)
+    np.savez_compressed(os.path.join(HERE, f"cv_{name}.npz"), xi=np.array(xi, float), H=np.array(H, float),
+                        eta=np.array(eta, float), rho=np.array(rho, float), T=np.array(T, float),
+                        K=np.array(K, float), N=N, M=M, Mc=Mc, seed=np.array(seed, np.uint64), Zc=Zc, Z=Z,
+                        ref_price=p, ref_stat=s, ref_iv=iv)
+
+
 def main():
     O.build(ref=True)
     write_debug8()
@@ -83,6 +94,11 @@ def main():
                 [0.8, 1.0], 64, 256, [123, 452, 567])
     dropin_case("mc", "computeIV_tensor", 3, 0.07, [0.07, 0.1], [2.2, 2.4], [-0.9, -0.85], [0.5, 1.0],
                 [0.8, 1.0], 64, 256, [123, 452, 567])
+    # control variate: unordered tuples with their own xi; a 256-path pilot,
+    # and a 4-path pilot whose Q is exceeded on some main paths (Qmax branch)
+    cv_case("base", [0.04, 0.05, 0.04, 0.235 ** 2], [0.1, 0.2, 0.1, 0.07], [1.5, 1.9, 1.5, 1.9],
+            [-0.7, -0.9, -0.7, -0.9], [1.0, 0.5, 1.0, 1.0], [1.0, 0.9, 1.1, 1.2], 16, 256, 256, [5, 7])
+    cv_case("qmax", [0.04, 0.06], [0.1, 0.3], [2.5, 1.2], [-0.8, -0.4], [1.5, 0.75], [1.0, 1.05], 16, 128, 4, [9])
     print("golden fixtures written to", HERE)
 
 

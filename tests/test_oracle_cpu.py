@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from tests._golden import QUAD_CASES, debug8, dropin, quad, rel_err
+from tests._golden import QUAD_CASES, debug8, dropin, dropin_cv, quad, rel_err
 
 
 def test_philox_known_answers(oracle):
@@ -115,3 +115,19 @@ def test_live_reference_random_grid(oracle):
     a = oracle.payoffs_rt(0.06, H, eta, rho, T, K, Z)
     b = oracle.ref_payoffs_rt(0.06, H, eta, rho, T, K, Z)
     assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-3)) < 1e-11
+
+
+@pytest.mark.parametrize("name", ["base", "qmax"])
+def test_cv_oracle_vs_reference_fixture(oracle, name):
+    """The control-variate estimator (ML_console_ST's ComputeIVRTVarRed,
+    compiled from its own sources) replayed on the pilot and main normals it
+    drew: price 1e-12, stat 1e-8; the qmax case takes the Q_max branch."""
+    d = dropin_cv(name)
+    price, stat, alpha, Q, cnt = oracle.price_rt_cv(d["xi"], d["H"], d["eta"], d["rho"], d["T"], d["K"],
+                                                    d["Zc"], d["Z"])
+    assert np.all(rel_err(price, d["ref_price"]) < 1e-12)
+    assert np.all(rel_err(stat, d["ref_stat"]) < 1e-8)
+    if name == "qmax":
+        assert cnt.sum() > 0
+    else:
+        assert cnt.sum() == 0
