@@ -48,9 +48,11 @@ CASES = [
     # workload-2 shape, reduced M
     dict(xi=0.235 ** 2, H=[0.1], eta=[1.9], rho=[-0.9], T=[1.0] * 21, K=list(np.linspace(0.6, 1.4, 21)), N=512,
          M=(1 << 18) + 77, seed=11),
-    # two Volterra passes, several variance groups, long horizon (FFT backend)
+    # two Volterra passes, several variance groups, N = 1024 (two TMEM passes of the tensor-core GEMM)
     dict(xi=0.04, H=[0.07, 0.3], eta=[1.5, 2.0], rho=[-0.7, -0.5], T=[0.5, 2.0], K=[0.9, 1.2], N=1024, M=5000,
          seed=3),
+    # longer horizon: the batched-FFT backend
+    dict(xi=0.05, H=[0.1], eta=[1.5], rho=[-0.7], T=[2.0, 2.0, 2.0], K=[0.8, 1.0, 1.2], N=1500, M=3001, seed=4),
 ]
 
 
