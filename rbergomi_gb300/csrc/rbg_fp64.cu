@@ -305,9 +305,12 @@ __device__ double bs_gen(double K, double T, double s, int put)
 // Implied vol by a warp: inverts on the out-of-the-money side (put-call
 // parity for K < 1, as rBergLib/BlackScholes.cpp:38-41 does).  The 32 lanes
 // price 32 volatilities at once: first a geometric grid 1e-3 * 2^(l/2) to
-// bracket the root, then repeated 33-section of the bracket (the price is
-// increasing in sigma), shrinking it ~33x per round to ~1e-15 relative.
-// All lanes return the same value; NaN when no volatility fits.
+// bracket the root, then 33-section rounds of the bracket (the price is
+// increasing in sigma, ~33x narrower per round) down to 1e-6 relative, then
+// Newton on the log price inside the bracket to 1e-15.  The search is a chain
+// of serial FP64 evaluations on GB300's slow FP64 pipe, so fewer rounds is
+// what makes it fast.  All lanes return the same value; NaN when no
+// volatility fits.
 __device__ double implied_vol_warp(double price, double K, double T)
 {
     const unsigned FULL = 0xffffffffu;
@@ -323,7 +326,9 @@ __device__ double implied_vol_warp(double price, double K, double T)
     int f = __ffs(b) - 1;
     double lo = (f > 0) ? 1e-3 * exp2(0.5 * (f - 1)) : 0.0;
     double hi = 1e-3 * exp2(0.5 * f);
-    for (int it = 0; it < 14 && hi - lo > 1e-15 * hi; ++it) {
+    // 33-section rounds (one evaluation per lane) until the bracket is within
+    // 1e-6 relative, where Newton converges quadratically
+    for (int it = 0; it < 14 && hi - lo > 1e-6 * hi; ++it) {
         const double s = lo + (hi - lo) * (double)(lane + 1) / 33.0;
         b = __ballot_sync(FULL, bs_gen(K, T, s, put) >= target);
         f = b ? __ffs(b) - 1 : 32;
@@ -332,7 +337,33 @@ __device__ double implied_vol_warp(double price, double K, double T)
         if (f > 0) lo = nlo;
         if (f < 32) hi = nhi;
     }
-    return 0.5 * (lo + hi);
+    // safeguarded Newton on the log price (every lane computes the same
+    // iterate).  A Newton step below 1e-14 relative ends the search: the
+    // convergence is quadratic, so the iterate it gives is at roundoff.  A
+    // step that leaves the bracket, or a vanishing price, falls back to
+    // bisection; 40 halvings take a 1e-6 bracket below 1e-15 on their own.
+    const double lt = log(target), sqT = sqrt(T);
+    double s = 0.5 * (lo + hi);
+    for (int it = 0; it < 40; ++it) {
+        const double p = bs_gen(K, T, s, put);
+        if (p == target) break;
+        if (p > target) hi = s;
+        else lo = s;
+        double sn = 0.5 * (lo + hi);
+        if (p > 0.0) {
+            const double d1 = (log(1.0 / K) + 0.5 * s * s * T) / (s * sqT);
+            const double vega = exp(-0.5 * d1 * d1) * 0.39894228040143267794 * sqT;
+            const double nt = s - (log(p) - lt) * p / vega;
+            if (fabs(nt - s) <= 1e-14 * s) {
+                s = nt;
+                break;
+            }
+            if (nt > lo && nt < hi) sn = nt;
+        }
+        s = sn;
+        if (hi - lo <= 1e-15 * hi) break;
+    }
+    return s;
 }
 
 // res: [0,n) price, [n,2n) stat, [2n,3n) iv, [3n,4n) sum, [4n,5n) sum2.
