@@ -195,11 +195,13 @@ __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned i
     return ok;
 }
 
-// the same wait, made warp-uniform so .sync.aligned tcgen05 ops stay converged
+// the same wait, made warp-uniform so .sync.aligned tcgen05 ops stay converged;
+// the first try is inline, so a phase that has already completed (the common
+// case in a balanced pipeline) costs no call
 __device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site,
                                                unsigned long long* prof = nullptr)
 {
-    const bool ok = mbar_wait(bar, parity, err, site, prof);
+    const bool ok = mbar_try(bar, parity) || mbar_wait(bar, parity, err, site, prof);
     return __all_sync(0xffffffffu, ok);
 }
 
@@ -491,15 +493,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         const int p = threadIdx.x & (kTileM - 1);
         const int h = threadIdx.x >> 7;  // which kStepsPerThread steps of the chunk
         const PhiloxKeys keys = philox_keys(a.seed);
-        int64_t lt = 0;
-        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
+        // stage s and its phase parity ph run over the chunks of all tiles
+        int s = 0;
+        uint32_t ph = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
             const int64_t m = tile * kTileM + p;
             const bool valid = m < a.B;
             const uint64_t gpath = (uint64_t)(a.path0 + m);
-            for (int v = 0; v < nv; ++v) {
-                const int64_t gc = lt * nv + v;
-                const int s = (int)(gc % S);
-                const uint32_t ph = (uint32_t)((gc / S) & 1);
+            for (int v = 0; v < nv; ++v, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
                 // redrawn chunks of the second pass feed only the MMA (W1 A tile)
                 const bool redraw = v >= n0 && v < 2 * n0;
                 const int c = (v < n0) ? v : v - n0;
@@ -526,17 +527,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         float* my_acc = acc_s + (size_t)wg * a.n_g * NS * kTileM;
         float* w10_s = acc_s + (size_t)2 * a.n_g * NS * kTileM;  // W1_0 per path
         float* wq0_s = w10_s + kTileM;                          // Wperp_0 per path (plain Monte Carlo)
-        int64_t lt = 0;
-        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
+        int s = 0;
+        uint32_t ph = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
             const int64_t m = tile * kTileM + p;
             const bool valid = m < a.B;
             for (int g = 0; g < a.n_g; ++g)
 #pragma unroll
                 for (int t = 0; t < NS; ++t) my_acc[(NS * g + t) * kTileM + p] = 0.f;
-            for (int v = 0; v < nv; ++v) {
-                const int64_t gc = lt * nv + v;
-                const int s = (int)(gc % S);
-                const uint32_t ph = (uint32_t)((gc / S) & 1);
+            for (int v = 0; v < nv; ++v, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
                 // the producers' FP32 tiles of this stage (the upper half also pairs
                 // its last column with the next chunk's first W1), then the MMA results
                 if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7, a.prof)) goto done;
@@ -553,9 +552,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 const bool pass_end = (c == nc - 1) || (c == n0 - 1);
                 const bool has_next = c + 1 < nc;
                 const bool bnd = (c == n0 - 1);  // successor W1 in this stage's boundary row
-                const int sn = (int)((gc + 1) % S);
+                const int sn = (s + 1 == S) ? 0 : s + 1;
                 if ((kEpiWGs == 1 || wg == 1) && has_next && !bnd &&
-                    !mbar_wait_warp(smem_u32(full + sn), (uint32_t)(((gc + 1) / S) & 1), a.err, 8, a.prof))
+                    !mbar_wait_warp(smem_u32(full + sn), sn == 0 ? ph ^ 1u : ph, a.err, 8, a.prof))
                     goto done;
                 if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
                 tc_fence_after();
@@ -726,13 +725,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         constexpr bool wide = !TWO;  // strip_k(Np) == kChunk exactly when one pass covers Np
         const int P0 = kChunk * n0;  // first column of the last pass
         if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
-            int64_t lt = 0, pass = 0;
+            int64_t pass = 0;
+            int s = 0;
+            uint32_t ph = 0;
             bool ok = true;
-            for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++lt) {
-                for (int v = 0; v < nv; ++v) {
-                    const int64_t gc = lt * nv + v;
-                    const int s = (int)(gc % S);
-                    const uint32_t ph = (uint32_t)((gc / S) & 1);
+            for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                for (int v = 0; v < nv; ++v, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
                     // output columns [lo, hi) of this chunk; TMEM column = output column - toff
                     int c, lo, hi, toff;
                     if (v < n0) { c = v; lo = kChunk * c; hi = P0; toff = 0; }
