@@ -282,8 +282,14 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
 
     for (int64_t pr = blockIdx.x; pr < npairs; pr += gridDim.x) {
         // 1. normals of both paths, both streams (Np + 1 entries: W1[N] pairs with the last column)
-        for (int q = threadIdx.x; q < 2 * NS * ngrp; q += T) {
-            const int g = q % ngrp, s = (q / ngrp) % NS, pth = q / (NS * ngrp);
+        // q = (pth NS + s) ngrp + g runs over the block with stride T; (g, s, pth)
+        // are carried along instead of divided out
+        int g = threadIdx.x, s = 0, pth = 0;
+        while (g >= ngrp) {
+            g -= ngrp;
+            if (++s == NS) { s = 0; ++pth; }
+        }
+        while (pth < 2) {
             const int64_t m = 2 * pr + pth;
             float z[4] = {0.f, 0.f, 0.f, 0.f};
             if (m < a.B) {
@@ -294,6 +300,11 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
             float* o = ws + (NS * pth + s) * W + 4 * g;
 #pragma unroll
             for (int e = 0; e < 4; ++e) o[e] = (4 * g + e < N) ? z[e] : 0.f;
+            g += T;
+            while (g >= ngrp) {
+                g -= ngrp;
+                if (++s == NS) { s = 0; ++pth; }
+            }
         }
         for (int n = N + threadIdx.x; n < W; n += T)  // tails of the rows read as zeros
 #pragma unroll
