@@ -373,6 +373,60 @@ def run_grid(args):
     }))
 
 
+def run_sobol(args):
+    """Sobol' quasi-Monte Carlo RT pricing, FP64 form (rbg_price_rt_sobol):
+    H=0.1, eta=1.9, rho=-0.9, xi=0.235^2, T=1, 21 strikes on [0.6, 1.4], N=256
+    (512 Sobol' dimensions), M = 2^20 points.  Direction integers: the
+    reference generator's own (rBergomi/sobol.cpp), recovered from its points
+    in tests/golden/sobol.npz.  The same call with the Brownian bridge and the
+    Philox FP64 pricer on the same workload are timed beside it."""
+    import torch
+
+    import rbergomi_gb300 as R
+
+    torch.cuda.set_device(0)
+    R.lib()
+    stream = torch.cuda.current_stream()
+    V = R.sobol_directions_from_points(np.load(os.path.join(ROOT, "tests", "golden", "sobol.npz"))["gray_points"])
+    M, N = int(args.paths or (1 << 20)), int(args.steps_per_path or 256)
+    K = list(np.round(np.linspace(0.6, 1.4, 21), 10))
+    a = (0.235 ** 2, [0.1], [1.9], [-0.9], [1.0] * 21, K, N, M)
+    flush = torch.empty((256 << 20) // 4, dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        times, out = [], None
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return float(np.mean(times)), out
+
+    n0 = R.launch_count()
+    with ClockSampler(0) as clk:
+        ms, (pq, sq, _) = timed(lambda: R.price_rt_sobol(*a, V, stream=stream.cuda_stream))
+    launches = R.launch_count() - n0
+    ms_b, (pb, _, _) = timed(lambda: R.price_rt_sobol(*a, V, bridge=True, stream=stream.cuda_stream))
+    ms_p, (pp, sp, _) = timed(lambda: R.price_rt(*a, seed=11, precision=R.FP64, stream=stream.cuda_stream))
+    print(json.dumps({
+        "metric": METRIC, "value": M * N / (ms / 1e3), "unit": "path-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "Sobol' points (the reference generator's direction integers)",
+        "config": {"workload": "sobol-fp64-n256-m1m", "N": N, "M": M, "strikes": 21, "dims": 2 * N,
+                   "l2": "flushed (256 MiB write) before each step"},
+        "bridge_value": M * N / (ms_b / 1e3), "philox_fp64_value": M * N / (ms_p / 1e3),
+        "max_abs_diff_qmc_vs_philox": float(np.max(np.abs(pq - pp))), "philox_stat_max": float(np.max(sp)),
+        "max_abs_diff_bridge_vs_plain_qmc": float(np.max(np.abs(pb - pq))),
+        "clocks": clk.summary(), "gpu_launches": launches,
+    }))
+
+
 # ------------------------------------------------------------ serving arm
 def serving_requests(n: int, rate: float, seed: int = 20261203):
     """Calibration-style traffic: Poisson arrivals at `rate`/s; H ~ U[.03,.45],
@@ -474,7 +528,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT,
-                    choices=sorted(WORKLOADS) + ["serving-poisson", "paramtot-grid-m1m"])
+                    choices=sorted(WORKLOADS) + ["serving-poisson", "paramtot-grid-m1m", "sobol-fp64-n256-m1m"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
     ap.add_argument("--split", type=int, default=0, help="0 = BF16x3, 1 = FP16x3")
     ap.add_argument("--cpu-paths", type=int, default=1 << 17)
@@ -491,6 +545,8 @@ def main():
     if args.workload == "serving-poisson":
         run_serving(args)
         return
+    if args.workload == "sobol-fp64-n256-m1m":
+        return run_sobol(args)
     if args.workload == "paramtot-grid-m1m":
         args.precision = args.precision or "fp64"
         run_grid(args)

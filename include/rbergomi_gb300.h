@@ -214,6 +214,34 @@ int rbg_generate_normals(uint64_t seed, int64_t path_offset, int64_t M, int N, i
 int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, int streams,
                                  double* Z);
 
+/* ---- Sobol' quasi-Monte Carlo (rBergomi/rBergomiMT.cpp:610-715,
+ * ComputePriceRTMT_sobol / ComputeIVRTMT_sobol, and their single-threaded
+ * twins :717-805; rBergomi/qmc.cpp:25-38 normalQMC_sample).
+ *
+ * Path m (global index path_offset + m) takes Sobol' point m + 1 + path_offset
+ * in dimension 2N; W1 = coordinates 0, 2, 4, ..., W1perp = 1, 3, 5, ...
+ * (rBergomi/aux.h:186-191 breakZ), each through the FP64 normal quantile.
+ * The caller supplies the direction integers, dims x 62 uint64 row-major:
+ * coordinate d of point s is (XOR of directions[d*62 + k] over the set bits k
+ * of s ^ (s >> 1)) * 2^-62, which is the point rBergomi/sobol.cpp i8_sobol
+ * returns for seed s when given its own table (the integers v[d][k] after
+ * its column scaling).  dims >= 2N; point indices stay below 2^62.  The
+ * library ships no table.
+ * bridge != 0 maps each stream through the Brownian-bridge ("hierarchical")
+ * construction of rBergomi/aux.h:106-125 (N a power of two, N <= 8192).
+ * The reference has no C export for these; this is the replacement for
+ * linking its C++ functions. */
+
+/* RT prices over Sobol' normals, FP64 form (o->precision == RBG_FP64); the
+ * seed is unused, o->path_offset shifts the point range.  stat is the
+ * reference's Monte Carlo formula applied to the QMC sample. */
+int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t* directions, int dims, int bridge,
+                       double* price, double* stat, double* iv);
+/* The Sobol' normals those prices use: M*2*N doubles in the quadrature
+ * layout, host pointer. */
+int rbg_sobol_normals(const uint64_t* directions, int dims, int N, int64_t M, int64_t path_offset, int bridge,
+                      double* Z);
+
 /* Implied vols of call prices (S0 = 1, r = 0) on the GPU; NaN where no
  * volatility reproduces the price. */
 int rbg_implied_vol(int n, const double* price, const double* K, const double* T, double* iv);

@@ -21,6 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "librbg_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "librbergomi_ref.so")
 ML_REF_SO = os.path.join(HERE, "_ref", "libml_ref.so")
+QMC_REF_SO = os.path.join(HERE, "_ref", "libqmc_ref.so")
 REF_SRC_DIR = "/root/reference"
 
 _dp = C.POINTER(C.c_double)
@@ -70,6 +71,13 @@ def lib():
                                                                   C.c_double, C.c_int, _dp, _dp, _dp, _dp,
                                                                   C.POINTER(C.c_int64)]
         L.rbgo_price_rt_cv.restype = C.c_int
+        L.rbgo_inv_normal.argtypes = [C.c_double]
+        L.rbgo_inv_normal.restype = C.c_double
+        L.rbgo_sobol_point.argtypes = [_u64p, C.c_int, C.c_uint64, _dp]
+        L.rbgo_hier.argtypes = [_dp, C.c_int, _dp]
+        L.rbgo_hier.restype = C.c_int
+        L.rbgo_sobol_normals.argtypes = [_u64p, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int, _dp]
+        L.rbgo_sobol_normals.restype = C.c_int
         _lib = L
     return _lib
 
@@ -267,3 +275,97 @@ def ref_compute(fn: str, xi, H, eta, rho, T, K, N, M, seed, num_threads=1):
                        *[a.ctypes.data_as(_dp) for a in arrs], out)
     names = ["price", "iv", "stat", "H", "eta", "rho", "T", "K"]
     return dict(zip(names, arrs))
+
+
+# ----------------------------------------------------------- Sobol' QMC
+# rBergomi/qmc.cpp, rBergomi/sobol.cpp (i8_sobol), rBergomi/aux.h (breakZ,
+# hierarchical2increments).  V: direction integers [dims][62] uint64, point
+# s coordinate d = (XOR of V[d][k] over the set bits k of s ^ (s >> 1)) 2^-62.
+SOBOL_BITS = 62
+
+
+def sobol_directions_from_points(points):
+    """Direction integers from a generator's points at indices 2^(k+1) - 1
+    (whose Gray code is 2^k): points[k][d] * 2^62 = V[d][k], exact for k <= 52."""
+    P = np.asarray(points, np.float64)
+    q = P * 2.0 ** 62
+    if not np.all(q == np.floor(q)):
+        raise ValueError("points are not multiples of 2^-62")
+    V = np.zeros((P.shape[1], SOBOL_BITS), np.uint64)
+    V[:, :P.shape[0]] = q.T.astype(np.uint64)
+    return V
+
+
+def inv_normal(p):
+    L = lib()
+    return np.array([L.rbgo_inv_normal(float(x)) for x in np.ravel(p)]).reshape(np.shape(p))
+
+
+def sobol_point(V, s, dims=None):
+    V = np.ascontiguousarray(V, np.uint64)
+    dims = V.shape[0] if dims is None else dims
+    x = np.empty(dims)
+    lib().rbgo_sobol_point(V.ctypes.data_as(_u64p), dims, int(s), x.ctypes.data_as(_dp))
+    return x
+
+
+def hier(Z):
+    Z = np.ascontiguousarray(Z, np.float64)
+    out = np.empty_like(Z)
+    if lib().rbgo_hier(Z.ctypes.data_as(_dp), len(Z), out.ctypes.data_as(_dp)):
+        raise ValueError("length must be a power of two")
+    return out
+
+
+def sobol_normals(V, N, M, path0=0, bridge=False):
+    """[M, 2, N] normals: path m takes point path0 + m + 1; W1 = even
+    coordinates, W1perp = odd ones; bridge: hierarchical2increments per stream."""
+    V = np.ascontiguousarray(V, np.uint64)
+    Z = np.empty((M, 2, N))
+    if lib().rbgo_sobol_normals(V.ctypes.data_as(_u64p), V.shape[0], N, path0, M, int(bridge), Z.ctypes.data_as(_dp)):
+        raise ValueError("bad Sobol' sizes")
+    return Z
+
+
+def qmc_ref_available() -> bool:
+    return os.path.exists(QMC_REF_SO)
+
+
+_qmc = None
+
+
+def _qmc_ref():
+    global _qmc
+    if _qmc is None:
+        if not qmc_ref_available():
+            raise FileNotFoundError(f"{QMC_REF_SO} not built (make -C oracle ref)")
+        R = C.CDLL(QMC_REF_SO)
+        lp = C.POINTER(C.c_longlong)
+        R.qmcglue_sobol_walk.argtypes = [C.c_int, C.c_longlong, lp, C.c_int, _dp]
+        R.qmcglue_normal_sample.argtypes = [C.c_int, C.c_longlong, _dp]
+        R.qmcglue_hier.argtypes = [_dp, C.c_int, _dp]
+        _qmc = R
+    return _qmc
+
+
+def qmc_ref_points(dims, seeds):
+    """The reference's i8_sobol points at the given ascending indices (one sequential walk)."""
+    seeds = np.ascontiguousarray(seeds, np.int64)
+    out = np.empty((len(seeds), dims))
+    _qmc_ref().qmcglue_sobol_walk(dims, int(seeds[-1]), seeds.ctypes.data_as(C.POINTER(C.c_longlong)), len(seeds),
+                                  out.ctypes.data_as(_dp))
+    return out
+
+
+def qmc_ref_normal_sample(dims, i):
+    """The reference's normalQMC_sample(Z, dims, i) (quantile from the Boost stand-in)."""
+    z = np.empty(dims)
+    _qmc_ref().qmcglue_normal_sample(dims, int(i), z.ctypes.data_as(_dp))
+    return z
+
+
+def qmc_ref_hier(Z):
+    Z = np.ascontiguousarray(Z, np.float64)
+    out = np.empty_like(Z)
+    _qmc_ref().qmcglue_hier(Z.ctypes.data_as(_dp), len(Z), out.ctypes.data_as(_dp))
+    return out

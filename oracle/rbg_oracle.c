@@ -597,3 +597,103 @@ int rbgo_price_rt_cv(long n, const double* xi, const double* H, const double* et
     free(G); free(s1); free(s2); free(cnt);
     return fail ? -1 : 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Sobol' quasi-Monte Carlo normals.                                         */
+/*   rBergomi/rBergomiMT.cpp:669-670 (ComputePriceRTMT_sobol): path m takes  */
+/*     Sobol' point m+1 in dimension 2N, then breakZ;                        */
+/*   rBergomi/qmc.cpp:21-38 (normalQMC_sample): i8_sobol, then the normal    */
+/*     quantile of every coordinate (qmc.h:36-46);                           */
+/*   rBergomi/sobol.cpp i8_sobol: Antonov-Saleev (Gray-code) order, point s  */
+/*     = XOR of the scaled direction integers v[d][k] over the set bits k of */
+/*     gray(s) = s ^ (s >> 1), times 2^-62;                                  */
+/*   rBergomi/aux.h:186-191 (breakZ): W1 = even coordinates, W1perp = odd;   */
+/*   rBergomi/aux.h:106-125 (hierarchical2increments): the Brownian-bridge   */
+/*     (Haar) map of one N = 2^m vector, used per stream when asked.         */
+/* The direction integers are the caller's: V[d * 62 + k].                   */
+/* ------------------------------------------------------------------------ */
+#define SOBOL_BITS 62
+
+/* Normal quantile: Hastings' start (Abramowitz & Stegun 26.2.23), then three
+ * Halley steps on Phi(x) = q in the lower tail.  Same steps as the oracle's
+ * Boost stand-in (oracle/shims/boost/math/distributions/normal.hpp). */
+double rbgo_inv_normal(double p)
+{
+    if (!(p > 0.0)) return p == 0.0 ? -INFINITY : NAN;
+    if (!(p < 1.0)) return p == 1.0 ? INFINITY : NAN;
+    const int upper = p > 0.5;
+    const double q = upper ? 1.0 - p : p;
+    const double t = sqrt(-2.0 * log(q));
+    double x = -(t - (2.515517 + t * (0.802853 + t * 0.010328)) / (1.0 + t * (1.432788 + t * (0.189269 + t * 0.001308))));
+    for (int i = 0; i < 3; ++i) {
+        const double e = 0.5 * erfc(-x * 0.70710678118654752440) - q;
+        const double u = e * 2.50662827463100050242 * exp(0.5 * x * x);
+        x = x - u / (1.0 + 0.5 * x * u);
+    }
+    return upper ? -x : x;
+}
+
+/* Coordinates [0, dims) of Sobol' point s (rBergomi/sobol.cpp i8_sobol). */
+void rbgo_sobol_point(const uint64_t* V, int dims, uint64_t s, double* x)
+{
+    const uint64_t g = s ^ (s >> 1);
+    for (int d = 0; d < dims; ++d) {
+        uint64_t q = 0;
+        for (int k = 0; k < SOBOL_BITS; ++k)
+            if ((g >> k) & 1u) q ^= V[(size_t)d * SOBOL_BITS + k];
+        x[d] = (double)q * 2.168404344971008868e-19; /* 2^-62 */
+    }
+}
+
+/* rBergomi/aux.h:106-125.  n must be 2^m; returns -1 otherwise. */
+int rbgo_hier(const double* Z, int n, double* dW)
+{
+    int m = 0;
+    while ((1 << m) < n) ++m;
+    if ((1 << m) != n) return -1;
+    for (int i = 0; i < n; ++i) {
+        double w = exp2(-0.5 * m) * Z[0];
+        for (int k = 1; k <= m; ++k) {
+            const int i2nm = i >> (m - k); /* floor(i 2^(k-m)) */
+            const int iota = (i2nm + 1) % 2;
+            const int weight = 2 * iota - 1;
+            const int index = (1 << (k - 1)) + (i2nm + iota + 1) / 2 - 1;
+            w += exp2(0.5 * (k - m - 1)) * weight * Z[index];
+        }
+        dW[i] = w;
+    }
+    return 0;
+}
+
+/* Z[(m * 2 + s) * N + j] for paths [path0, path0 + M): point path0 + m + 1,
+ * W1 (s = 0) = coordinates 0, 2, 4, ..., W1perp (s = 1) = 1, 3, 5, ...;
+ * bridge: each stream through rbgo_hier.  Returns -1 on bad sizes. */
+int rbgo_sobol_normals(const uint64_t* V, int dims, int N, int64_t path0, int64_t M, int bridge, double* Z)
+{
+    if (dims < 2 * N) return -1;
+    if (bridge && (N & (N - 1))) return -1;
+    int bad = 0;
+#pragma omp parallel
+    {
+        double* x = (double*)malloc(sizeof(double) * 2 * (size_t)N);
+        double* t = (double*)malloc(sizeof(double) * (size_t)N);
+#pragma omp for schedule(static)
+        for (int64_t m = 0; m < M; ++m) {
+            rbgo_sobol_point(V, 2 * N, (uint64_t)(path0 + m + 1), x);
+            double* z = Z + (size_t)m * 2 * N;
+            for (int j = 0; j < N; ++j) {
+                z[j] = rbgo_inv_normal(x[2 * j]);
+                z[N + j] = rbgo_inv_normal(x[2 * j + 1]);
+            }
+            if (bridge) {
+                for (int s = 0; s < 2; ++s) {
+                    if (rbgo_hier(z + s * N, N, t)) bad = 1;
+                    memcpy(z + s * N, t, sizeof(double) * N);
+                }
+            }
+        }
+        free(x);
+        free(t);
+    }
+    return bad ? -1 : 0;
+}

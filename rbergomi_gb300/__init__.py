@@ -66,6 +66,7 @@ EXPORTS = [
     "rbg_server_poll", "rbg_server_wait", "rbg_server_get_stats", "rbg_server_destroy", "rbg_server_last_error",
     "rbg_price_rt_unordered", "computeIV_tensor", "rbg_price_mc", "rbg_payoffs_mc", "rbg_generate_normals_streams",
     "rbg_plan_info_mc", "rbg_plan_info_unordered", "rbg_price_rt_cv", "rbg_price_rt_cv_normals",
+    "rbg_price_rt_sobol", "rbg_sobol_normals",
 ]
 
 STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4
@@ -101,6 +102,8 @@ def lib():
         L.rbg_payoffs_mc.argtypes = [P, O, C.c_void_p, C.c_void_p, C.c_int]
         L.rbg_payoffs_mc.restype = C.c_int
         L.rbg_generate_normals_streams.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_int, _dp]
+        L.rbg_price_rt_sobol.argtypes = [P, O, _u64p, C.c_int, C.c_int, _dp, _dp, _dp]
+        L.rbg_sobol_normals.argtypes = [_u64p, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int, _dp]
         L.rbg_generate_normals_streams.restype = C.c_int
         L.rbg_generate_normals.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int, C.c_int, _dp]
         L.rbg_generate_normals.restype = C.c_int
@@ -323,6 +326,59 @@ def generate_normals(seed, M, N, precision=FP64, path_offset=0, streams=2) -> np
     _check(lib().rbg_generate_normals_streams(int(seed) & 0xFFFFFFFFFFFFFFFF, int(path_offset), int(M), int(N),
                                               int(precision), int(streams), Z.ctypes.data_as(_dp)))
     return Z
+
+
+SOBOL_BITS = 62
+
+
+def _sobol_table(directions):
+    V = np.asarray(directions)
+    if V.ndim != 2 or V.shape[1] > SOBOL_BITS:
+        raise ValueError("Sobol' directions must be [dims, <= 62] integers")
+    T = np.zeros((V.shape[0], SOBOL_BITS), np.uint64)
+    T[:, :V.shape[1]] = V.astype(np.uint64)
+    return T
+
+
+def sobol_directions_from_points(points) -> np.ndarray:
+    """Direction table [dims, 62] from a Sobol' generator's points at indices
+    2^(k+1) - 1, k = 0, 1, ... (rows of `points`): those points have Gray code
+    2^k, so point * 2^62 is column k (exact for k <= 52)."""
+    P = np.asarray(points, np.float64)
+    q = P * 2.0 ** 62
+    if P.ndim != 2 or P.shape[0] > 52 or not np.all(q == np.floor(q)):
+        raise ValueError("expected points at indices 2^(k+1) - 1 on the 2^-62 grid, k < 52")
+    V = np.zeros((P.shape[1], SOBOL_BITS), np.uint64)
+    V[:, :P.shape[0]] = q.T.astype(np.uint64)
+    return V
+
+
+def sobol_normals(directions, N, M, path_offset=0, bridge=False) -> np.ndarray:
+    """Sobol' quasi-Monte Carlo normals [M, 2, N] (rBergomi/qmc.cpp
+    normalQMC_sample + breakZ): path m takes point path_offset + m + 1.
+    directions: [dims, 62] direction integers (coordinate d of point s is the
+    XOR of directions[d, k] over the set bits k of s ^ (s >> 1), times 2^-62).
+    bridge: Brownian-bridge map of each stream (rBergomi/aux.h
+    hierarchical2increments; N a power of two)."""
+    V = _sobol_table(directions)
+    Z = np.empty((M, 2, N))
+    _check(lib().rbg_sobol_normals(V.ctypes.data_as(C.POINTER(C.c_uint64)), V.shape[0], int(N), int(M),
+                                   int(path_offset), int(bool(bridge)), Z.ctypes.data_as(_dp)))
+    return Z
+
+
+def price_rt_sobol(xi, H, eta, rho, T, K, N, M, directions, bridge=False, **opts):
+    """RT prices over Sobol' normals, FP64 form (the reference's
+    ComputeIVRTMT_sobol, rBergomi/rBergomiMT.cpp:610-715): (price, stat, iv)."""
+    V = _sobol_table(directions)
+    p = _Params(xi, H, eta, rho, T, K, N, M)
+    opts.setdefault("precision", FP64)
+    o = options(**opts)
+    price, stat, iv = np.empty(p.out), np.empty(p.out), np.empty(p.out)
+    _check(lib().rbg_price_rt_sobol(C.byref(p.s), C.byref(o), V.ctypes.data_as(C.POINTER(C.c_uint64)), V.shape[0],
+                                    int(bool(bridge)), price.ctypes.data_as(_dp), stat.ctypes.data_as(_dp),
+                                    iv.ctypes.data_as(_dp)))
+    return price, stat, iv
 
 
 def price_mc(xi, H, eta, rho, T, K, N, M, **opts):

@@ -21,7 +21,8 @@ LIB = os.path.join(PKG, "librbergomi_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
-SOURCES = ["rbg_plan.cpp", "rbg_api.cpp", "rbg_fp64.cu", "rbg_mixed.cu", "rbg_fft.cu", "rbg_static.cu", "rbg_server.cpp"]
+SOURCES = ["rbg_plan.cpp", "rbg_api.cpp", "rbg_fp64.cu", "rbg_mixed.cu", "rbg_fft.cu", "rbg_static.cu", "rbg_qmc.cu",
+           "rbg_server.cpp"]
 
 
 def nvcc() -> str:

@@ -136,10 +136,11 @@ struct Ctx {
     int dev = -1;
     cudaStream_t stream = nullptr;
     std::mutex mu;
-    DevBuf z, ivb, ivp, part, acc, tabs, res, pay, mixed_ws, cv;
-    // host images of what `tabs` and `mixed_ws` hold, so that a call with
-    // the same tables (a calibration loop, a benchmark) uploads nothing
+    DevBuf z, ivb, ivp, part, acc, tabs, res, pay, mixed_ws, cv, sobol;
+    // host images of what `tabs`, `mixed_ws` and `sobol` hold, so that a call
+    // with the same tables (a calibration loop, a benchmark) uploads nothing
     std::vector<unsigned char> tabs_img, mixed_img;
+    std::vector<unsigned long long> sobol_img;
     ~Ctx() {}
 };
 
@@ -245,8 +246,12 @@ static int64_t fp64_batch(const Plan& plan, int64_t M, int ns = 2)
 
 // mc: the plain Monte Carlo estimator (third normal stream Wperp, payoff
 // max(S_T - K, 0)) instead of the Romano-Touzi conditional price.
+// sobol_vt: Sobol' quasi-Monte Carlo normals (device direction table
+// [kSobolBits][2N], path m takes point path_offset + m + 1; br: Brownian
+// bridge or nullptr) instead of the Philox stream.  RT only.
 static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M, cudaStream_t st,
-                      double* host_res, bool mc)
+                      double* host_res, bool mc, const unsigned long long* sobol_vt = nullptr,
+                      const SobolBridge* br = nullptr)
 {
     TableSet ts;
     int rc = upload_tables(c, plan, st, ts);
@@ -267,8 +272,13 @@ static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M,
         const int64_t b = std::min(B, M - m0);
         {
             ProfScope ps(kStageNormals, st);
-            launch_normals(o.seed, o.path_offset + m0, b, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st,
-                           ns);
+            if (sobol_vt) {
+                if (launch_sobol_normals(sobol_vt, N, (uint64_t)(o.path_offset + m0 + 1), b, br, c.z.as<double>(), st))
+                    return fail(RBG_ERR_UNSUPPORTED, "Brownian bridge shared memory not available for this N");
+            } else {
+                launch_normals(o.seed, o.path_offset + m0, b, N, o.normals == RBG_NORMALS_F32, c.z.as<double>(), st,
+                               ns);
+            }
         }
         {
             ProfScope ps(kStagePathFp64, st);
@@ -654,6 +664,99 @@ int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, 
 int rbg_generate_normals(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, double* Z)
 {
     return rbg_generate_normals_streams(seed, path_offset, M, N, precision, 2, Z);
+}
+
+// ------------------------------------------------------ Sobol' QMC normals
+// Checks the request and puts the first 2N coordinates of the caller's
+// direction table on the device, transposed to [kSobolBits][2N] (kept, so a
+// repeated table uploads nothing).  bridge: the hierarchical map's
+// coefficients, computed as rBergomi/aux.h:106-125 does (exp2 of halves).
+static int sobol_setup(Ctx& c, const uint64_t* dirs, int dims, int N, int bridge, int64_t path_offset, int64_t M,
+                       cudaStream_t st, SobolBridge& br)
+{
+    if (!dirs) return fail(RBG_ERR_ARG, "null Sobol' direction table");
+    if (N < 1 || M < 1 || path_offset < 0) return fail(RBG_ERR_ARG, "bad sizes");
+    if (dims < 2 * N) return fail(RBG_ERR_ARG, "the Sobol' direction table has fewer than 2N dimensions");
+    if ((uint64_t)path_offset + (uint64_t)M >= ((uint64_t)1 << kSobolBits) - 1)
+        return fail(RBG_ERR_ARG, "Sobol' point index beyond 2^62");
+    if (bridge) {
+        int m = 0;
+        while ((1 << m) < N) ++m;
+        if ((1 << m) != N) return fail(RBG_ERR_ARG, "the Brownian bridge needs N a power of two");
+        if (m > kMaxBridgeLevels) return fail(RBG_ERR_UNSUPPORTED, "the Brownian bridge supports N <= 8192");
+        br.m = m;
+        br.c[0] = std::exp2(-0.5 * m);
+        for (int n = 1; n <= m; ++n) br.c[n] = std::exp2(0.5 * (n - m - 1));
+    }
+    const int D = 2 * N;
+    std::vector<unsigned long long> img((size_t)kSobolBits * D);
+    for (int k = 0; k < kSobolBits; ++k)
+        for (int d = 0; d < D; ++d) img[(size_t)k * D + d] = dirs[(size_t)d * kSobolBits + k];
+    if (img != c.sobol_img) {
+        int rc = ensure(c.sobol, sizeof(unsigned long long) * img.size(), "Sobol' table");
+        if (rc) return rc;
+        c.sobol_img.clear();
+        RBG_CUDA(cudaMemcpyAsync(c.sobol.p, img.data(), sizeof(unsigned long long) * img.size(),
+                                 cudaMemcpyHostToDevice, st));
+        RBG_CUDA(cudaStreamSynchronize(st));
+        g_h2d += sizeof(unsigned long long) * img.size();
+        c.sobol_img.swap(img);
+    }
+    return RBG_OK;
+}
+
+int rbg_sobol_normals(const uint64_t* directions, int dims, int N, int64_t M, int64_t path_offset, int bridge,
+                      double* Z)
+{
+    if (!Z) return fail(RBG_ERR_ARG, "null output");
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    SobolBridge br{};
+    if ((rc = sobol_setup(*c, directions, dims, N, bridge, path_offset, M, c->stream, br))) return rc;
+    const int64_t B = std::max<int64_t>(1, std::min<int64_t>(M, ((int64_t)1 << 30) / (16 * (int64_t)N)));
+    if ((rc = ensure(c->z, sizeof(double) * 2 * N * (size_t)B, "normals"))) return rc;
+    for (int64_t m0 = 0; m0 < M; m0 += B) {
+        const int64_t b = std::min(B, M - m0);
+        if (launch_sobol_normals(c->sobol.as<unsigned long long>(), N, (uint64_t)(path_offset + m0 + 1), b,
+                                 bridge ? &br : nullptr, c->z.as<double>(), c->stream))
+            return fail(RBG_ERR_UNSUPPORTED, "Brownian bridge shared memory not available for this N");
+        RBG_CUDA(cudaGetLastError());
+        RBG_CUDA(cudaMemcpyAsync(Z + m0 * 2 * N, c->z.p, sizeof(double) * 2 * N * b, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    }
+    RBG_CUDA(cudaStreamSynchronize(c->stream));
+    return RBG_OK;
+}
+
+int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t* directions, int dims, int bridge,
+                       double* price, double* stat, double* iv)
+{
+    if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
+    if (o->precision != RBG_FP64) return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals run in the FP64 form");
+    if (o->conv == RBG_CONV_GEMM || o->conv == RBG_CONV_FFT)
+        return fail(RBG_ERR_UNSUPPORTED, "FP64 form uses the direct Volterra sum");
+    g_h2d = g_d2h = 0;
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err, false)) return fail(RBG_ERR_ARG, err);
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
+    SobolBridge br{};
+    if ((rc = sobol_setup(*c, directions, dims, plan.N, bridge, o->path_offset, p->M, st, br))) return rc;
+    std::vector<double> res(5 * plan.outs.size(), 0.0);
+    if ((rc = price_fp64(*c, plan, *o, p->M, st, res.data(), false, c->sobol.as<unsigned long long>(),
+                         bridge ? &br : nullptr)))
+        return rc;
+    const size_t no = plan.outs.size();
+    if (price) std::memcpy(price, res.data(), no * sizeof(double));
+    if (stat) std::memcpy(stat, res.data() + no, no * sizeof(double));
+    if (iv) std::memcpy(iv, res.data() + 2 * no, no * sizeof(double));
+    return RBG_OK;
 }
 
 int rbg_price_mc(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv)

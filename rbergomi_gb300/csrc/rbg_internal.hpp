@@ -92,6 +92,21 @@ struct Fp64Tables {
 
 // ns normal streams per path: 2 (W1, W1perp) for RT, 3 (+ Wperp) for plain MC
 void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream, int ns = 2);
+
+// Sobol' quasi-Monte Carlo normals (rbg_qmc.cu).  Direction integers per
+// coordinate: kSobolBits columns; coordinate d of point s is (XOR of
+// V[d][k] over the set bits k of s ^ (s >> 1)) * 2^-62.
+constexpr int kSobolBits = 62;
+constexpr int kMaxBridgeLevels = 13;  // Brownian bridge: N = 2^m, m <= 13
+struct SobolBridge {
+    double c[kMaxBridgeLevels + 1];  // c[0] = 2^(-m/2), c[n] = 2^((n - m - 1)/2)
+    int m;
+};
+// Z [B][2][N] for points s0 .. s0 + B - 1; Vt = [kSobolBits][2N] on the
+// device; br = nullptr: no bridge.  Returns nonzero when the bridge's shared
+// memory cannot be granted.
+int launch_sobol_normals(const unsigned long long* Vt, int N, uint64_t s0, int64_t B, const SobolBridge* br,
+                         double* Z, void* stream);
 int path_fp64_warps(int N);
 size_t path_fp64_smem(int N, int warps);
 // ivp non-null: Z has three streams per path (plain MC) and ivp[g][B] gets IsvdWp

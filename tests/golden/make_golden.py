@@ -16,6 +16,12 @@ Outputs (all small, committed):
   cv_*.npz             RBergomi::ComputeIVRTVarRed of ML_console_ST (the
                        control-variate Romano-Touzi estimator) with a small
                        pilot, plus the pilot and main normals it drew
+  sobol.npz            the reference's Sobol' generator (rBergomi/sobol.cpp
+                       i8_sobol, 1111 dimensions): its points at indices
+                       2^(k+1) - 1, k < 24 (from which the direction integers
+                       follow), a run of points 1..64 in 128 dimensions, a few
+                       normalQMC_sample outputs (rBergomi/qmc.cpp) and one
+                       hierarchical2increments input/output pair (aux.h)
 The GPU machine has no reference; tests read only these files there.
 """
 from __future__ import annotations
@@ -74,6 +80,17 @@ def cv_case(name, xi, H, eta, rho, T, K, N, M, Mc, seed):
                         ref_price=p, ref_stat=s, ref_iv=iv)
 
 
+def sobol_case():
+    D, K = 1111, 24
+    gray_pts = O.qmc_ref_points(D, [(1 << (k + 1)) - 1 for k in range(K)])
+    run = O.qmc_ref_points(128, np.arange(1, 65))
+    samp_idx = np.array([1, 2, 3, 17, 1000, 4099, 65536], np.int64)
+    samples = np.stack([O.qmc_ref_normal_sample(128, i) for i in samp_idx])
+    z = np.random.default_rng(11).standard_normal(256)
+    np.savez_compressed(os.path.join(HERE, "sobol.npz"), gray_points=gray_pts, run_points=run,
+                        sample_index=samp_idx, samples=samples, hier_in=z, hier_out=O.qmc_ref_hier(z))
+
+
 def main():
     O.build(ref=True)
     write_debug8()
@@ -99,6 +116,7 @@ def main():
     cv_case("base", [0.04, 0.05, 0.04, 0.235 ** 2], [0.1, 0.2, 0.1, 0.07], [1.5, 1.9, 1.5, 1.9],
             [-0.7, -0.9, -0.7, -0.9], [1.0, 0.5, 1.0, 1.0], [1.0, 0.9, 1.1, 1.2], 16, 256, 256, [5, 7])
     cv_case("qmax", [0.04, 0.06], [0.1, 0.3], [2.5, 1.2], [-0.8, -0.4], [1.5, 0.75], [1.0, 1.05], 16, 128, 4, [9])
+    sobol_case()
     print("golden fixtures written to", HERE)
 
 

@@ -1,0 +1,83 @@
+"""Sobol' quasi-Monte Carlo on the GPU against the oracle (FP64 form).
+
+Direction integers: the reference's own (rBergomi/sobol.cpp), recovered from
+its points in tests/golden/sobol.npz (valid for point indices below 2^24).
+Normals: CUDA's FP64 normcdfinv against the oracle's quantile, a few ulps.
+Prices: the FP64 pipeline on identical normals, 1e-12 relative."""
+import os
+
+import numpy as np
+import pytest
+
+from tests._golden import rel_err
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "sobol.npz")
+NORMAL_TOL = 2e-14  # absolute, |z| < 9.1 on Sobol' points
+PRICE_TOL = 1e-12
+STAT_TOL = 1e-8
+
+GRID = dict(xi=0.04, H=[0.05, 0.1, 0.1, 0.3], eta=[1.0, 1.5, 1.5, 2.5], rho=[-0.95, -0.7, -0.5, -0.7],
+            T=[0.25, 0.5, 1.0, 2.0], K=[0.9, 1.1, 1.0, 0.8])
+
+
+@pytest.fixture(scope="module")
+def R():
+    import rbergomi_gb300 as R
+    R.lib()
+    return R
+
+
+@pytest.fixture(scope="module")
+def V(oracle):
+    return oracle.sobol_directions_from_points(np.load(GOLD)["gray_points"])
+
+
+@pytest.mark.parametrize("N,M,off,bridge", [(64, 3000, 0, False), (37, 1000, 12345, False), (64, 2000, 777, True),
+                                            (1, 50, 0, True), (512, 300, 99, True)])
+def test_normals_match_oracle(R, oracle, V, N, M, off, bridge):
+    Z = R.sobol_normals(V, N, M, path_offset=off, bridge=bridge)
+    Zo = oracle.sobol_normals(V, N, M, path0=off, bridge=bridge)
+    assert np.max(np.abs(Z - Zo)) < NORMAL_TOL * (4 if bridge else 1)
+
+
+def test_normals_offset_is_a_suffix(R, V):
+    a = R.sobol_normals(V, 32, 150)
+    b = R.sobol_normals(V, 32, 100, path_offset=50)
+    np.testing.assert_array_equal(a[50:], b)
+
+
+@pytest.mark.parametrize("N,M,bridge", [(64, 4096, False), (64, 4096, True), (100, 2500, False)])
+def test_prices_match_oracle_on_identical_normals(R, oracle, V, N, M, bridge):
+    g = GRID
+    price, stat, iv = R.price_rt_sobol(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, V, bridge=bridge)
+    Z = oracle.sobol_normals(V, N, M, bridge=bridge)
+    op, os_ = oracle.reduce(oracle.payoffs_rt(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], Z))
+    assert np.all(rel_err(price, op) < PRICE_TOL)
+    assert np.all(rel_err(stat, os_) < STAT_TOL)
+    O = len(g["T"])
+    ivo = np.array([oracle.iv_call(p, g["K"][i % O], g["T"][i % O]) for i, p in enumerate(op)])
+    ok = ~np.isnan(ivo)
+    assert np.all(rel_err(iv[ok], ivo[ok]) < 1e-10)
+
+
+def test_qmc_agrees_with_monte_carlo(R, V):
+    """The QMC estimate (point set 1..2^16) and a 2^21-path Philox estimate of
+    the same prices agree within 4 combined standard errors (the QMC run's
+    `stat`, the Monte Carlo formula the reference reports, bounds its error
+    from above)."""
+    args = (0.04, [0.1], [1.5], [-0.7], [0.5, 1.0], [1.0, 1.1], 128)
+    pq, sq, _ = R.price_rt_sobol(*args, 1 << 16, V)
+    pm, sm, _ = R.price_rt(*args, 1 << 21, seed=3, precision=R.FP64)
+    assert np.all(np.abs(pq - pm) < 4 * np.hypot(sq, sm))
+
+
+def test_rejects_bad_requests(R, V):
+    args = (0.04, [0.1], [1.5], [-0.7], [1.0], [1.0])
+    with pytest.raises(R.RbgError, match="fewer than 2N"):
+        R.price_rt_sobol(*args, 600, 16, V)       # 1111 dimensions < 1200
+    with pytest.raises(R.RbgError, match="power of two"):
+        R.price_rt_sobol(*args, 48, 16, V, bridge=True)
+    with pytest.raises(R.RbgError, match="fewer than 2N"):
+        R.sobol_normals(V[:10], 8, 4)
