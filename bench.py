@@ -374,7 +374,8 @@ def run_grid(args):
 
 
 def run_sobol(args):
-    """Sobol' quasi-Monte Carlo RT pricing, FP64 form (rbg_price_rt_sobol):
+    """Sobol' quasi-Monte Carlo RT pricing, FP64 form (rbg_price_rt_sobol; the
+    mixed form on the same points is timed beside it as mixed_value):
     H=0.1, eta=1.9, rho=-0.9, xi=0.235^2, T=1, 21 strikes on [0.6, 1.4], N=256
     (512 Sobol' dimensions), M = 2^20 points.  Direction integers: the
     reference generator's own (rBergomi/sobol.cpp), recovered from its points
@@ -414,6 +415,7 @@ def run_sobol(args):
     launches = R.launch_count() - n0
     ms_b, (pb, _, _) = timed(lambda: R.price_rt_sobol(*a, V, bridge=True, stream=stream.cuda_stream))
     ms_p, (pp, sp, _) = timed(lambda: R.price_rt(*a, seed=11, precision=R.FP64, stream=stream.cuda_stream))
+    ms_m, (pm, _, _) = timed(lambda: R.price_rt_sobol(*a, V, precision=R.MIXED, stream=stream.cuda_stream))
     print(json.dumps({
         "metric": METRIC, "value": M * N / (ms / 1e3), "unit": "path-steps/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -421,6 +423,7 @@ def run_sobol(args):
         "config": {"workload": "sobol-fp64-n256-m1m", "N": N, "M": M, "strikes": 21, "dims": 2 * N,
                    "l2": "flushed (256 MiB write) before each step"},
         "bridge_value": M * N / (ms_b / 1e3), "philox_fp64_value": M * N / (ms_p / 1e3),
+        "mixed_value": M * N / (ms_m / 1e3), "max_rel_diff_mixed_vs_fp64_qmc": float(np.max(np.abs(pm - pq) / pq)),
         "max_abs_diff_qmc_vs_philox": float(np.max(np.abs(pq - pp))), "philox_stat_max": float(np.max(sp)),
         "max_abs_diff_bridge_vs_plain_qmc": float(np.max(np.abs(pb - pq))),
         "clocks": clk.summary(), "gpu_launches": launches,

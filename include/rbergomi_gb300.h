@@ -232,9 +232,11 @@ int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, 
  * The reference has no C export for these; this is the replacement for
  * linking its C++ functions. */
 
-/* RT prices over Sobol' normals, FP64 form (o->precision == RBG_FP64); the
- * seed is unused, o->path_offset shifts the point range.  stat is the
- * reference's Monte Carlo formula applied to the QMC sample. */
+/* RT prices over Sobol' normals; the seed is unused, o->path_offset shifts
+ * the point range.  stat is the reference's Monte Carlo formula applied to
+ * the QMC sample.  o->precision == RBG_FP64: the FP64 form (normcdfinv),
+ * bridge allowed.  RBG_MIXED: the tensor-core form on the same points (FP32
+ * quantile, GEMM backend: N <= 1024), no bridge, point indices below 2^32. */
 int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t* directions, int dims, int bridge,
                        double* price, double* stat, double* iv);
 /* The Sobol' normals those prices use: M*2*N doubles in the quadrature

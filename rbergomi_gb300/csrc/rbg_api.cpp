@@ -136,11 +136,12 @@ struct Ctx {
     int dev = -1;
     cudaStream_t stream = nullptr;
     std::mutex mu;
-    DevBuf z, ivb, ivp, part, acc, tabs, res, pay, mixed_ws, cv, sobol;
+    DevBuf z, ivb, ivp, part, acc, tabs, res, pay, mixed_ws, cv, sobol, sobol32;
     // host images of what `tabs`, `mixed_ws` and `sobol` hold, so that a call
     // with the same tables (a calibration loop, a benchmark) uploads nothing
     std::vector<unsigned char> tabs_img, mixed_img;
     std::vector<unsigned long long> sobol_img;
+    std::vector<unsigned int> sobol32_img;
     ~Ctx() {}
 };
 
@@ -306,8 +307,10 @@ static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M,
 
 // Mixed form: tcgen05 fused path kernel writes FP32 (Ivdt, IsvdW) per
 // (variance group, path); the FP64 payoff/sum kernels finish.
+// sob: Sobol' normals (device table [32][2N], bits 30..61 of the direction
+// integers; GEMM backend, RT) instead of the Philox stream.
 static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M, cudaStream_t st,
-                       double* host_res, bool mc = false)
+                       double* host_res, bool mc = false, const unsigned int* sob = nullptr)
 {
     TableSet ts;
     int rc = upload_tables(c, plan, st, ts);
@@ -315,6 +318,9 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
     const int no = (int)plan.outs.size();
     MixedJob job;
     if ((rc = mixed_prepare(plan, o, M, job, g_err, 0, mc))) return rc;
+    job.sob = sob;
+    if (sob && job.backend != RBG_CONV_GEMM)
+        return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend (N <= 1024)");
     const int64_t B = job.batch;
     if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
     const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
@@ -730,12 +736,43 @@ int rbg_sobol_normals(const uint64_t* directions, int dims, int N, int64_t M, in
     return RBG_OK;
 }
 
+// Mixed form: the table's bits 30..61 as uint32 [32][2N] (points below 2^32),
+// kept on the device like the FP64 table.
+static int sobol32_setup(Ctx& c, const uint64_t* dirs, int dims, int N, int64_t path_offset, int64_t M,
+                         cudaStream_t st)
+{
+    if (!dirs) return fail(RBG_ERR_ARG, "null Sobol' direction table");
+    if (N < 1 || M < 1 || path_offset < 0) return fail(RBG_ERR_ARG, "bad sizes");
+    if (dims < 2 * N) return fail(RBG_ERR_ARG, "the Sobol' direction table has fewer than 2N dimensions");
+    if ((uint64_t)path_offset + (uint64_t)M + 128 >= ((uint64_t)1 << 32))
+        return fail(RBG_ERR_ARG, "Sobol' point index beyond 2^32 in the mixed form");
+    const int D = 2 * N;
+    std::vector<unsigned int> img((size_t)32 * D);
+    for (int k = 0; k < 32; ++k)
+        for (int d = 0; d < D; ++d) img[(size_t)k * D + d] = (unsigned int)(dirs[(size_t)d * kSobolBits + k] >> 30);
+    if (img != c.sobol32_img) {
+        int rc = ensure(c.sobol32, sizeof(unsigned int) * img.size(), "Sobol' table");
+        if (rc) return rc;
+        c.sobol32_img.clear();
+        RBG_CUDA(cudaMemcpyAsync(c.sobol32.p, img.data(), sizeof(unsigned int) * img.size(), cudaMemcpyHostToDevice,
+                                 st));
+        RBG_CUDA(cudaStreamSynchronize(st));
+        g_h2d += sizeof(unsigned int) * img.size();
+        c.sobol32_img.swap(img);
+    }
+    return RBG_OK;
+}
+
 int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t* directions, int dims, int bridge,
                        double* price, double* stat, double* iv)
 {
     if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
-    if (o->precision != RBG_FP64) return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals run in the FP64 form");
-    if (o->conv == RBG_CONV_GEMM || o->conv == RBG_CONV_FFT)
+    if (o->precision != RBG_FP64 && o->precision != RBG_MIXED) return fail(RBG_ERR_ARG, "unknown precision");
+    if (o->precision == RBG_MIXED && bridge)
+        return fail(RBG_ERR_UNSUPPORTED, "the Brownian bridge runs in the FP64 form only");
+    if (o->precision == RBG_MIXED && o->conv == RBG_CONV_FFT)
+        return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend (N <= 1024)");
+    if (o->precision == RBG_FP64 && (o->conv == RBG_CONV_GEMM || o->conv == RBG_CONV_FFT))
         return fail(RBG_ERR_UNSUPPORTED, "FP64 form uses the direct Volterra sum");
     g_h2d = g_d2h = 0;
     Plan plan;
@@ -746,12 +783,17 @@ int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
-    SobolBridge br{};
-    if ((rc = sobol_setup(*c, directions, dims, plan.N, bridge, o->path_offset, p->M, st, br))) return rc;
     std::vector<double> res(5 * plan.outs.size(), 0.0);
-    if ((rc = price_fp64(*c, plan, *o, p->M, st, res.data(), false, c->sobol.as<unsigned long long>(),
-                         bridge ? &br : nullptr)))
-        return rc;
+    if (o->precision == RBG_MIXED) {
+        if ((rc = sobol32_setup(*c, directions, dims, plan.N, o->path_offset, p->M, st))) return rc;
+        if ((rc = price_mixed(*c, plan, *o, p->M, st, res.data(), false, c->sobol32.as<unsigned int>()))) return rc;
+    } else {
+        SobolBridge br{};
+        if ((rc = sobol_setup(*c, directions, dims, plan.N, bridge, o->path_offset, p->M, st, br))) return rc;
+        if ((rc = price_fp64(*c, plan, *o, p->M, st, res.data(), false, c->sobol.as<unsigned long long>(),
+                             bridge ? &br : nullptr)))
+            return rc;
+    }
     const size_t no = plan.outs.size();
     if (price) std::memcpy(price, res.data(), no * sizeof(double));
     if (stat) std::memcpy(stat, res.data() + no, no * sizeof(double));

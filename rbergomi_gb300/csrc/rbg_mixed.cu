@@ -421,10 +421,90 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
     }
 }
 
+// Sobol' quasi-Monte Carlo normal in FP32 from the top 32 bits q of a
+// coordinate (x = q 2^-32): the quantile of the lower tail u = min(x, 1 - x),
+// so points near 1 keep their relative precision; sign restored after.  The
+// tail count 2^32 - q is formed in 64 bits: written as the 32-bit
+// `up ? 0u - q : q` it is the integer absolute-value idiom, which the
+// compiler turns into a signed abs that reads q = 2^31 (x = 1/2) as -2^31.
+__device__ __forceinline__ float sobol_normal_f32(unsigned int q)
+{
+    const bool up = q >= 0x80000000u;
+    const unsigned long long r = up ? (1ull << 32) - q : (unsigned long long)q;
+    const float z = normcdfinvf(__ull2float_rn(r) * 0x1p-32f);
+    return up ? -z : z;
+}
+
+// Sobol' producer (RT, rbg_price_rt_sobol in the mixed form): warp w of the
+// producers draws paths 16 w .. 16 w + 15 of the tile and lane l step
+// j = 32 c + l, i.e. coordinates 2 j (W1) and 2 j + 1 (W1perp) of the
+// paths' points path0 + m + 1 (rBergomi/rBergomiMT.cpp:669-670 with breakZ).
+// The first point comes from its Gray code, the next 15 by one XOR each
+// (point s + 1 = point s ^ v[ctz(s + 1)]).  a.sob holds bits 30..61 of the
+// direction integers, [32][2N] uint32.  Writes the FP32 W1 / W1perp tiles and
+// the 16-bit hi/lo A tile (REDRAW: W1 and the A tile only).
+template <int BF16, bool REDRAW>
+__device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t tile, int c, int n0, unsigned char* st,
+                                                    float* w1s)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int N = a.N, Np = a.Np;
+    const int j = kChunk * c + lane;
+    const bool jin = j < N;
+    const int64_t m0 = tile * kTileM + 16 * w;
+    const unsigned long long s0 = (unsigned long long)(a.path0 + m0) + 1ull;
+    const uint2* tab = reinterpret_cast<const uint2*>(a.sob);  // [32][N] coordinate pairs
+    unsigned int q0 = 0, q1 = 0;
+    if (jin) {
+        for (unsigned long long g = s0 ^ (s0 >> 1); g; g &= g - 1) {
+            const uint2 v = __ldg(tab + (size_t)(__ffsll((long long)g) - 1) * N + j);
+            q0 ^= v.x;
+            q1 ^= v.y;
+        }
+    }
+    float* w1ps = w1s + kFW1p;
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+        const int p = 16 * w + i;
+        const int64_t m = m0 + i;
+        const bool ok = jin && m < a.B;
+        const float z0 = ok ? sobol_normal_f32(q0) : 0.f;
+        const float z1 = (ok && !REDRAW) ? sobol_normal_f32(q1) : 0.f;
+        if (!REDRAW) {
+            w1s[ftile_at(p, lane)] = z0;
+            w1ps[ftile_at(p, lane)] = z1;
+            if (a.dbg_w && m < a.B) {
+                a.dbg_w[(m * 2 + 0) * Np + j] = z0;
+                a.dbg_w[(m * 2 + 1) * Np + j] = z1;
+            }
+        }
+        uint32_t hi, lo;
+        split2<BF16>(z0, 0.f, hi, lo);
+        const int off = p * 64 + ((((lane >> 3)) ^ ((p >> 1) & 3)) << 4) + ((lane & 7) << 1);
+        *(unsigned short*)(st + off) = (unsigned short)hi;
+        *(unsigned short*)(st + kTileBytes + off) = (unsigned short)lo;
+        if (jin && i < 15) {
+            const uint2 v = __ldg(tab + (size_t)(__ffsll((long long)(s0 + i + 1)) - 1) * N + j);
+            q0 ^= v.x;
+            q1 ^= v.y;
+        }
+    }
+    // last chunk of the first pass: W1 at step 32 n0 for the boundary row
+    if (!REDRAW && c == n0 - 1 && lane < 16) {
+        const int p = 16 * w + lane, jb = kChunk * n0;
+        const unsigned long long sb = s0 + lane;
+        unsigned int q = 0;
+        for (unsigned long long g = sb ^ (sb >> 1); g; g &= g - 1)
+            q ^= __ldg(a.sob + (size_t)(__ffsll((long long)g) - 1) * 2 * N + 2 * jb);
+        w1s[kFBnd + p] = (m0 + lane < a.B && jb < N) ? sobol_normal_f32(q) : 0.f;
+    }
+}
+
 // TWO: two TMEM passes per tile (512 < Np <= 1024).  The one-pass
 // instantiation has n0 = 0 at compile time, so the virtual-chunk bookkeeping
 // folds away there.
-template <int BF16, bool TWO, bool MC>
+// SOB: Sobol' normals (produce_chunk_sobol) instead of Philox; RT only.
+template <int BF16, bool TWO, bool MC, bool SOB = false>
 __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
     constexpr int NS = MC ? 3 : 2;  // normal streams per path = sums per variance group
@@ -507,10 +587,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
                 unsigned char* st = base + L.a0 + s * kStageA;
                 float* w1s = (float*)(base + L.f0 + s * kStageFB);
-                if (TWO && redraw)
+                if (SOB) {
+                    if (TWO && redraw)
+                        produce_chunk_sobol<BF16, true>(a, tile, c, n0, st, w1s);
+                    else
+                        produce_chunk_sobol<BF16, false>(a, tile, c, n0, st, w1s);
+                } else if (TWO && redraw) {
                     produce_chunk<BF16, true, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
-                else
+                } else {
                     produce_chunk<BF16, false, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+                }
                 fence_proxy_async();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(full + s));
@@ -1102,8 +1188,10 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     }
     // fuse the payoffs into the GEMM path kernel when every launch has few outputs
     // Pricing the payoffs inside the path kernel's epilogue (RBG_FUSE_PAYOFFS)
-    // measured slower than the separate FP32 payoff kernel on GB300: the
-    // epilogue warps are the kernel's critical path.
+    // measured slower than the separate FP32 payoff kernel on GB300 (6.84
+    // against 6.14 ms per step at N = 512, 2^22 paths, 21 strikes): the
+    // per-path Black-Scholes evaluations take issue slots the producer warps,
+    // which set the kernel's pace, need.
     job.fused = RBG_FUSE_PAYOFFS && (backend == RBG_CONV_GEMM) && !mc;
     for (const MixedLaunch& r : job.launches)
         if (r.args.n_o > kMixedMaxFused || smem_layout(Np, 2, r.args.n_g, r.args.n_o).total > optin)
@@ -1190,6 +1278,10 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         err = "plain Monte Carlo launch without an IsvdWp buffer";
         return RBG_ERR_ARG;
     }
+    if (job.sob && (job.mc || job.backend != RBG_CONV_GEMM)) {
+        err = "Sobol' normals in the mixed form need the RT estimator and the GEMM backend";
+        return RBG_ERR_UNSUPPORTED;
+    }
     unsigned char* base = (unsigned char*)ws;
     for (const MixedLaunch& r : job.launches) {
         MixedArgs A = r.args;
@@ -1209,6 +1301,7 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         A.err = (unsigned int*)(base + job.off_err);
         A.dbg_w = dbg_w;
         A.dbg_x = dbg_x;
+        A.sob = job.sob;
         A.seed = seed;
         A.path0 = path0;
         A.B = B;
@@ -1221,7 +1314,11 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         } else {
             void (*kern)(MixedArgs);
             const bool two = A.n0 > 0;
-            if (job.split == RBG_SPLIT_BF16X3)
+            if (job.sob && job.split == RBG_SPLIT_BF16X3)
+                kern = two ? k_mixed_gemm<1, true, false, true> : k_mixed_gemm<1, false, false, true>;
+            else if (job.sob)
+                kern = two ? k_mixed_gemm<0, true, false, true> : k_mixed_gemm<0, false, false, true>;
+            else if (job.split == RBG_SPLIT_BF16X3)
                 kern = job.mc ? (two ? k_mixed_gemm<1, true, true> : k_mixed_gemm<1, false, true>)
                               : (two ? k_mixed_gemm<1, true, false> : k_mixed_gemm<1, false, false>);
             else

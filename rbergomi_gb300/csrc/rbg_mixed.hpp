@@ -31,6 +31,7 @@ struct MixedArgs {
     unsigned long long* prof;    // diagnostic runs only: wait cycles per site, busy cycles per role
     const float2* spec;          // FFT backend: FFT(Gamma)/L, L points
     const float2* tw;            // FFT backend: exp(-2 pi i t / L), L points
+    const unsigned int* sob;     // Sobol' normals (GEMM backend, RT): [32][2N] bits 30..61 of the direction integers
     uint64_t seed;
     int64_t path0, B;
     int N, Np, nc, n_g, g0, tmem_cols, stages;
@@ -56,6 +57,7 @@ struct MixedJob {
     int backend = RBG_CONV_GEMM;  // RBG_CONV_GEMM or RBG_CONV_FFT
     bool fused = false;           // payoffs priced inside the path kernel (GEMM backend, <= 64 per launch)
     bool mc = false;              // plain Monte Carlo: third normal stream Wperp and IsvdWp per (group, path)
+    const unsigned int* sob = nullptr;  // Sobol' table on the device (set by the caller): QMC normals, not Philox
     size_t off_tw = 0;
     std::vector<MixedLaunch> launches;   // one per (Volterra pass, <= 16 groups)
     std::vector<const void*> table_dev;  // optional device copies of each launch's strip / spectrum

@@ -98,11 +98,14 @@ def test_live_reference_generator(oracle, V):
         np.testing.assert_array_equal(oracle.hier(z), oracle.qmc_ref_hier(z))
 
 
-def test_sobol_entry_rejects_mixed_precision():
+def test_sobol_entry_rejects_unsupported_forms():
     import rbergomi_gb300 as R
 
     V = np.zeros((8, 62), np.uint64)
-    with pytest.raises(R.RbgError, match="FP64"):
-        R.price_rt_sobol(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 4, 16, V, precision=R.MIXED)
+    a = (0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 4, 16, V)
+    with pytest.raises(R.RbgError, match="FP64 form only"):
+        R.price_rt_sobol(*a, bridge=True, precision=R.MIXED)
+    with pytest.raises(R.RbgError, match="GEMM backend"):
+        R.price_rt_sobol(*a, precision=R.MIXED, conv=R.CONV_FFT)
     with pytest.raises(ValueError):
         R.price_rt_sobol(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 4, 16, np.zeros((8, 63), np.uint64))

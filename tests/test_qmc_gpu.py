@@ -73,6 +73,31 @@ def test_qmc_agrees_with_monte_carlo(R, V):
     assert np.all(np.abs(pq - pm) < 4 * np.hypot(sq, sm))
 
 
+@pytest.mark.parametrize("N,M", [(37, 3001), (512, 20000), (544, 8192)])
+def test_mixed_form_matches_fp64_form(R, V, N, M):
+    """The tensor-core form on the same Sobol' points (FP32 quantile, BF16x3
+    Volterra GEMM, one and two TMEM passes): within 1e-4 relative and 0.2
+    standard errors of the FP64 form, the mixed form's bound on Philox normals."""
+    g = GRID
+    a = (g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, V)
+    p64, s64, _ = R.price_rt_sobol(*a, precision=R.FP64)
+    p32, s32, _ = R.price_rt_sobol(*a, precision=R.MIXED)
+    assert np.all(rel_err(p32, p64) < 1e-4)
+    assert np.all(np.abs(p32 - p64) < 0.2 * s64)
+    assert np.all(rel_err(s32, s64) < 1e-3)
+
+
+def test_mixed_form_path_offset(R, V):
+    """Shifting the point range moves the QMC estimate; the same shifted
+    range in the FP64 form agrees."""
+    a = (0.04, [0.1], [1.5], [-0.7], [1.0, 1.0], [1.0, 1.2], 64, 5000, V)
+    p0, _, _ = R.price_rt_sobol(*a, precision=R.MIXED)
+    p1, s1, _ = R.price_rt_sobol(*a, precision=R.MIXED, path_offset=100000)
+    q1, _, _ = R.price_rt_sobol(*a, precision=R.FP64, path_offset=100000)
+    assert np.all(p0 != p1)
+    assert np.all(np.abs(p1 - q1) < 0.2 * s1)
+
+
 def test_rejects_bad_requests(R, V):
     args = (0.04, [0.1], [1.5], [-0.7], [1.0], [1.0])
     with pytest.raises(R.RbgError, match="fewer than 2N"):
