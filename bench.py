@@ -416,6 +416,7 @@ def run_sobol(args):
     ms_b, (pb, _, _) = timed(lambda: R.price_rt_sobol(*a, V, bridge=True, stream=stream.cuda_stream))
     ms_p, (pp, sp, _) = timed(lambda: R.price_rt(*a, seed=11, precision=R.FP64, stream=stream.cuda_stream))
     ms_m, (pm, _, _) = timed(lambda: R.price_rt_sobol(*a, V, precision=R.MIXED, stream=stream.cuda_stream))
+    ms_pm, _ = timed(lambda: R.price_rt(*a, seed=11, precision=R.MIXED, stream=stream.cuda_stream))
     print(json.dumps({
         "metric": METRIC, "value": M * N / (ms / 1e3), "unit": "path-steps/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -424,6 +425,7 @@ def run_sobol(args):
                    "l2": "flushed (256 MiB write) before each step"},
         "bridge_value": M * N / (ms_b / 1e3), "philox_fp64_value": M * N / (ms_p / 1e3),
         "mixed_value": M * N / (ms_m / 1e3), "max_rel_diff_mixed_vs_fp64_qmc": float(np.max(np.abs(pm - pq) / pq)),
+        "philox_mixed_value": M * N / (ms_pm / 1e3),
         "max_abs_diff_qmc_vs_philox": float(np.max(np.abs(pq - pp))), "philox_stat_max": float(np.max(sp)),
         "max_abs_diff_bridge_vs_plain_qmc": float(np.max(np.abs(pb - pq))),
         "clocks": clk.summary(), "gpu_launches": launches,

@@ -240,9 +240,11 @@ int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, 
 int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t* directions, int dims, int bridge,
                        double* price, double* stat, double* iv);
 /* The Sobol' normals those prices use: M*2*N doubles in the quadrature
- * layout, host pointer. */
+ * layout, host pointer.  precision RBG_FP64: normcdfinv of the 62-bit point;
+ * RBG_MIXED: the mixed form's FP32 normals (top 32 bits of the point, FP32
+ * quantile), widened exactly to double (no bridge). */
 int rbg_sobol_normals(const uint64_t* directions, int dims, int N, int64_t M, int64_t path_offset, int bridge,
-                      double* Z);
+                      int precision, double* Z);
 
 /* Implied vols of call prices (S0 = 1, r = 0) on the GPU; NaN where no
  * volatility reproduces the price. */

@@ -103,7 +103,7 @@ def lib():
         L.rbg_payoffs_mc.restype = C.c_int
         L.rbg_generate_normals_streams.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_int, _dp]
         L.rbg_price_rt_sobol.argtypes = [P, O, _u64p, C.c_int, C.c_int, _dp, _dp, _dp]
-        L.rbg_sobol_normals.argtypes = [_u64p, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int, _dp]
+        L.rbg_sobol_normals.argtypes = [_u64p, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int, C.c_int, _dp]
         L.rbg_generate_normals_streams.restype = C.c_int
         L.rbg_generate_normals.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int, C.c_int, _dp]
         L.rbg_generate_normals.restype = C.c_int
@@ -353,17 +353,18 @@ def sobol_directions_from_points(points) -> np.ndarray:
     return V
 
 
-def sobol_normals(directions, N, M, path_offset=0, bridge=False) -> np.ndarray:
+def sobol_normals(directions, N, M, path_offset=0, bridge=False, precision=FP64) -> np.ndarray:
     """Sobol' quasi-Monte Carlo normals [M, 2, N] (rBergomi/qmc.cpp
     normalQMC_sample + breakZ): path m takes point path_offset + m + 1.
     directions: [dims, 62] direction integers (coordinate d of point s is the
     XOR of directions[d, k] over the set bits k of s ^ (s >> 1), times 2^-62).
     bridge: Brownian-bridge map of each stream (rBergomi/aux.h
-    hierarchical2increments; N a power of two)."""
+    hierarchical2increments; N a power of two).  precision=MIXED: the mixed
+    form's FP32 normals, widened to double."""
     V = _sobol_table(directions)
     Z = np.empty((M, 2, N))
     _check(lib().rbg_sobol_normals(V.ctypes.data_as(C.POINTER(C.c_uint64)), V.shape[0], int(N), int(M),
-                                   int(path_offset), int(bool(bridge)), Z.ctypes.data_as(_dp)))
+                                   int(path_offset), int(bool(bridge)), int(precision), Z.ctypes.data_as(_dp)))
     return Z
 
 

@@ -712,9 +712,14 @@ static int sobol_setup(Ctx& c, const uint64_t* dirs, int dims, int N, int bridge
 }
 
 int rbg_sobol_normals(const uint64_t* directions, int dims, int N, int64_t M, int64_t path_offset, int bridge,
-                      double* Z)
+                      int precision, double* Z)
 {
     if (!Z) return fail(RBG_ERR_ARG, "null output");
+    if (precision != RBG_FP64 && precision != RBG_MIXED) return fail(RBG_ERR_ARG, "unknown precision");
+    if (precision == RBG_MIXED && bridge)
+        return fail(RBG_ERR_UNSUPPORTED, "the Brownian bridge runs in the FP64 form only");
+    if (precision == RBG_MIXED && (uint64_t)path_offset + (uint64_t)M + 128 >= ((uint64_t)1 << 32))
+        return fail(RBG_ERR_ARG, "Sobol' point index beyond 2^32 in the mixed form");
     Ctx* c = nullptr;
     int rc = get_ctx(&c);
     if (rc) return rc;
@@ -726,7 +731,7 @@ int rbg_sobol_normals(const uint64_t* directions, int dims, int N, int64_t M, in
     for (int64_t m0 = 0; m0 < M; m0 += B) {
         const int64_t b = std::min(B, M - m0);
         if (launch_sobol_normals(c->sobol.as<unsigned long long>(), N, (uint64_t)(path_offset + m0 + 1), b,
-                                 bridge ? &br : nullptr, c->z.as<double>(), c->stream))
+                                 bridge ? &br : nullptr, c->z.as<double>(), c->stream, precision == RBG_MIXED))
             return fail(RBG_ERR_UNSUPPORTED, "Brownian bridge shared memory not available for this N");
         RBG_CUDA(cudaGetLastError());
         RBG_CUDA(cudaMemcpyAsync(Z + m0 * 2 * N, c->z.p, sizeof(double) * 2 * N * b, cudaMemcpyDeviceToHost,

@@ -78,6 +78,49 @@ __device__ __forceinline__ void sincos_approx(float x, float& s, float& c)
     asm("cos.approx.ftz.f32 %0, %1;" : "=f"(c) : "f"(x));
 }
 
+// Standard normal quantile of u in (0, 1/2] in FP32 (the mixed form's Sobol'
+// normals).  The form of M. Giles, "Approximating the erfinv function" (GPU
+// Computing Gems, Jade Edition, 2011): Phi^-1(u) = sqrt(2) x P(w) with
+// x = 2u - 1 and w = -ln(1 - x^2) = -ln(4u(1 - u)); P is a degree-8
+// polynomial in w - 2.5 for w < 5 and in sqrt(w) - 3 above.  The coefficients
+// were fitted for this library (weighted least squares on the relative error
+// against double-precision erfinv, w in [0, 5) and [5, 22.5], i.e. u down to
+// 2^-32): relative error <= 6e-7 of the exact quantile of the FP32 input.
+__device__ __forceinline__ float normal_quantile_lower_f32(float u)
+{
+    const float x = fmaf(2.f, u, -1.f);
+    const float w = -0.693147181f * lg2_approx(4.f * u * (1.f - u));
+    float p;
+    if (w < 5.f) {
+        const float t = w - 2.5f;
+        const float c[9] = {2.853470238e-8f, 3.437269397e-7f, -3.528858501e-6f, -4.396779949e-6f, 2.186021901e-4f, -1.253707519e-3f, -4.177707740e-3f, 2.466407261e-1f, 1.501409422e+0f};
+        p = c[0];
+#pragma unroll
+        for (int i = 1; i < 9; ++i) p = fmaf(p, t, c[i]);
+    } else {
+        const float s = sqrt_approx(w) - 3.f;
+        const float c[9] = {-8.581864353e-6f, -1.442782343e-4f, 1.150858774e-3f, -3.388356747e-3f, 5.807593624e-3f, -7.720514824e-3f, 9.428526195e-3f, 1.001682603e+0f, 2.832977331e+0f};
+        p = c[0];
+#pragma unroll
+        for (int i = 1; i < 9; ++i) p = fmaf(p, s, c[i]);
+    }
+    return 1.41421356f * x * p;
+}
+
+// Sobol' normal in FP32 from the top 32 bits q of a coordinate (x = q 2^-32):
+// the quantile of the lower tail u = min(x, 1 - x), so points near 1 keep
+// their relative precision; sign restored after.  The tail count 2^32 - q is
+// formed in 64 bits: written as the 32-bit `up ? 0u - q : q` it is the
+// integer absolute-value idiom, which the compiler turns into a signed abs
+// that reads q = 2^31 (x = 1/2) as -2^31.
+__device__ __forceinline__ float sobol_normal_f32(unsigned int q)
+{
+    const bool up = q >= 0x80000000u;
+    const unsigned long long r = up ? (1ull << 32) - q : (unsigned long long)q;
+    const float z = normal_quantile_lower_f32(__ull2float_rn(r) * 0x1p-32f);
+    return up ? -z : z;
+}
+
 // FP64 Box-Muller on uniforms (x + 1/2) 2^-32.
 __device__ __forceinline__ void box_muller_f64(uint32_t a, uint32_t b, double& z0, double& z1)
 {

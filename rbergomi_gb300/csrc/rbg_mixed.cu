@@ -421,28 +421,18 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
     }
 }
 
-// Sobol' quasi-Monte Carlo normal in FP32 from the top 32 bits q of a
-// coordinate (x = q 2^-32): the quantile of the lower tail u = min(x, 1 - x),
-// so points near 1 keep their relative precision; sign restored after.  The
-// tail count 2^32 - q is formed in 64 bits: written as the 32-bit
-// `up ? 0u - q : q` it is the integer absolute-value idiom, which the
-// compiler turns into a signed abs that reads q = 2^31 (x = 1/2) as -2^31.
-__device__ __forceinline__ float sobol_normal_f32(unsigned int q)
-{
-    const bool up = q >= 0x80000000u;
-    const unsigned long long r = up ? (1ull << 32) - q : (unsigned long long)q;
-    const float z = normcdfinvf(__ull2float_rn(r) * 0x1p-32f);
-    return up ? -z : z;
-}
-
 // Sobol' producer (RT, rbg_price_rt_sobol in the mixed form): warp w of the
 // producers draws paths 16 w .. 16 w + 15 of the tile and lane l step
 // j = 32 c + l, i.e. coordinates 2 j (W1) and 2 j + 1 (W1perp) of the
 // paths' points path0 + m + 1 (rBergomi/rBergomiMT.cpp:669-670 with breakZ).
 // The first point comes from its Gray code, the next 15 by one XOR each
 // (point s + 1 = point s ^ v[ctz(s + 1)]).  a.sob holds bits 30..61 of the
-// direction integers, [32][2N] uint32.  Writes the FP32 W1 / W1perp tiles and
-// the 16-bit hi/lo A tile (REDRAW: W1 and the A tile only).
+// direction integers, [32][2N] uint32 (point indices below 2^32).  Table
+// reads are issued independently of the XORs that use them: the Gray-code
+// rows as one unrolled predicated batch, and the walk's rows up front (15
+// consecutive indices have ctz <= 3 except at most one multiple of 16).
+// Writes the FP32 W1 / W1perp tiles and the 16-bit hi/lo A tile (REDRAW: W1
+// and the A tile only).
 template <int BF16, bool REDRAW>
 __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t tile, int c, int n0, unsigned char* st,
                                                     float* w1s)
@@ -455,12 +445,22 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
     const unsigned long long s0 = (unsigned long long)(a.path0 + m0) + 1ull;
     const uint2* tab = reinterpret_cast<const uint2*>(a.sob);  // [32][N] coordinate pairs
     unsigned int q0 = 0, q1 = 0;
+    uint2 r[4] = {}, rb = {};  // the walk's rows 0..3 and the row of the one multiple of 16 in (s0, s0 + 15]
+    const unsigned long long m16 = ((s0 >> 4) + 1) << 4;
+    const bool has16 = m16 <= s0 + 15;
     if (jin) {
-        for (unsigned long long g = s0 ^ (s0 >> 1); g; g &= g - 1) {
-            const uint2 v = __ldg(tab + (size_t)(__ffsll((long long)g) - 1) * N + j);
-            q0 ^= v.x;
-            q1 ^= v.y;
+        const unsigned long long g = s0 ^ (s0 >> 1);  // point indices stay below 2^32
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            if ((g >> k) & 1ull) {
+                const uint2 v = __ldg(tab + (size_t)k * N + j);
+                q0 ^= v.x;
+                q1 ^= v.y;
+            }
         }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) r[k] = __ldg(tab + (size_t)k * N + j);
+        if (has16) rb = __ldg(tab + (size_t)(__ffsll((long long)m16) - 1) * N + j);
     }
     float* w1ps = w1s + kFW1p;
 #pragma unroll 4
@@ -483,8 +483,9 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
         const int off = p * 64 + ((((lane >> 3)) ^ ((p >> 1) & 3)) << 4) + ((lane & 7) << 1);
         *(unsigned short*)(st + off) = (unsigned short)hi;
         *(unsigned short*)(st + kTileBytes + off) = (unsigned short)lo;
-        if (jin && i < 15) {
-            const uint2 v = __ldg(tab + (size_t)(__ffsll((long long)(s0 + i + 1)) - 1) * N + j);
+        if (i < 15) {
+            const int k = __ffsll((long long)(s0 + i + 1)) - 1;
+            const uint2 v = k == 0 ? r[0] : k == 1 ? r[1] : k == 2 ? r[2] : k == 3 ? r[3] : rb;
             q0 ^= v.x;
             q1 ^= v.y;
         }

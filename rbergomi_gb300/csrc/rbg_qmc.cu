@@ -19,15 +19,17 @@
 
 #include <cmath>
 
+#include "rbg_device.cuh"
 #include "rbg_internal.hpp"
 
 namespace rbg {
 
-// coordinates 2j and 2j + 1 of point s; Vt is [kSobolBits][2N]
-__device__ __forceinline__ void sobol_pair(const unsigned long long* __restrict__ Vt, int N, unsigned long long s,
-                                           int j, double& x0, double& x1)
+// the 62-bit integers of coordinates 2j and 2j + 1 of point s; Vt is [kSobolBits][2N]
+__device__ __forceinline__ void sobol_pair_q(const unsigned long long* __restrict__ Vt, int N, unsigned long long s,
+                                             int j, unsigned long long& q0, unsigned long long& q1)
 {
-    unsigned long long g = s ^ (s >> 1), q0 = 0, q1 = 0;
+    unsigned long long g = s ^ (s >> 1);
+    q0 = q1 = 0;
     const ulonglong2* col = reinterpret_cast<const ulonglong2*>(Vt) + j;  // 16-byte aligned: 2N columns per row
     while (g) {
         const int k = __ffsll((long long)g) - 1;
@@ -36,11 +38,20 @@ __device__ __forceinline__ void sobol_pair(const unsigned long long* __restrict_
         q1 ^= v.y;
         g &= g - 1;
     }
+}
+
+__device__ __forceinline__ void sobol_pair(const unsigned long long* __restrict__ Vt, int N, unsigned long long s,
+                                           int j, double& x0, double& x1)
+{
+    unsigned long long q0, q1;
+    sobol_pair_q(Vt, N, s, j, q0, q1);
     x0 = __ull2double_rn(q0) * 0x1p-62;
     x1 = __ull2double_rn(q1) * 0x1p-62;
 }
 
-// Z[b][0][j], Z[b][1][j] for paths b < B (point s0 + b)
+// Z[b][0][j], Z[b][1][j] for paths b < B (point s0 + b).  F32: the mixed
+// form's normals (top 32 bits, FP32 quantile), widened exactly to double.
+template <bool F32>
 __global__ void k_sobol_normals(const unsigned long long* __restrict__ Vt, int N, unsigned long long s0, int64_t B,
                                 double* __restrict__ Z)
 {
@@ -49,11 +60,16 @@ __global__ void k_sobol_normals(const unsigned long long* __restrict__ Vt, int N
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t b = idx / N;
         const int j = (int)(idx - b * N);
-        double x0, x1;
-        sobol_pair(Vt, N, s0 + (unsigned long long)b, j, x0, x1);
+        unsigned long long q0, q1;
+        sobol_pair_q(Vt, N, s0 + (unsigned long long)b, j, q0, q1);
         double* z = Z + (size_t)b * 2 * N;
-        z[j] = normcdfinv(x0);
-        z[N + j] = normcdfinv(x1);
+        if (F32) {
+            z[j] = (double)sobol_normal_f32((unsigned int)(q0 >> 30));
+            z[N + j] = (double)sobol_normal_f32((unsigned int)(q1 >> 30));
+        } else {
+            z[j] = normcdfinv(__ull2double_rn(q0) * 0x1p-62);
+            z[N + j] = normcdfinv(__ull2double_rn(q1) * 0x1p-62);
+        }
     }
 }
 
@@ -93,7 +109,7 @@ __global__ void k_sobol_bridge(const unsigned long long* __restrict__ Vt, int N,
 }
 
 int launch_sobol_normals(const unsigned long long* Vt, int N, uint64_t s0, int64_t B, const SobolBridge* br,
-                         double* Z, void* stream)
+                         double* Z, void* stream, int f32)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -103,7 +119,10 @@ int launch_sobol_normals(const unsigned long long* Vt, int N, uint64_t s0, int64
         const int64_t total = B * N;
         int64_t blocks = (total + 255) / 256;
         if (blocks > (int64_t)sms * 64) blocks = (int64_t)sms * 64;
-        k_sobol_normals<<<(unsigned)blocks, 256, 0, st>>>(Vt, N, (unsigned long long)s0, B, Z);
+        if (f32)
+            k_sobol_normals<true><<<(unsigned)blocks, 256, 0, st>>>(Vt, N, (unsigned long long)s0, B, Z);
+        else
+            k_sobol_normals<false><<<(unsigned)blocks, 256, 0, st>>>(Vt, N, (unsigned long long)s0, B, Z);
     } else {
         const size_t smem = sizeof(double) * 2 * (size_t)N;
         if (smem > 48 * 1024 &&

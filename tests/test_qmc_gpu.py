@@ -42,6 +42,16 @@ def test_normals_match_oracle(R, oracle, V, N, M, off, bridge):
     assert np.max(np.abs(Z - Zo)) < NORMAL_TOL * (4 if bridge else 1)
 
 
+@pytest.mark.parametrize("N,M,off", [(64, 4000, 0), (300, 500, 70000)])
+def test_fp32_normals_match_oracle(R, oracle, V, N, M, off):
+    """The mixed form's FP32 Sobol' normals (top 32 bits of the point, fitted
+    FP32 quantile, relative error <= 6e-7) against the oracle's FP64 normals."""
+    Z = R.sobol_normals(V, N, M, path_offset=off, precision=R.MIXED)
+    Zo = oracle.sobol_normals(V, N, M, path0=off)
+    assert np.all(Z.astype(np.float32).astype(np.float64) == Z)
+    assert np.max(np.abs(Z - Zo) / (1e-6 * np.abs(Zo) + 1e-7)) <= 1.0
+
+
 def test_normals_offset_is_a_suffix(R, V):
     a = R.sobol_normals(V, 32, 150)
     b = R.sobol_normals(V, 32, 100, path_offset=50)
