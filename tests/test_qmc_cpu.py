@@ -109,3 +109,32 @@ def test_sobol_entry_rejects_unsupported_forms():
         R.price_rt_sobol(*a, precision=R.MIXED, conv=R.CONV_FFT)
     with pytest.raises(ValueError):
         R.price_rt_sobol(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 4, 16, np.zeros((8, 63), np.uint64))
+
+
+def test_fp32_quantile_coefficients():
+    """The FP32 quantile of the mixed form's Sobol' normals
+    (rbg_device.cuh normal_quantile_lower_f32), evaluated in float32 with the
+    coefficients parsed from the CUDA source: relative error <= 6e-7 of the
+    exact quantile of its float32 input on [2^-32, 1/2]."""
+    import re
+
+    from scipy.special import ndtri
+
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "rbergomi_gb300", "csrc",
+                            "rbg_device.cuh")).read()
+    body = src[src.index("normal_quantile_lower_f32(float u)"):]
+    cen, tail = [np.array([float(v.rstrip("f")) for v in m.split(",")], np.float32)
+                 for m in re.findall(r"const float c\[9\] = \{([^}]*)\}", body)[:2]]
+    f32 = np.float32
+    u = np.concatenate([np.logspace(np.log10(2.0 ** -32), np.log10(0.5), 100000),
+                        np.linspace(0.3, 0.5, 50000)]).astype(f32)
+    x = f32(2) * u - f32(1)
+    w = (-np.log(f32(4) * u * (f32(1) - u))).astype(f32)
+    t, s = (w - f32(2.5)).astype(f32), (np.sqrt(w) - f32(3)).astype(f32)
+    p, q = np.full_like(u, cen[0]), np.full_like(u, tail[0])
+    for a, b in zip(cen[1:], tail[1:]):
+        p, q = (p * t + a).astype(f32), (q * s + b).astype(f32)
+    z = (f32(1.41421356) * x * np.where(w < 5, p, q)).astype(np.float64)
+    zt = ndtri(u.astype(np.float64))
+    m = np.abs(zt) > 1e-6
+    assert np.max(np.abs(z[m] - zt[m]) / np.abs(zt[m])) < 6e-7
