@@ -70,7 +70,9 @@ void computeIVRT_tensor(double xi, double* H, double* eta, double* rho, int par_
  * computeIVRT_tensor_quadrature, rBergLib/cinterface.h:73-75
  * (cinterface.cpp:102-131).  Z holds 2*N*M doubles: sample m uses
  * Z[2mN, 2mN+N) as W1 and Z[(2m+1)N, (2m+2)N) as W1perp.  payoff receives
- * M * par_size * op_size doubles, payoff[m*out_size + i].  Always FP64. */
+ * M * par_size * op_size doubles, payoff[m*out_size + i].  FP64 unless the
+ * environment sets RBG_PRECISION=mixed (then the mixed form's FP32 payoffs
+ * per path, widened to double). */
 void computeIVRT_tensor_quadrature(double xi, double* H, double* eta, double* rho, int par_size, double* T,
                                    double* K, int op_size, int N, long M, double* Z, int num_threads,
                                    double* payoff);
@@ -192,7 +194,9 @@ int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, do
 
 /* Per-path payoffs for caller-supplied normals (quadrature layout).  Z and
  * payoff are host pointers unless device_ptrs != 0, in which case both are
- * device pointers on the current device.  FP64 only. */
+ * device pointers on the current device.  o->precision RBG_MIXED runs the
+ * caller's normals (read as FP32) through the tensor-core path kernel and
+ * writes each path's FP32 payoff as double; NULL o or RBG_FP64: FP64. */
 int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs);
 
 /* Plain Monte Carlo on the Philox stream (streams W1, W1perp, Wperp): the
@@ -202,7 +206,7 @@ int rbg_price_mc(const rbg_params* p, const rbg_options* o, double* price, doubl
 
 /* Plain Monte Carlo per-path payoffs for caller-supplied normals: Z holds
  * 3*N*M doubles, sample m uses Z[3mN + sN, 3mN + sN + N) for s = 0 (W1),
- * 1 (W1perp), 2 (Wperp); payoff[m*out + i].  FP64 only. */
+ * 1 (W1perp), 2 (Wperp); payoff[m*out + i].  Precision as rbg_payoffs_rt. */
 int rbg_payoffs_mc(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs);
 
 /* Writes the normals the pricer would draw for paths

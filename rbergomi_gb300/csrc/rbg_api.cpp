@@ -547,6 +547,72 @@ static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payo
     return RBG_OK;
 }
 
+// Mixed form of the quadrature entry points: the caller's normals run through
+// the tensor-core path kernel (FP32 path state; a.ext instead of the Philox
+// stream) and the FP32 payoff per path is written as double.
+static int payoffs_quadrature_mixed(const rbg_params* p, const rbg_options& o, const double* Z, double* payoff,
+                                    int device_ptrs, bool mc)
+{
+    Plan plan;
+    std::string err;
+    if (!build_plan(*p, plan, err, mc)) return fail(RBG_ERR_ARG, err);
+    if (!Z || !payoff) return fail(RBG_ERR_ARG, "null Z/payoff");
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : c->stream;
+    TableSet ts;
+    if ((rc = upload_tables(*c, plan, st, ts))) return rc;
+    const int no = (int)plan.outs.size(), N = plan.N, ns = mc ? 3 : 2;
+    const int64_t M = p->M;
+    MixedJob job;
+    if ((rc = mixed_prepare(plan, o, M, job, g_err, 0, mc))) return rc;
+    int64_t B = job.batch;
+    B = std::min<int64_t>(B, std::max<int64_t>(256, ((int64_t)1 << 30) / (8 * (int64_t)no)));  // payoffs <= 1 GiB
+    if (!device_ptrs)  // staged normals <= 2 GiB
+        B = std::min<int64_t>(B, std::max<int64_t>(256, ((int64_t)1 << 31) / (8 * (int64_t)ns * N)));
+    if ((rc = ensure(c->mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
+    if ((rc = ensure(c->ivb, sizeof(float) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    if (mc && (rc = ensure(c->ivp, sizeof(float) * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
+    float* ivq = mc ? c->ivp.as<float>() : nullptr;
+    if (!device_ptrs) {
+        if ((rc = ensure(c->z, sizeof(double) * ns * N * (size_t)B, "normals"))) return rc;
+        if ((rc = ensure(c->pay, sizeof(double) * no * (size_t)B, "payoffs"))) return rc;
+    }
+    if (c->mixed_img != job.host_ws) {
+        c->mixed_img.clear();
+        if ((rc = mixed_upload(job, c->mixed_ws.p, st, g_err))) return rc;
+        c->mixed_img = job.host_ws;
+    } else {
+        RBG_CUDA(cudaMemsetAsync((unsigned char*)c->mixed_ws.p + job.off_err, 0, 4, st));
+    }
+    for (int64_t m0 = 0; m0 < M; m0 += B) {
+        const int64_t b = std::min(B, M - m0);
+        const double* Zd;
+        double* Pd;
+        if (device_ptrs) {
+            Zd = Z + m0 * ns * N;
+            Pd = payoff + m0 * no;
+        } else {
+            RBG_CUDA(cudaMemcpyAsync(c->z.p, Z + m0 * ns * N, sizeof(double) * ns * N * b, cudaMemcpyHostToDevice,
+                                     st));
+            Zd = c->z.as<double>();
+            Pd = c->pay.as<double>();
+        }
+        if ((rc = mixed_launch(job, c->mixed_ws.p, o.seed, 0, b, c->ivb.p, st, g_err, nullptr, nullptr, nullptr,
+                               nullptr, ivq, Zd)))
+            return rc;
+        launch_payoff_store_f32(ts.t.outs, no, c->ivb.p, ivq, b, Pd, st);
+        RBG_CUDA(cudaGetLastError());
+        if (!device_ptrs)
+            RBG_CUDA(cudaMemcpyAsync(payoff + m0 * no, Pd, sizeof(double) * no * b, cudaMemcpyDeviceToHost, st));
+    }
+    if ((rc = mixed_check(job, c->mixed_ws.p, st, g_err))) return rc;
+    RBG_CUDA(cudaStreamSynchronize(st));
+    return RBG_OK;
+}
+
 }  // namespace rbg
 
 using namespace rbg;
@@ -640,7 +706,8 @@ int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, do
 int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs)
 {
     if (!p) return fail(RBG_ERR_ARG, "null params");
-    if (o && o->precision != RBG_FP64) return fail(RBG_ERR_UNSUPPORTED, "per-path payoffs are FP64 only");
+    if (o && o->precision == RBG_MIXED) return payoffs_quadrature_mixed(p, *o, Z, payoff, device_ptrs, false);
+    if (o && o->precision != RBG_FP64) return fail(RBG_ERR_ARG, "unknown precision");
     return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr);
 }
 
@@ -821,7 +888,8 @@ int rbg_price_mc(const rbg_params* p, const rbg_options* o, double* price, doubl
 int rbg_payoffs_mc(const rbg_params* p, const rbg_options* o, const double* Z, double* payoff, int device_ptrs)
 {
     if (!p) return fail(RBG_ERR_ARG, "null params");
-    if (o && o->precision != RBG_FP64) return fail(RBG_ERR_UNSUPPORTED, "per-path payoffs are FP64 only");
+    if (o && o->precision == RBG_MIXED) return payoffs_quadrature_mixed(p, *o, Z, payoff, device_ptrs, true);
+    if (o && o->precision != RBG_FP64) return fail(RBG_ERR_ARG, "unknown precision");
     return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr, true);
 }
 
@@ -1111,7 +1179,11 @@ void computeIVRT_tensor_quadrature(double xi, double* H, double* eta, double* rh
     (void)num_threads;
     if (M <= 0 || (long)par_size * op_size == 0) return;  // nothing to price: no payoffs written
     rbg_params p{xi, H, eta, rho, par_size, T, K, op_size, N, (int64_t)M};
-    die_on(rbg_payoffs_rt(&p, nullptr, Z, payoff, 0));
+    rbg_options o;
+    rbg_default_options(&o);
+    const char* prec = std::getenv("RBG_PRECISION");
+    if (prec && std::strcmp(prec, "mixed") == 0) o.precision = RBG_MIXED;
+    die_on(rbg_payoffs_rt(&p, &o, Z, payoff, 0));
 }
 
 }  // extern "C"

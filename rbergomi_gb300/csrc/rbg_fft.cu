@@ -292,7 +292,12 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
         while (pth < 2) {
             const int64_t m = 2 * pr + pth;
             float z[4] = {0.f, 0.f, 0.f, 0.f};
-            if (m < a.B) {
+            if (m < a.B && a.ext) {
+                // the caller's FP64 normals, quadrature layout [B][NS][N]
+                const double* zz = a.ext + ((size_t)m * NS + s) * N + 4 * g;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) z[e] = (4 * g + e < N) ? (float)zz[e] : 0.f;
+            } else if (m < a.B) {
                 const uint4 x = philox_group(keys, (uint64_t)(a.path0 + m), (uint32_t)g, (uint32_t)s);
                 box_muller_f32(x.x, x.y, z[0], z[1]);
                 box_muller_f32(x.z, x.w, z[2], z[3]);

@@ -341,19 +341,53 @@ __device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rh
 // REDRAW (a first-pass chunk drawn again for the second pass), the FP32 W1 /
 // W1perp tiles the epilogue reads.  Compiled per REDRAW so that the W1 and
 // W1perp Philox streams stay interleaved in the common case.
-template <int BF16, bool REDRAW, bool MC>
+template <int BF16, bool REDRAW, bool MC, bool EXT = false>
 __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKeys& keys, uint64_t gpath, bool valid,
                                               int64_t m, int p, int h, int c, int n0, unsigned char* st,
                                               float* w1s)
 {
     constexpr int SPT = kStepsPerThread;
+    constexpr int NS = MC ? 3 : 2;
     const int Np = a.Np;
     const int sw = (p >> 1) & 3;
     float* w1ps = w1s + kFW1p;
     const int step0 = kChunk * c + SPT * h;
     float w[SPT], wp[SPT], wq[MC ? SPT : 1];
+    if (EXT) {
+        // the caller's FP64 normals, quadrature layout: path m's stream s at
+        // a.ext + (m NS + s) N.  Rows start on 16 bytes only when N is even
+        // and the base is 16-byte aligned; otherwise every load is scalar.
+        const int N = a.N;
+        const double* z = a.ext + (size_t)m * NS * N;
+        const bool vec = (N & 1) == 0 && (reinterpret_cast<uintptr_t>(a.ext) & 15) == 0;
+        if (valid && vec && step0 + SPT <= N) {
 #pragma unroll
-    for (int q = 0; q < SPT / 4; ++q) {
+            for (int q = 0; q < SPT; q += 2) {
+                const double2 u = *(const double2*)(z + step0 + q);
+                w[q] = (float)u.x; w[q + 1] = (float)u.y;
+                if (!REDRAW) {
+                    const double2 v = *(const double2*)(z + N + step0 + q);
+                    wp[q] = (float)v.x; wp[q + 1] = (float)v.y;
+                    if (MC) {
+                        const double2 x2 = *(const double2*)(z + 2 * N + step0 + q);
+                        wq[q] = (float)x2.x; wq[q + 1] = (float)x2.y;
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < SPT; ++q) {
+                const bool in = valid && step0 + q < N;
+                w[q] = in ? (float)z[step0 + q] : 0.f;
+                if (!REDRAW) {
+                    wp[q] = in ? (float)z[N + step0 + q] : 0.f;
+                    if (MC) wq[q] = in ? (float)z[2 * N + step0 + q] : 0.f;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < (EXT ? 0 : SPT / 4); ++q) {
         const uint32_t g = (uint32_t)((step0 >> 2) + q);
         const uint4 x0 = philox_group(keys, gpath, g, 0);
         box_muller_f32(x0.x, x0.y, w[4 * q], w[4 * q + 1]);
@@ -401,14 +435,20 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
         // redrawn chunks, so W1 at step 32 n0 for the last column's sqrt(v) dW
         // goes into this stage's boundary row
         if (c == n0 - 1 && h == kHPerPath - 1) {
-            const uint4 xb = philox_group(keys, gpath, (uint32_t)(8 * n0), 0);
-            float b0, b1;
-            box_muller_f32(xb.x, xb.y, b0, b1);
-            w1s[kFBnd + p] = valid ? b0 : 0.f;
-            if (MC) {
-                const uint4 xq = philox_group(keys, gpath, (uint32_t)(8 * n0), 2);
-                box_muller_f32(xq.x, xq.y, b0, b1);
-                w1s[kFWqBnd + p] = valid ? b0 : 0.f;
+            if (EXT) {
+                const double* z = a.ext + (size_t)m * NS * a.N;
+                w1s[kFBnd + p] = valid ? (float)z[kChunk * n0] : 0.f;
+                if (MC) w1s[kFWqBnd + p] = valid ? (float)z[2 * a.N + kChunk * n0] : 0.f;
+            } else {
+                const uint4 xb = philox_group(keys, gpath, (uint32_t)(8 * n0), 0);
+                float b0, b1;
+                box_muller_f32(xb.x, xb.y, b0, b1);
+                w1s[kFBnd + p] = valid ? b0 : 0.f;
+                if (MC) {
+                    const uint4 xq = philox_group(keys, gpath, (uint32_t)(8 * n0), 2);
+                    box_muller_f32(xq.x, xq.y, b0, b1);
+                    w1s[kFWqBnd + p] = valid ? b0 : 0.f;
+                }
             }
         }
         if (a.dbg_w && valid) {
@@ -504,8 +544,9 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
 // TWO: two TMEM passes per tile (512 < Np <= 1024).  The one-pass
 // instantiation has n0 = 0 at compile time, so the virtual-chunk bookkeeping
 // folds away there.
-// SOB: Sobol' normals (produce_chunk_sobol) instead of Philox; RT only.
-template <int BF16, bool TWO, bool MC, bool SOB = false>
+// SRC: where the normals come from: 0 Philox, 1 Sobol' (produce_chunk_sobol,
+// RT only), 2 the caller's FP64 normals (a.ext, quadrature layout).
+template <int BF16, bool TWO, bool MC, int SRC = 0>
 __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
     constexpr int NS = MC ? 3 : 2;  // normal streams per path = sums per variance group
@@ -588,15 +629,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
                 unsigned char* st = base + L.a0 + s * kStageA;
                 float* w1s = (float*)(base + L.f0 + s * kStageFB);
-                if (SOB) {
+                if (SRC == 1) {
                     if (TWO && redraw)
                         produce_chunk_sobol<BF16, true>(a, tile, c, n0, st, w1s);
                     else
                         produce_chunk_sobol<BF16, false>(a, tile, c, n0, st, w1s);
                 } else if (TWO && redraw) {
-                    produce_chunk<BF16, true, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+                    produce_chunk<BF16, true, MC, SRC == 2>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
                 } else {
-                    produce_chunk<BF16, false, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+                    produce_chunk<BF16, false, MC, SRC == 2>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
                 }
                 fence_proxy_async();
                 __syncwarp();
@@ -988,6 +1029,39 @@ void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int6
     count_launch();
 }
 
+// Per-path payoffs in FP32 (the mixed form of the quadrature entry points):
+// payoff[m * n_out + i] for paths m < B, as double.
+template <bool MC>
+__global__ void k_payoff_store_f32(const OutDev* __restrict__ outs, int n_out, const float2* __restrict__ ivb,
+                                   const float* __restrict__ ivq, int64_t B, double* __restrict__ payoff)
+{
+    const int64_t total = B * n_out;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t m = idx / n_out;
+        const int i = (int)(idx - m * n_out);
+        const OutDev od = outs[i];
+        const size_t at = (size_t)od.vg * B + m;
+        const float2 iv = ivb[at];
+        const float rho = (float)od.rho, K = (float)od.K;
+        payoff[idx] = MC ? (double)mc_payoff_f32(iv.x, iv.y, ivq[at], rho, K)
+                         : (double)rt_payoff_f32(iv.x, iv.y, rho, K, logf(K));
+    }
+}
+
+void launch_payoff_store_f32(const OutDev* outs, int n_out, const void* ivb, const float* ivq, int64_t B,
+                             double* payoff, cudaStream_t st)
+{
+    const int64_t total = B * n_out;
+    int64_t blocks = (total + 255) / 256;
+    if (blocks > (1 << 20)) blocks = 1 << 20;
+    if (ivq)
+        k_payoff_store_f32<true><<<(unsigned)blocks, 256, 0, st>>>(outs, n_out, (const float2*)ivb, ivq, B, payoff);
+    else
+        k_payoff_store_f32<false><<<(unsigned)blocks, 256, 0, st>>>(outs, n_out, (const float2*)ivb, ivq, B, payoff);
+    count_launch();
+}
+
 // ------------------------------------------------------------------- host
 namespace {
 
@@ -1273,8 +1347,12 @@ int mixed_part_rows(const MixedJob& job, int64_t B)
 
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
                  cudaStream_t st, std::string& err, float* dbg_w, float* dbg_x, double* part,
-                 unsigned long long* prof, float* ivq)
+                 unsigned long long* prof, float* ivq, const double* ext)
 {
+    if (ext && (job.sob || job.fused)) {
+        err = "caller normals run with the separate payoff kernels and without Sobol' normals";
+        return RBG_ERR_UNSUPPORTED;
+    }
     if (job.mc && !ivq) {
         err = "plain Monte Carlo launch without an IsvdWp buffer";
         return RBG_ERR_ARG;
@@ -1303,6 +1381,7 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         A.dbg_w = dbg_w;
         A.dbg_x = dbg_x;
         A.sob = job.sob;
+        A.ext = ext;
         A.seed = seed;
         A.path0 = path0;
         A.B = B;
@@ -1316,9 +1395,15 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
             void (*kern)(MixedArgs);
             const bool two = A.n0 > 0;
             if (job.sob && job.split == RBG_SPLIT_BF16X3)
-                kern = two ? k_mixed_gemm<1, true, false, true> : k_mixed_gemm<1, false, false, true>;
+                kern = two ? k_mixed_gemm<1, true, false, 1> : k_mixed_gemm<1, false, false, 1>;
             else if (job.sob)
-                kern = two ? k_mixed_gemm<0, true, false, true> : k_mixed_gemm<0, false, false, true>;
+                kern = two ? k_mixed_gemm<0, true, false, 1> : k_mixed_gemm<0, false, false, 1>;
+            else if (ext && job.split == RBG_SPLIT_BF16X3)
+                kern = job.mc ? (two ? k_mixed_gemm<1, true, true, 2> : k_mixed_gemm<1, false, true, 2>)
+                              : (two ? k_mixed_gemm<1, true, false, 2> : k_mixed_gemm<1, false, false, 2>);
+            else if (ext)
+                kern = job.mc ? (two ? k_mixed_gemm<0, true, true, 2> : k_mixed_gemm<0, false, true, 2>)
+                              : (two ? k_mixed_gemm<0, true, false, 2> : k_mixed_gemm<0, false, false, 2>);
             else if (job.split == RBG_SPLIT_BF16X3)
                 kern = job.mc ? (two ? k_mixed_gemm<1, true, true> : k_mixed_gemm<1, false, true>)
                               : (two ? k_mixed_gemm<1, true, false> : k_mixed_gemm<1, false, false>);

@@ -32,6 +32,7 @@ struct MixedArgs {
     const float2* spec;          // FFT backend: FFT(Gamma)/L, L points
     const float2* tw;            // FFT backend: exp(-2 pi i t / L), L points
     const unsigned int* sob;     // Sobol' normals (GEMM backend, RT): [32][2N] bits 30..61 of the direction integers
+    const double* ext;           // caller normals for this launch's paths, [B][ns][N] FP64 (quadrature layout)
     uint64_t seed;
     int64_t path0, B;
     int N, Np, nc, n_g, g0, tmem_cols, stages;
@@ -77,9 +78,12 @@ int mixed_upload(const MixedJob& job, void* ws, cudaStream_t st, std::string& er
 // (rows = mixed_part_rows(job, B), zeroed by the caller) and write ivb only
 // when it is non-null.
 // Plain Monte Carlo jobs also write IsvdWp per (group, path) to ivq.
+// ext: the caller's normals for paths [0, B) of this launch ([B][ns][N] FP64
+// on the device) instead of the Philox stream.
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
                  cudaStream_t st, std::string& err, float* dbg_w = nullptr, float* dbg_x = nullptr,
-                 double* part = nullptr, unsigned long long* prof = nullptr, float* ivq = nullptr);
+                 double* part = nullptr, unsigned long long* prof = nullptr, float* ivq = nullptr,
+                 const double* ext = nullptr);
 int mixed_part_rows(const MixedJob& job, int64_t B);
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
 // FFT backend (rbg_fft.cu)
@@ -89,6 +93,9 @@ void fft_tables(const double* gamma, int N, int logL, float* spec, float* tw);
 cudaError_t launch_mixed_fft(const MixedArgs& A, int sms, cudaStream_t st);
 
 // ivq non-null: plain Monte Carlo payoffs max(S_T - K, 0) from (Ivdt, IsvdW, IsvdWp)
+// per-path FP32 payoffs, payoff[m * n_out + i] as double (mixed quadrature)
+void launch_payoff_store_f32(const OutDev* outs, int n_out, const void* ivb, const float* ivq, int64_t B,
+                             double* payoff, cudaStream_t st);
 void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int64_t B, int G, double* part,
                             int nchunks, cudaStream_t st, const float* ivq = nullptr);
 
