@@ -341,53 +341,19 @@ __device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rh
 // REDRAW (a first-pass chunk drawn again for the second pass), the FP32 W1 /
 // W1perp tiles the epilogue reads.  Compiled per REDRAW so that the W1 and
 // W1perp Philox streams stay interleaved in the common case.
-template <int BF16, bool REDRAW, bool MC, bool EXT = false>
+template <int BF16, bool REDRAW, bool MC>
 __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKeys& keys, uint64_t gpath, bool valid,
                                               int64_t m, int p, int h, int c, int n0, unsigned char* st,
                                               float* w1s)
 {
     constexpr int SPT = kStepsPerThread;
-    constexpr int NS = MC ? 3 : 2;
     const int Np = a.Np;
     const int sw = (p >> 1) & 3;
     float* w1ps = w1s + kFW1p;
     const int step0 = kChunk * c + SPT * h;
     float w[SPT], wp[SPT], wq[MC ? SPT : 1];
-    if (EXT) {
-        // the caller's FP64 normals, quadrature layout: path m's stream s at
-        // a.ext + (m NS + s) N.  Rows start on 16 bytes only when N is even
-        // and the base is 16-byte aligned; otherwise every load is scalar.
-        const int N = a.N;
-        const double* z = a.ext + (size_t)m * NS * N;
-        const bool vec = (N & 1) == 0 && (reinterpret_cast<uintptr_t>(a.ext) & 15) == 0;
-        if (valid && vec && step0 + SPT <= N) {
 #pragma unroll
-            for (int q = 0; q < SPT; q += 2) {
-                const double2 u = *(const double2*)(z + step0 + q);
-                w[q] = (float)u.x; w[q + 1] = (float)u.y;
-                if (!REDRAW) {
-                    const double2 v = *(const double2*)(z + N + step0 + q);
-                    wp[q] = (float)v.x; wp[q + 1] = (float)v.y;
-                    if (MC) {
-                        const double2 x2 = *(const double2*)(z + 2 * N + step0 + q);
-                        wq[q] = (float)x2.x; wq[q + 1] = (float)x2.y;
-                    }
-                }
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < SPT; ++q) {
-                const bool in = valid && step0 + q < N;
-                w[q] = in ? (float)z[step0 + q] : 0.f;
-                if (!REDRAW) {
-                    wp[q] = in ? (float)z[N + step0 + q] : 0.f;
-                    if (MC) wq[q] = in ? (float)z[2 * N + step0 + q] : 0.f;
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < (EXT ? 0 : SPT / 4); ++q) {
+    for (int q = 0; q < SPT / 4; ++q) {
         const uint32_t g = (uint32_t)((step0 >> 2) + q);
         const uint4 x0 = philox_group(keys, gpath, g, 0);
         box_muller_f32(x0.x, x0.y, w[4 * q], w[4 * q + 1]);
@@ -435,20 +401,14 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
         // redrawn chunks, so W1 at step 32 n0 for the last column's sqrt(v) dW
         // goes into this stage's boundary row
         if (c == n0 - 1 && h == kHPerPath - 1) {
-            if (EXT) {
-                const double* z = a.ext + (size_t)m * NS * a.N;
-                w1s[kFBnd + p] = valid ? (float)z[kChunk * n0] : 0.f;
-                if (MC) w1s[kFWqBnd + p] = valid ? (float)z[2 * a.N + kChunk * n0] : 0.f;
-            } else {
-                const uint4 xb = philox_group(keys, gpath, (uint32_t)(8 * n0), 0);
-                float b0, b1;
-                box_muller_f32(xb.x, xb.y, b0, b1);
-                w1s[kFBnd + p] = valid ? b0 : 0.f;
-                if (MC) {
-                    const uint4 xq = philox_group(keys, gpath, (uint32_t)(8 * n0), 2);
-                    box_muller_f32(xq.x, xq.y, b0, b1);
-                    w1s[kFWqBnd + p] = valid ? b0 : 0.f;
-                }
+            const uint4 xb = philox_group(keys, gpath, (uint32_t)(8 * n0), 0);
+            float b0, b1;
+            box_muller_f32(xb.x, xb.y, b0, b1);
+            w1s[kFBnd + p] = valid ? b0 : 0.f;
+            if (MC) {
+                const uint4 xq = philox_group(keys, gpath, (uint32_t)(8 * n0), 2);
+                box_muller_f32(xq.x, xq.y, b0, b1);
+                w1s[kFWqBnd + p] = valid ? b0 : 0.f;
             }
         }
         if (a.dbg_w && valid) {
@@ -538,6 +498,69 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
         for (unsigned long long g = sb ^ (sb >> 1); g; g &= g - 1)
             q ^= __ldg(a.sob + (size_t)(__ffsll((long long)g) - 1) * 2 * N + 2 * jb);
         w1s[kFBnd + p] = (m0 + lane < a.B && jb < N) ? sobol_normal_f32(q) : 0.f;
+    }
+}
+
+// Caller-normals producer (the mixed quadrature entry points): the caller's
+// FP64 normals in the quadrature layout, path m's stream s at a.ext +
+// (m NS + s) N.  Warp w of the producers takes paths 16 w .. 16 w + 15 of the
+// tile and lane l step j = 32 c + l, so each load instruction reads 32
+// consecutive doubles of one row (256 B, coalesced; no alignment beyond the
+// doubles' own).  Writes the FP32 W1 / W1perp (/ Wperp) tiles and the 16-bit
+// hi/lo A tile (REDRAW: W1 and the A tile only).
+template <int BF16, bool REDRAW, bool MC>
+__device__ __forceinline__ void produce_chunk_ext(const MixedArgs& a, int64_t tile, int c, int n0, unsigned char* st,
+                                                  float* w1s)
+{
+    constexpr int NS = MC ? 3 : 2;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int N = a.N, Np = a.Np;
+    const int j = kChunk * c + lane;
+    const bool jin = j < N;
+    const int64_t m0 = tile * kTileM + 16 * w;
+    float* w1ps = w1s + kFW1p;
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+        const int p = 16 * w + i;
+        const int64_t m = m0 + i;
+        const bool ok = jin && m < a.B;
+        const double* z = a.ext + (size_t)m * NS * N + j;
+        const float z0 = ok ? (float)__ldg(z) : 0.f;
+        if (!REDRAW) {
+            w1s[ftile_at(p, lane)] = z0;
+            w1ps[ftile_at(p, lane)] = ok ? (float)__ldg(z + N) : 0.f;
+            if (MC) w1s[kFWq + ftile_at(p, lane)] = ok ? (float)__ldg(z + 2 * N) : 0.f;
+            if (a.dbg_w && m < a.B) {
+                a.dbg_w[(m * 2 + 0) * Np + j] = z0;
+                a.dbg_w[(m * 2 + 1) * Np + j] = w1ps[ftile_at(p, lane)];
+            }
+        }
+        uint32_t hi, lo;
+        split2<BF16>(z0, 0.f, hi, lo);
+        const int off = p * 64 + ((((lane >> 3)) ^ ((p >> 1) & 3)) << 4) + ((lane & 7) << 1);
+        *(unsigned short*)(st + off) = (unsigned short)hi;
+        *(unsigned short*)(st + kTileBytes + off) = (unsigned short)lo;
+    }
+    // the next chunk's rows into L2 while this one is consumed: the loads above
+    // keep too few bytes in flight to cover HBM latency on their own.  One
+    // 128-byte line per 16 lanes; every address stays inside its row.
+    if ((lane & 15) == 0 && j + kChunk < N) {
+#pragma unroll 4
+        for (int i = 0; i < 16; ++i) {
+            if (m0 + i >= a.B) break;
+            const double* z = a.ext + (size_t)(m0 + i) * NS * N + j + kChunk;
+#pragma unroll
+            for (int s = 0; s < (REDRAW ? 1 : NS); ++s)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(z + (size_t)s * N));
+        }
+    }
+    // last chunk of the first pass: W1 (and Wperp) at step 32 n0 for the boundary rows
+    if (!REDRAW && c == n0 - 1 && lane < 16) {
+        const int p = 16 * w + lane;
+        const int64_t m = m0 + lane;
+        const double* z = a.ext + (size_t)m * NS * N + kChunk * n0;
+        w1s[kFBnd + p] = m < a.B ? (float)__ldg(z) : 0.f;
+        if (MC) w1s[kFWqBnd + p] = m < a.B ? (float)__ldg(z + 2 * N) : 0.f;
     }
 }
 
@@ -634,10 +657,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                         produce_chunk_sobol<BF16, true>(a, tile, c, n0, st, w1s);
                     else
                         produce_chunk_sobol<BF16, false>(a, tile, c, n0, st, w1s);
+                } else if (SRC == 2) {
+                    if (TWO && redraw)
+                        produce_chunk_ext<BF16, true, MC>(a, tile, c, n0, st, w1s);
+                    else
+                        produce_chunk_ext<BF16, false, MC>(a, tile, c, n0, st, w1s);
                 } else if (TWO && redraw) {
-                    produce_chunk<BF16, true, MC, SRC == 2>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+                    produce_chunk<BF16, true, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
                 } else {
-                    produce_chunk<BF16, false, MC, SRC == 2>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+                    produce_chunk<BF16, false, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
                 }
                 fence_proxy_async();
                 __syncwarp();
