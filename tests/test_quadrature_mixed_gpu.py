@@ -83,3 +83,23 @@ def test_dropin_quadrature_honours_mixed_precision(R):
     p64 = R.computeIVRT_tensor_quadrature(*args)
     assert np.max(np.abs(p64 - c["payoff"])) < 1e-11   # back to FP64 without the variable
     assert not np.array_equal(pay, p64)
+
+
+@pytest.mark.parametrize("shift", [0, 1])
+def test_mixed_quadrature_device_buffers(R, shift):
+    """Device pointers (a caller's own CUDA buffers): the same payoffs as the
+    host-buffer call, also when the normals start only 8-byte aligned (one
+    double into an allocation)."""
+    torch = pytest.importorskip("torch")
+    xi, H, eta, rho, T, K = 0.04, [0.1], [1.5], [-0.7], [0.5, 1.0], [0.9, 1.1]
+    M, N = 3001, 37
+    Z = R.generate_normals(8, M, N)
+    want = R.payoffs_rt(xi, H, eta, rho, T, K, Z, precision=R.MIXED)
+    buf = torch.zeros(shift + Z.size, dtype=torch.float64, device="cuda")
+    buf[shift:] = torch.from_numpy(Z.ravel()).cuda()
+    out = torch.full((M, len(T)), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()  # the library runs on its own stream
+    R.payoffs_rt(xi, H, eta, rho, T, K, buf.data_ptr() + 8 * shift, device_ptrs=True, M=M, N=N,
+                 precision=R.MIXED, out_ptr=out.data_ptr())
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), want)
