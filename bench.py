@@ -159,6 +159,33 @@ def peaks():
         return 1900.0, 6800.0, "fallback"
 
 
+def kernel_figure(kernel: str, key: str):
+    """A per-kernel figure from the committed ncu summaries (profiles/traffic.json)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)[kernel][key]
+    except (OSError, KeyError, ValueError, TypeError):
+        return None
+
+
+def issue_roofline(kernel: str, path_steps_per_launch: float, kernel_ms: float, clocks: dict):
+    """The binding resource of the mixed path kernels is instruction issue:
+    ncu's thread-instructions per path-step (profiles/traffic.json) times the
+    live kernel rate, in warp-instructions/s, against one issue per cycle per
+    SM sub-partition (4 per SM) at the SM clock sampled during the run."""
+    ips = kernel_figure(kernel, "inst_per_path_step")
+    mhz = clocks.get("sm_mhz") if clocks else None
+    if ips is None or not mhz:
+        return None
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    achieved = path_steps_per_launch / (kernel_ms / 1e3) * ips / 32.0
+    peak = 4.0 * sms * mhz * 1e6
+    return {"unit": "warp-instr/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "inst_per_path_step": ips, "source": "ncu smsp__inst_executed (profiles), live kernel time, sampled clock"}
+
+
 def traffic_per_launch(kernel: str, w):
     """DRAM bytes per launch from the committed ncu summary, scaled by paths."""
     try:
@@ -307,6 +334,8 @@ def run_gpu(args, w):
         "prices_per_s": ws * len(w["H"]) * len(w["K"]) / (ms_step / 1e3),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(), "gpu_launches": launches,
     }
+    if prec == R.MIXED:
+        roof["issue"] = issue_roofline(kname, path_steps(w) / max(1, kn // args.steps), avg_kernel_ms, line["clocks"])
     line.update(extra)
     print(json.dumps(line))
 
