@@ -66,7 +66,7 @@ EXPORTS = [
     "rbg_server_poll", "rbg_server_wait", "rbg_server_get_stats", "rbg_server_destroy", "rbg_server_last_error",
     "rbg_price_rt_unordered", "computeIV_tensor", "rbg_price_mc", "rbg_payoffs_mc", "rbg_generate_normals_streams",
     "rbg_plan_info_mc", "rbg_plan_info_unordered", "rbg_price_rt_cv", "rbg_price_rt_cv_normals",
-    "rbg_price_rt_sobol", "rbg_sobol_normals",
+    "rbg_price_rt_sobol", "rbg_sobol_normals", "rbg_debug_wait_timeout",
 ]
 
 STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4

@@ -1004,6 +1004,29 @@ void rbg_last_transfer_bytes(uint64_t* h2d, uint64_t* d2h)
     if (d2h) *d2h = g_d2h;
 }
 
+int rbg_debug_wait_timeout(unsigned int limit_us, unsigned int* site)
+{
+    if (limit_us == 0 || limit_us > 2000000u) return fail(RBG_ERR_ARG, "limit must be in (0, 2 s]");
+    Ctx* c = nullptr;
+    int rc = get_ctx(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(c->mu);
+    DevBuf word;
+    if (word.ensure(sizeof(unsigned int))) return fail(RBG_ERR_NOMEM, "error word");
+    unsigned int host = 0;
+    cudaError_t e = cudaMemsetAsync(word.p, 0, sizeof(unsigned int), c->stream);
+    const unsigned int kSite = 99;
+    if (e == cudaSuccess && launch_wait_probe(word.as<unsigned int>(), (uint64_t)limit_us * 1000u, kSite, c->stream))
+        e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&host, word.p, sizeof(host), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    word.release();
+    if (e != cudaSuccess) return fail(RBG_ERR_CUDA, std::string("wait probe: ") + cudaGetErrorString(e));
+    if (site) *site = host;
+    if (host != 0) return fail(RBG_ERR_TIMEOUT, "bounded wait expired (site " + std::to_string(host) + ")");
+    return fail(RBG_ERR_CUDA, "wait probe returned without expiring");
+}
+
 int rbg_debug_mixed_profile(const rbg_params* p, const rbg_options* o, uint64_t* cycles, int n)
 {
     if (!p || !o || !cycles || n < 32) return fail(RBG_ERR_ARG, "need params, options and 32 counters");

@@ -172,9 +172,10 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 // Bounded wait for the phase of the given parity; false on timeout or when
 // another role already failed (then the caller winds down).  The error word
 // and the clock are polled every 64 tries only (at most 64 x 20 us apart).  With `prof` set (diagnostic
-// runs), lane 0 adds the cycles it waited to prof[site].
+// runs), lane 0 adds the cycles it waited to prof[site].  limit_ns: the
+// time limit (2 s in the pricing kernels).
 __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site,
-                                       unsigned long long* prof = nullptr)
+                                       unsigned long long* prof = nullptr, uint64_t limit_ns = kWaitNs)
 {
     if (mbar_try(bar, parity)) return true;
     const long long c0 = prof ? clock64() : 0;
@@ -184,7 +185,7 @@ __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned i
         if (mbar_try(bar, parity)) break;
         if ((it & 63u) == 0u) {
             if (*(volatile unsigned int*)err != 0u) { ok = false; break; }
-            if (globaltimer() - t0 > kWaitNs) {
+            if (globaltimer() - t0 > limit_ns) {
                 atomicCAS(err, 0u, site);
                 ok = false;
                 break;
@@ -1088,6 +1089,27 @@ void launch_payoff_store_f32(const OutDev* outs, int n_out, const void* ivb, con
     else
         k_payoff_store_f32<false><<<(unsigned)blocks, 256, 0, st>>>(outs, n_out, (const float2*)ivb, ivq, B, payoff);
     count_launch();
+}
+
+// Failure-detection check: one warp waits, through the pricing kernels'
+// bounded-wait helper, on an mbarrier that nothing arrives on, with the given
+// limit; the expiry records `site` in the error word, as a pipeline wait
+// would, and the kernel returns.
+__global__ void k_wait_probe(unsigned int* err, uint64_t limit_ns, unsigned int site)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(smem_u32(&bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+    const bool ok = mbar_wait(smem_u32(&bar), 0, err, site, nullptr, limit_ns);
+    if (__all_sync(0xffffffffu, ok) && threadIdx.x == 0) atomicExch(err, 0xffffffffu);  // cannot happen: nothing arrives
+}
+
+int launch_wait_probe(unsigned int* err, uint64_t limit_ns, unsigned int site, cudaStream_t st)
+{
+    k_wait_probe<<<1, 32, 0, st>>>(err, limit_ns, site);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 // ------------------------------------------------------------------- host
