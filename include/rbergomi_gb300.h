@@ -244,11 +244,11 @@ int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, 
 int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t* directions, int dims, int bridge,
                        double* price, double* stat, double* iv);
 /* Failure-detection check (no counterpart in the reference): one warp waits,
- * with the pricing kernels' bounded-wait helper and a limit of limit_us
- * microseconds (<= 2 s), on an mbarrier nothing arrives on.  Returns
- * RBG_ERR_TIMEOUT with the expiring wait's site in *site (as a stalled
- * pipeline reports), leaving the context usable. */
-int rbg_debug_wait_timeout(unsigned int limit_us, unsigned int* site);
+ * with the pricing kernels' bounded-wait helper and a 20 ms limit, on an
+ * mbarrier nothing arrives on.  Returns RBG_ERR_TIMEOUT with the expiring
+ * wait's site in *site (as a stalled pipeline reports), leaving the context
+ * usable. */
+int rbg_debug_wait_timeout(unsigned int* site);
 
 /* The Sobol' normals those prices use: M*2*N doubles in the quadrature
  * layout, host pointer.  precision RBG_FP64: normcdfinv of the 62-bit point;

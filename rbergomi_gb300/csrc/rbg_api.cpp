@@ -1004,9 +1004,8 @@ void rbg_last_transfer_bytes(uint64_t* h2d, uint64_t* d2h)
     if (d2h) *d2h = g_d2h;
 }
 
-int rbg_debug_wait_timeout(unsigned int limit_us, unsigned int* site)
+int rbg_debug_wait_timeout(unsigned int* site)
 {
-    if (limit_us == 0 || limit_us > 2000000u) return fail(RBG_ERR_ARG, "limit must be in (0, 2 s]");
     Ctx* c = nullptr;
     int rc = get_ctx(&c);
     if (rc) return rc;
@@ -1016,7 +1015,7 @@ int rbg_debug_wait_timeout(unsigned int limit_us, unsigned int* site)
     unsigned int host = 0;
     cudaError_t e = cudaMemsetAsync(word.p, 0, sizeof(unsigned int), c->stream);
     const unsigned int kSite = 99;
-    if (e == cudaSuccess && launch_wait_probe(word.as<unsigned int>(), (uint64_t)limit_us * 1000u, kSite, c->stream))
+    if (e == cudaSuccess && launch_wait_probe(word.as<unsigned int>(), kSite, c->stream))
         e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&host, word.p, sizeof(host), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

@@ -172,10 +172,11 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 // Bounded wait for the phase of the given parity; false on timeout or when
 // another role already failed (then the caller winds down).  The error word
 // and the clock are polled every 64 tries only (at most 64 x 20 us apart).  With `prof` set (diagnostic
-// runs), lane 0 adds the cycles it waited to prof[site].  limit_ns: the
-// time limit (2 s in the pricing kernels).
+// runs), lane 0 adds the cycles it waited to prof[site].  LIMIT_NS: the time
+// limit, a compile-time constant (2 s in the pricing kernels).
+template <uint64_t LIMIT_NS = kWaitNs>
 __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned int* err, unsigned int site,
-                                       unsigned long long* prof = nullptr, uint64_t limit_ns = kWaitNs)
+                                       unsigned long long* prof = nullptr)
 {
     if (mbar_try(bar, parity)) return true;
     const long long c0 = prof ? clock64() : 0;
@@ -185,7 +186,7 @@ __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned i
         if (mbar_try(bar, parity)) break;
         if ((it & 63u) == 0u) {
             if (*(volatile unsigned int*)err != 0u) { ok = false; break; }
-            if (globaltimer() - t0 > limit_ns) {
+            if (globaltimer() - t0 > LIMIT_NS) {
                 atomicCAS(err, 0u, site);
                 ok = false;
                 break;
@@ -1092,22 +1093,23 @@ void launch_payoff_store_f32(const OutDev* outs, int n_out, const void* ivb, con
 }
 
 // Failure-detection check: one warp waits, through the pricing kernels'
-// bounded-wait helper, on an mbarrier that nothing arrives on, with the given
+// bounded-wait helper, on an mbarrier that nothing arrives on, with a 20 ms
 // limit; the expiry records `site` in the error word, as a pipeline wait
 // would, and the kernel returns.
-__global__ void k_wait_probe(unsigned int* err, uint64_t limit_ns, unsigned int site)
+constexpr uint64_t kProbeWaitNs = 20000000ull;
+__global__ void k_wait_probe(unsigned int* err, unsigned int site)
 {
     __shared__ __align__(8) uint64_t bar;
     if (threadIdx.x == 0) mbar_init(smem_u32(&bar), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncwarp();
-    const bool ok = mbar_wait(smem_u32(&bar), 0, err, site, nullptr, limit_ns);
+    const bool ok = mbar_wait<kProbeWaitNs>(smem_u32(&bar), 0, err, site);
     if (__all_sync(0xffffffffu, ok) && threadIdx.x == 0) atomicExch(err, 0xffffffffu);  // cannot happen: nothing arrives
 }
 
-int launch_wait_probe(unsigned int* err, uint64_t limit_ns, unsigned int site, cudaStream_t st)
+int launch_wait_probe(unsigned int* err, unsigned int site, cudaStream_t st)
 {
-    k_wait_probe<<<1, 32, 0, st>>>(err, limit_ns, site);
+    k_wait_probe<<<1, 32, 0, st>>>(err, site);
     count_launch();
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -87,8 +87,8 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
 int mixed_part_rows(const MixedJob& job, int64_t B);
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
 // one warp waits on an mbarrier nothing arrives on, with the pipeline's bounded
-// wait and the given limit; *err receives `site` on expiry
-int launch_wait_probe(unsigned int* err, uint64_t limit_ns, unsigned int site, cudaStream_t st);
+// wait and a 20 ms limit; *err receives `site` on expiry
+int launch_wait_probe(unsigned int* err, unsigned int site, cudaStream_t st);
 // FFT backend (rbg_fft.cu)
 int fft_log2_len(int N);
 size_t fft_smem_bytes(int N, int n_g, int ns = 2);
