@@ -101,53 +101,132 @@ def run_reference(args, w):
 
 
 # --------------------------------------------------------------- GPU arm
+class _Nvml:
+    """Read-only NVML queries through ctypes (libnvidia-ml ships with the driver):
+    SM clock, its maximum, board power and the active clock-event reasons of one
+    GPU, found by the PCI bus id CUDA reports for the device."""
+
+    SM = 1  # NVML_CLOCK_SM
+    # nvmlClocksEventReasons bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, cuda_index: int):
+        import ctypes
+        import torch
+        self.c = ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.lib = lib
+        pr = torch.cuda.get_device_properties(cuda_index)
+        bus = f"{pr.pci_domain_id:08X}:{pr.pci_bus_id:02X}:{pr.pci_device_id:02X}.0".encode()
+        self.dev = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByPciBusId_v2(ctypes.c_char_p(bus), ctypes.byref(self.dev)) != 0:
+            lib.nvmlShutdown()
+            raise OSError(f"no NVML device at {bus.decode()}")
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        u = ctypes.c_uint()
+        self.max_mhz = float(u.value) if lib.nvmlDeviceGetMaxClockInfo(self.dev, self.SM, ctypes.byref(u)) == 0 \
+            else None
+
+    def sample(self):
+        c, lib = self.c, self.lib
+        mhz, mw, rs = c.c_uint(), c.c_uint(), c.c_ulonglong()
+        if lib.nvmlDeviceGetClockInfo(self.dev, self.SM, c.byref(mhz)) != 0:
+            return None
+        watts = mw.value / 1e3 if lib.nvmlDeviceGetPowerUsage(self.dev, c.byref(mw)) == 0 else None
+        bits = rs.value if self.reasons_fn(self.dev, c.byref(rs)) == 0 else 0
+        return float(mhz.value), watts, [n for b, n in self.REASONS.items() if bits & b]
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
 class ClockSampler:
-    """nvidia-smi clock/throttle samples while the timed region runs."""
+    """SM clock, power and throttle reasons sampled while the timed region runs:
+    NVML every 10 ms on a thread, or `nvidia-smi -lms 200` where NVML cannot be
+    loaded."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    SMI_REASONS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.nvml = None
+        self.rows = []  # (sm MHz, max MHz, watts or None, [active reasons])
+        self.source = None
+
+    def _poll(self):
+        while not self.stop.wait(0.01):
+            s = self.nvml.sample()
+            if s:
+                self.rows.append((s[0], self.nvml.max_mhz, s[1], s[2]))
 
     def __enter__(self):
+        import threading
+        try:
+            self.nvml = _Nvml(self.index)
+        except Exception:
+            self.nvml = None
+        if self.nvml is not None:
+            self.source = "nvml 10 ms"
+            s = self.nvml.sample()
+            if s:
+                self.rows.append((s[0], self.nvml.max_mhz, s[1], s[2]))
+            self.stop = threading.Event()
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.source = "nvidia-smi 200 ms"
         except OSError:
             self.proc = None
         return self
 
     def __exit__(self, *exc):
-        self.out = ""
+        if self.nvml is not None:
+            self.stop.set()
+            self.thread.join()
+            s = self.nvml.sample()
+            if s:
+                self.rows.append((s[0], self.nvml.max_mhz, s[1], s[2]))
+            self.nvml.close()
+            return
+        out = ""
         if self.proc:
             self.proc.terminate()
             try:
-                self.out, _ = self.proc.communicate(timeout=5)
+                out, _ = self.proc.communicate(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                self.out, _ = self.proc.communicate()
-
-    def summary(self):
-        rows = []
-        for line in (self.out or "").strip().splitlines():
+                out, _ = self.proc.communicate()
+        for line in (out or "").strip().splitlines():
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 8:
                 continue
             try:
-                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[4:8]))
+                self.rows.append((float(parts[1]), float(parts[2]), float(parts[3]),
+                                  [n for n, v in zip(self.SMI_REASONS, parts[4:8]) if v.lower() == "active"]))
             except ValueError:
                 continue
+
+    def summary(self):
+        rows = self.rows
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        active = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
-        loaded = [r for r in rows if r[2] > 200.0] or rows
-        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": active, "samples": len(rows)}
+        active = sorted({n for r in rows for n in r[3]})
+        loaded = [r for r in rows if r[2] is not None and r[2] > 200.0] or rows
+        maxes = [r[1] for r in rows if r[1] is not None]
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(maxes) if maxes else None,
+                "reasons": active, "samples": len(rows), "source": self.source}
 
 
 def peaks():
@@ -565,7 +644,8 @@ def main():
                     choices=sorted(WORKLOADS) + ["serving-poisson", "paramtot-grid-m1m", "sobol-fp64-n256-m1m"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
     ap.add_argument("--split", type=int, default=0, help="0 = BF16x3, 1 = FP16x3")
-    ap.add_argument("--cpu-paths", type=int, default=1 << 17)
+    ap.add_argument("--cpu-paths", type=int, default=1 << 18,
+                    help="CPU legs: paths per sample (about 20 core-seconds on 16 cores at N = 512)")
     ap.add_argument("--paths", type=int, default=None, help="override M (small cases for ncu captures)")
     ap.add_argument("--steps-per-path", type=int, default=None, help="override N (crossover sweeps)")
     ap.add_argument("--conv", default="auto", choices=["auto", "gemm", "fft"], help="mixed-form Volterra backend")
