@@ -109,16 +109,18 @@ __device__ __forceinline__ float normal_quantile_lower_f32(float u)
 
 // Sobol' normal in FP32 from the top 32 bits q of a coordinate (x = q 2^-32):
 // the quantile of the lower tail u = min(x, 1 - x), so points near 1 keep
-// their relative precision; sign restored after.  The tail count 2^32 - q is
-// formed in 64 bits: written as the 32-bit `up ? 0u - q : q` it is the
-// integer absolute-value idiom, which the compiler turns into a signed abs
-// that reads q = 2^31 (x = 1/2) as -2^31.
+// their relative precision; sign restored after.  For x >= 1/2 the tail
+// 1 - x = (~q + 1) 2^-32 is formed as float(~q) 2^-32 + 2^-32 in one FMA:
+// exact below 2^-8, within one float ulp of the correctly rounded tail above.
+// (~q, not 0 - q: the subtraction form is the integer absolute-value idiom,
+// which the compiler turns into a signed abs that reads q = 2^31 as -2^31.)
+// Both ~q (x >= 1/2) and q (x < 1/2) lie below 2^31.
 __device__ __forceinline__ float sobol_normal_f32(unsigned int q)
 {
-    const bool up = q >= 0x80000000u;
-    const unsigned long long r = up ? (1ull << 32) - q : (unsigned long long)q;
-    const float z = normal_quantile_lower_f32(__ull2float_rn(r) * 0x1p-32f);
-    return up ? -z : z;
+    const unsigned int up = (unsigned int)((int)q >> 31);  // all ones for x >= 1/2
+    const float f = __uint2float_rn(q ^ up);
+    const float z = normal_quantile_lower_f32(fmaf(f, 0x1p-32f, __uint_as_float(up & 0x2f800000u)));
+    return __uint_as_float(__float_as_uint(z) ^ (up & 0x80000000u));
 }
 
 // FP64 Box-Muller on uniforms (x + 1/2) 2^-32.

@@ -435,12 +435,54 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
 // consecutive indices have ctz <= 3 except at most one multiple of 16).
 // Writes the FP32 W1 / W1perp tiles and the 16-bit hi/lo A tile (REDRAW: W1
 // and the A tile only).
+
+// The Gray-code start: XOR of the table rows of the set bits of g (< 2^KB),
+// all loads issued before the XORs need them.
+template <int KB>
+__device__ __forceinline__ void sobol_gray_start(const uint2* tab, int N, int j, unsigned long long g,
+                                                 unsigned int& q0, unsigned int& q1)
+{
+#pragma unroll
+    for (int k = 0; k < KB; ++k) {
+        if ((g >> k) & 1ull) {
+            const uint2 v = __ldg(tab + (size_t)k * N + j);
+            q0 ^= v.x;
+            q1 ^= v.y;
+        }
+    }
+}
+
+// One point of the Sobol' producer: lane's step j of path row p (path m),
+// from the point's coordinates q0 (W1) and q1 (W1perp).
+template <int BF16, bool REDRAW>
+__device__ __forceinline__ void sobol_point(const MixedArgs& a, int p, int64_t m, int j, int lane, bool jin,
+                                            unsigned int q0, unsigned int q1, unsigned char* st, float* w1s)
+{
+    const bool ok = jin && m < a.B;
+    const float z0 = ok ? sobol_normal_f32(q0) : 0.f;
+    const float z1 = (ok && !REDRAW) ? sobol_normal_f32(q1) : 0.f;
+    if (!REDRAW) {
+        const int at = ftile_at(p, lane);
+        w1s[at] = z0;
+        w1s[kFW1p + at] = z1;
+        if (a.dbg_w && m < a.B) {
+            a.dbg_w[(m * 2 + 0) * a.Np + j] = z0;
+            a.dbg_w[(m * 2 + 1) * a.Np + j] = z1;
+        }
+    }
+    uint32_t hi, lo;
+    split2<BF16>(z0, 0.f, hi, lo);
+    const int off = p * 64 + ((((lane >> 3)) ^ ((p >> 1) & 3)) << 4) + ((lane & 7) << 1);
+    *(unsigned short*)(st + off) = (unsigned short)hi;
+    *(unsigned short*)(st + kTileBytes + off) = (unsigned short)lo;
+}
+
 template <int BF16, bool REDRAW>
 __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t tile, int c, int n0, unsigned char* st,
                                                     float* w1s)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int N = a.N, Np = a.Np;
+    const int N = a.N;
     const int j = kChunk * c + lane;
     const bool jin = j < N;
     const int64_t m0 = tile * kTileM + 16 * w;
@@ -452,44 +494,41 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
     const bool has16 = m16 <= s0 + 15;
     if (jin) {
         const unsigned long long g = s0 ^ (s0 >> 1);  // point indices stay below 2^32
-#pragma unroll
-        for (int k = 0; k < 32; ++k) {
-            if ((g >> k) & 1ull) {
-                const uint2 v = __ldg(tab + (size_t)k * N + j);
-                q0 ^= v.x;
-                q1 ^= v.y;
-            }
-        }
+        if ((g >> 20) == 0ull)  // warp-uniform: fewer than 2^20 points in
+            sobol_gray_start<20>(tab, N, j, g, q0, q1);
+        else
+            sobol_gray_start<32>(tab, N, j, g, q0, q1);
 #pragma unroll
         for (int k = 0; k < 4; ++k) r[k] = __ldg(tab + (size_t)k * N + j);
         if (has16) rb = __ldg(tab + (size_t)(__ffsll((long long)m16) - 1) * N + j);
     }
-    float* w1ps = w1s + kFW1p;
-#pragma unroll 4
-    for (int i = 0; i < 16; ++i) {
-        const int p = 16 * w + i;
-        const int64_t m = m0 + i;
-        const bool ok = jin && m < a.B;
-        const float z0 = ok ? sobol_normal_f32(q0) : 0.f;
-        const float z1 = (ok && !REDRAW) ? sobol_normal_f32(q1) : 0.f;
-        if (!REDRAW) {
-            w1s[ftile_at(p, lane)] = z0;
-            w1ps[ftile_at(p, lane)] = z1;
-            if (a.dbg_w && m < a.B) {
-                a.dbg_w[(m * 2 + 0) * Np + j] = z0;
-                a.dbg_w[(m * 2 + 1) * Np + j] = z1;
-            }
+    if ((s0 & 15ull) == 1ull) {
+        // s0 = 16 t + 1 (path offsets that are multiples of 16): s0 + i + 1 =
+        // 16 t + i + 2, so the walk's rows are fixed by i -- 1, 0, 2, 0, 1, 0, 3,
+        // 0, 1, 0, 2, 0, 1, 0 and the multiple of 16 last
+#pragma unroll 1
+        for (int t = 0; t < 4; ++t) {
+            const int i0 = 4 * t, p0 = 16 * w + i0;
+            sobol_point<BF16, REDRAW>(a, p0, m0 + i0, j, lane, jin, q0, q1, st, w1s);
+            q0 ^= r[1].x; q1 ^= r[1].y;
+            sobol_point<BF16, REDRAW>(a, p0 + 1, m0 + i0 + 1, j, lane, jin, q0, q1, st, w1s);
+            q0 ^= r[0].x; q1 ^= r[0].y;
+            sobol_point<BF16, REDRAW>(a, p0 + 2, m0 + i0 + 2, j, lane, jin, q0, q1, st, w1s);
+            const uint2 v = t == 1 ? r[3] : t == 3 ? rb : r[2];
+            q0 ^= v.x; q1 ^= v.y;
+            sobol_point<BF16, REDRAW>(a, p0 + 3, m0 + i0 + 3, j, lane, jin, q0, q1, st, w1s);
+            q0 ^= r[0].x; q1 ^= r[0].y;
         }
-        uint32_t hi, lo;
-        split2<BF16>(z0, 0.f, hi, lo);
-        const int off = p * 64 + ((((lane >> 3)) ^ ((p >> 1) & 3)) << 4) + ((lane & 7) << 1);
-        *(unsigned short*)(st + off) = (unsigned short)hi;
-        *(unsigned short*)(st + kTileBytes + off) = (unsigned short)lo;
-        if (i < 15) {
-            const int k = __ffsll((long long)(s0 + i + 1)) - 1;
-            const uint2 v = k == 0 ? r[0] : k == 1 ? r[1] : k == 2 ? r[2] : k == 3 ? r[3] : rb;
-            q0 ^= v.x;
-            q1 ^= v.y;
+    } else {
+#pragma unroll 4
+        for (int i = 0; i < 16; ++i) {
+            sobol_point<BF16, REDRAW>(a, 16 * w + i, m0 + i, j, lane, jin, q0, q1, st, w1s);
+            if (i < 15) {
+                const int k = __ffsll((long long)(s0 + i + 1)) - 1;
+                const uint2 v = k == 0 ? r[0] : k == 1 ? r[1] : k == 2 ? r[2] : k == 3 ? r[3] : rb;
+                q0 ^= v.x;
+                q1 ^= v.y;
+            }
         }
     }
     // last chunk of the first pass: W1 at step 32 n0 for the boundary row

@@ -106,6 +106,12 @@ def test_mixed_form_path_offset(R, V):
     q1, _, _ = R.price_rt_sobol(*a, precision=R.FP64, path_offset=100000)
     assert np.all(p0 != p1)
     assert np.all(np.abs(p1 - q1) < 0.2 * s1)
+    # offsets that are not multiples of 16 take the producer's general walk
+    for off in (100003, 7):
+        p2, s2, _ = R.price_rt_sobol(*a, precision=R.MIXED, path_offset=off)
+        q2, _, _ = R.price_rt_sobol(*a, precision=R.FP64, path_offset=off)
+        assert np.all(rel_err(p2, q2) < 1e-4)
+        assert np.all(np.abs(p2 - q2) < 0.2 * s2)
 
 
 def test_rejects_bad_requests(R, V):
