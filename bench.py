@@ -102,7 +102,7 @@ def run_reference(args, w):
 
 # --------------------------------------------------------------- GPU arm
 class _Nvml:
-    """Read-only NVML queries through ctypes (libnvidia-ml ships with the driver):
+    """Read-only NVML queries through ctypes (libnvidia-ml is installed with the GPU kernel driver):
     SM clock, its maximum, board power and the active clock-event reasons of one
     GPU, found by the PCI bus id CUDA reports for the device."""
 
