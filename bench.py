@@ -291,9 +291,8 @@ def run_gpu(args, w):
     prec = R.MIXED if args.precision == "mixed" else R.FP64
     # weak scaling: every rank prices its own M paths (disjoint Philox paths)
     offset = rank * w["M"]
-    conv = {"auto": R.CONV_AUTO, "gemm": R.CONV_GEMM, "fft": R.CONV_FFT}[args.conv]
-    kw = dict(seed=w["seed"], precision=prec, split=args.split, path_offset=offset, stream=sptr,
-              conv=conv if prec == R.MIXED else R.CONV_AUTO)
+    conv = {"auto": R.CONV_AUTO, "gemm": R.CONV_GEMM, "fft": R.CONV_FFT, "direct": R.CONV_DIRECT}[args.conv]
+    kw = dict(seed=w["seed"], precision=prec, split=args.split, path_offset=offset, stream=sptr, conv=conv)
     flush = torch.empty((256 << 20) // 4, dtype=torch.float32, device="cuda")
 
     def step():
@@ -341,8 +340,9 @@ def run_gpu(args, w):
     Np = (w["N"] + 31) // 32 * 32
     nc = Np // 32
     exec_flops = 6.0 * 32 * 32 * nc * (nc + 1) / 2 * w["M"] / max(1, kn // args.steps)
+    fp64_fft = args.conv == "fft" or (args.conv == "auto" and 200 <= w["N"] <= 2048)
     kname = ("k_mixed_fft" if (args.conv == "fft" or (args.conv == "auto" and w["N"] > 1024))
-             else "k_mixed_gemm") if prec == R.MIXED else "k_path_fp64"
+             else "k_mixed_gemm") if prec == R.MIXED else ("k_path_fp64_fft" if fp64_fft else "k_path_fp64")
     roof = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
             "frac": achieved_tf / bf16_peak, "traffic": traffic_per_launch(kname, w),
             "kernel": kname,
@@ -648,7 +648,8 @@ def main():
                     help="CPU legs: paths per sample (about 20 core-seconds on 16 cores at N = 512)")
     ap.add_argument("--paths", type=int, default=None, help="override M (small cases for ncu captures)")
     ap.add_argument("--steps-per-path", type=int, default=None, help="override N (crossover sweeps)")
-    ap.add_argument("--conv", default="auto", choices=["auto", "gemm", "fft"], help="mixed-form Volterra backend")
+    ap.add_argument("--conv", default="auto", choices=["auto", "gemm", "fft", "direct"],
+                    help="Volterra backend: gemm / fft (mixed form), fft / direct (FP64 form)")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--requests", type=int, default=10000, help="serving: number of requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: Poisson arrival rate per second")

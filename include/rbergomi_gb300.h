@@ -94,7 +94,9 @@ enum rbg_precision { RBG_FP64 = 0, RBG_MIXED = 1 };
 
 /* Volterra convolution backend.  In mixed mode AUTO picks the tcgen05
  * Toeplitz GEMM for N <= 1024 (one TMEM pass up to 512 steps, two above) and
- * the batched FFT convolution above; the FP64 form uses the direct sum. */
+ * the batched FFT convolution above.  The FP64 form has two: the direct
+ * causal sum (DIRECT) and an FP64 FFT convolution (FFT, 2 <= N <= 2048); AUTO
+ * takes the FFT from 200 steps to 2048.  GEMM is mixed-mode only. */
 enum rbg_conv { RBG_CONV_AUTO = 0, RBG_CONV_GEMM = 1, RBG_CONV_FFT = 2, RBG_CONV_DIRECT = 3 };
 
 /* Normal transform used by the FP64 form: its own FP64 Box-Muller (default),

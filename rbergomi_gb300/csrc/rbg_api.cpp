@@ -178,7 +178,26 @@ struct TableSet {
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts)
+// The FP64 form's Volterra backend for N steps: logL > 0 selects the FFT
+// convolution (AUTO: from kFp64FftMinN steps), 0 the direct sum.
+static int fp64_conv_log2(int conv, int N, int* logL)
+{
+    *logL = 0;
+    if (conv == RBG_CONV_GEMM) return fail(RBG_ERR_UNSUPPORTED, "the FP64 form has no GEMM backend");
+    if (conv == RBG_CONV_DIRECT) return RBG_OK;
+    const int l = fp64_fft_log2_len(N);
+    if (conv == RBG_CONV_FFT) {
+        if (!l) return fail(RBG_ERR_UNSUPPORTED, "the FP64 FFT convolution needs 2 <= N <= 2048");
+        *logL = l;
+    } else if (N >= kFp64FftMinN) {
+        *logL = l;
+    }
+    return RBG_OK;
+}
+
+// logL > 0: also the FP64 FFT convolution's spectra (one per distinct H) and
+// twiddles
+static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts, int logL = 0)
 {
     const int nv = (int)plan.vols.size(), ng = (int)plan.vgs.size(), no = (int)plan.outs.size(), N = plan.N;
     std::vector<VolDev> vols(nv);
@@ -200,8 +219,14 @@ static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts
     size_t off_T = align_up(off_outs + sizeof(OutDev) * no, 256);
     size_t off_gamma = align_up(off_T + sizeof(double) * no, 256);
     size_t off_comp = align_up(off_gamma + sizeof(double) * plan.gamma.size(), 256);
-    size_t total = align_up(off_comp + sizeof(double) * plan.comp.size(), 256);
+    const size_t L = logL > 0 ? (size_t)1 << logL : 0;
+    size_t off_spec = align_up(off_comp + sizeof(double) * plan.comp.size(), 256);
+    size_t off_tw = align_up(off_spec + 2 * sizeof(double) * L * nv, 256);
+    size_t total = align_up(off_tw + 2 * sizeof(double) * L, 256);
     std::vector<unsigned char> host(total, 0);
+    if (logL > 0)
+        fp64_fft_tables(plan.gamma.data(), nv, N, logL, (double*)(host.data() + off_spec),
+                        (double*)(host.data() + off_tw));
     std::memcpy(host.data() + off_vols, vols.data(), sizeof(VolDev) * nv);
     std::memcpy(host.data() + off_vgs, vgs.data(), sizeof(VGDev) * ng);
     std::memcpy(host.data() + off_outs, outs.data(), sizeof(OutDev) * no);
@@ -223,6 +248,9 @@ static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts
     ts.t.outs = (const OutDev*)(base + off_outs);
     ts.t.gamma = (const double*)(base + off_gamma);
     ts.t.comp = (const double*)(base + off_comp);
+    ts.t.spec = logL > 0 ? (const double2*)(base + off_spec) : nullptr;
+    ts.t.tw = logL > 0 ? (const double2*)(base + off_tw) : nullptr;
+    ts.t.logL = logL;
     ts.t.n_vol = nv;
     ts.t.n_vg = ng;
     ts.t.n_out = no;
@@ -255,8 +283,10 @@ static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M,
                       const SobolBridge* br = nullptr)
 {
     TableSet ts;
-    int rc = upload_tables(c, plan, st, ts);
+    int logL = 0;
+    int rc = fp64_conv_log2(o.conv, plan.N, &logL);
     if (rc) return rc;
+    if ((rc = upload_tables(c, plan, st, ts, logL))) return rc;
     const int no = (int)plan.outs.size(), N = plan.N, ns = mc ? 3 : 2;
     const int64_t B = fp64_batch(plan, M, ns);
     if ((rc = ensure(c.z, sizeof(double) * ns * N * (size_t)B, "normals"))) return rc;
@@ -394,11 +424,7 @@ static int price_plan(const Plan& plan, int64_t M, const rbg_options* o, std::ve
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
     res.assign(5 * plan.outs.size(), 0.0);
-    if (o->precision == RBG_FP64) {
-        if (o->conv == RBG_CONV_GEMM || o->conv == RBG_CONV_FFT)
-            return fail(RBG_ERR_UNSUPPORTED, "FP64 form uses the direct Volterra sum");
-        return price_fp64(*c, plan, *o, M, st, res.data(), mc);
-    }
+    if (o->precision == RBG_FP64) return price_fp64(*c, plan, *o, M, st, res.data(), mc);
     if (o->precision == RBG_MIXED) return price_mixed(*c, plan, *o, M, st, res.data(), mc);
     return fail(RBG_ERR_ARG, "unknown precision");
 }
@@ -421,8 +447,10 @@ static int price_cv(Ctx& c, const Plan& plan, const rbg_cv_params& p, const rbg_
                     const double* Z, cudaStream_t st, double* host_res)
 {
     TableSet ts;
-    int rc = upload_tables(c, plan, st, ts);
+    int logL = 0;
+    int rc = fp64_conv_log2(o.conv, plan.N, &logL);
     if (rc) return rc;
+    if ((rc = upload_tables(c, plan, st, ts, logL))) return rc;
     const int no = (int)plan.outs.size(), N = plan.N, ng = (int)plan.vgs.size();
     const int64_t Mc = p.M_control, M = p.M;
     const int64_t B = fp64_batch(plan, M, 4);  // normals plus two (Ivdt, IsvdW) sets per path
@@ -499,7 +527,7 @@ static int price_cv_any(const rbg_cv_params* p, const rbg_options* o, const doub
 }
 
 static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payoff, int device_ptrs,
-                              cudaStream_t user_stream, bool mc = false)
+                              cudaStream_t user_stream, bool mc = false, int conv = RBG_CONV_AUTO)
 {
     Plan plan;
     std::string err;
@@ -511,7 +539,9 @@ static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payo
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = user_stream ? user_stream : c->stream;
     TableSet ts;
-    if ((rc = upload_tables(*c, plan, st, ts))) return rc;
+    int logL = 0;
+    if ((rc = fp64_conv_log2(conv, plan.N, &logL))) return rc;
+    if ((rc = upload_tables(*c, plan, st, ts, logL))) return rc;
     const int no = (int)plan.outs.size(), N = plan.N, ns = mc ? 3 : 2;
     const int64_t M = p->M;
     int64_t B = fp64_batch(plan, M, ns);
@@ -708,7 +738,8 @@ int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, d
     if (!p) return fail(RBG_ERR_ARG, "null params");
     if (o && o->precision == RBG_MIXED) return payoffs_quadrature_mixed(p, *o, Z, payoff, device_ptrs, false);
     if (o && o->precision != RBG_FP64) return fail(RBG_ERR_ARG, "unknown precision");
-    return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr);
+    return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr, false,
+                              o ? o->conv : RBG_CONV_AUTO);
 }
 
 int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, int N, int precision, int streams,
@@ -844,8 +875,6 @@ int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t
         return fail(RBG_ERR_UNSUPPORTED, "the Brownian bridge runs in the FP64 form only");
     if (o->precision == RBG_MIXED && o->conv == RBG_CONV_FFT)
         return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend (N <= 1024)");
-    if (o->precision == RBG_FP64 && (o->conv == RBG_CONV_GEMM || o->conv == RBG_CONV_FFT))
-        return fail(RBG_ERR_UNSUPPORTED, "FP64 form uses the direct Volterra sum");
     g_h2d = g_d2h = 0;
     Plan plan;
     std::string err;
@@ -890,7 +919,8 @@ int rbg_payoffs_mc(const rbg_params* p, const rbg_options* o, const double* Z, d
     if (!p) return fail(RBG_ERR_ARG, "null params");
     if (o && o->precision == RBG_MIXED) return payoffs_quadrature_mixed(p, *o, Z, payoff, device_ptrs, true);
     if (o && o->precision != RBG_FP64) return fail(RBG_ERR_ARG, "unknown precision");
-    return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr, true);
+    return payoffs_quadrature(p, Z, payoff, device_ptrs, o ? (cudaStream_t)o->stream : nullptr, true,
+                              o ? o->conv : RBG_CONV_AUTO);
 }
 
 int rbg_implied_vol(int n, const double* price, const double* K, const double* T, double* iv)

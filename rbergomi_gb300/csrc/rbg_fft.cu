@@ -466,6 +466,28 @@ void fft_tables(const double* gamma, int N, int logL, float* spec, float* tw)
     }
 }
 
+// The FP64 form's FFT convolution: spec[v] = FFT(Gamma_v zero-padded to L,
+// Gamma_v[0] = 0, as the direct sum over k < j leaves it out) / L and the
+// twiddles exp(-2 pi i q / L), complex doubles (re, im)
+void fp64_fft_tables(const double* gamma, int n_vol, int N, int logL, double* spec, double* tw)
+{
+    const int L = 1 << logL;
+    for (int v = 0; v < n_vol; ++v) {
+        std::vector<std::complex<double>> x(L, 0.0);
+        for (int n = 1; n < N; ++n) x[n] = gamma[(size_t)v * N + n];
+        fft_host(x, false);
+        for (int k = 0; k < L; ++k) {
+            spec[((size_t)v * L + k) * 2] = x[k].real() / L;
+            spec[((size_t)v * L + k) * 2 + 1] = x[k].imag() / L;
+        }
+    }
+    const double pi = 3.14159265358979323846;
+    for (int q = 0; q < L; ++q) {
+        tw[2 * q] = std::cos(-2 * pi * q / L);
+        tw[2 * q + 1] = std::sin(-2 * pi * q / L);
+    }
+}
+
 template <int LOGL, bool MC>
 static cudaError_t launch_fft_lm(const MixedArgs& A, int sms, cudaStream_t st)
 {

@@ -142,6 +142,215 @@ __global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t 
     }
 }
 
+// ------------------------------------------------------ path pass, FFT
+// The same pass with the Volterra sum as an FP64 FFT convolution: O(N log N)
+// FP64 operations per path instead of N^2 / 2, so from a few hundred steps it
+// does the FP64 pipe a fraction of the work.  The reference convolves the
+// same way (fftOMP over FFTW, rBergLib/rBergomiMT.cpp:83-109); the results
+// differ from the direct sum by roundoff.
+//
+// One CTA of 256 threads per pair of paths (a, b): z = W1_a + i W1_b,
+// zero-padded to L = 2^logL >= 2N - 1, so the circular convolution with the
+// real Gamma holds both linear ones, y = conv(z, Gamma) = Y2_a + i Y2_b.
+// y = IFFT(FFT(z) FFT(Gamma)) = conj(FFT(conj(FFT(z) spec))) with
+// spec = FFT(Gamma) / L, so one forward Stockham transform serves both
+// directions.  FFT(z) is kept for every distinct H (pass v).
+//
+// Stockham autosort, radix 4 (one radix-2 pass first when logL is odd), in
+// place: each thread loads its butterflies' inputs, the block synchronises,
+// then each thread writes its outputs (the formulation of Govindaraju et al.,
+// "High performance discrete Fourier transforms on graphics processors",
+// SC'08: pass (R, Ns) reads x[j + r L / R], twiddles by exp(-2 pi i r (j mod
+// Ns) / (Ns R)) and writes x[(j - j mod Ns) R + j mod Ns + r Ns]).
+constexpr int kFftThreads = 256;
+constexpr int kFp64FftMinLogL = 8;  // shorter transforms run at L = 256 (any L >= 2N - 1 holds the sums)
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
+// MAXB: butterflies per thread, L / R / 256 rounded up
+template <int R, int MAXB>
+__device__ __forceinline__ void stockham_pass(double2* x, int L, int Ns, const double2* __restrict__ tw)
+{
+    const int nb = L / R;
+    const int tstep = L / (Ns * R);
+    double2 v[MAXB][R];
+#pragma unroll
+    for (int b = 0; b < MAXB; ++b) {
+        const int j = threadIdx.x + b * kFftThreads;
+        if (j < nb) {
+            const int k = j & (Ns - 1);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const double2 a = x[j + r * nb];
+                v[b][r] = (r == 0 || k == 0) ? a : cmul(a, __ldg(tw + r * k * tstep));
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < MAXB; ++b) {
+        const int j = threadIdx.x + b * kFftThreads;
+        if (j < nb) {
+            const int k = j & (Ns - 1);
+            const int d = (j - k) * R + k;
+            if (R == 2) {
+                const double2 a = v[b][0], c = v[b][1];
+                x[d] = make_double2(a.x + c.x, a.y + c.y);
+                x[d + Ns] = make_double2(a.x - c.x, a.y - c.y);
+            } else {
+                // X0 = a + b + c + e, X1 = a - i b - c + i e, X2 = a - b + c - e, X3 = a + i b - c - i e
+                const double2 a = v[b][0], bb = v[b][1], c = v[b][2], e = v[b][3];
+                const double2 s0 = make_double2(a.x + c.x, a.y + c.y), d0 = make_double2(a.x - c.x, a.y - c.y);
+                const double2 s1 = make_double2(bb.x + e.x, bb.y + e.y), d1 = make_double2(bb.x - e.x, bb.y - e.y);
+                x[d] = make_double2(s0.x + s1.x, s0.y + s1.y);
+                x[d + Ns] = make_double2(d0.x + d1.y, d0.y - d1.x);       // d0 - i d1
+                x[d + 2 * Ns] = make_double2(s0.x - s1.x, s0.y - s1.y);
+                x[d + 3 * Ns] = make_double2(d0.x - d1.y, d0.y + d1.x);   // d0 + i d1
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// forward DFT of x (L = 2^LOGL) in natural order
+template <int LOGL>
+__device__ __forceinline__ void fft_forward(double2* x, const double2* __restrict__ tw)
+{
+    constexpr int L = 1 << LOGL;
+    constexpr int B2 = (L / 2 + kFftThreads - 1) / kFftThreads, B4 = (L / 4 + kFftThreads - 1) / kFftThreads;
+    int Ns = 1;
+    if (LOGL & 1) {
+        stockham_pass<2, B2>(x, L, Ns, tw);
+        Ns = 2;
+    }
+#pragma unroll 1
+    for (; Ns < L; Ns *= 4) stockham_pass<4, B4>(x, L, Ns, tw);
+}
+
+// block sum over the 128 threads of one path half (threads 0..127 or 128..255)
+__device__ __forceinline__ double half_sum(double s, double* red, int slot)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) red[slot * 8 + w] = s;
+    __syncthreads();
+    const int w0 = (threadIdx.x >> 7) * 4;
+    const double r = (red[slot * 8 + w0] + red[slot * 8 + w0 + 1]) + (red[slot * 8 + w0 + 2] + red[slot * 8 + w0 + 3]);
+    return r;
+}
+
+template <int LOGL, int NS, bool ANTI>
+__global__ void __launch_bounds__(kFftThreads) k_path_fp64_fft(Fp64Tables t, const double* __restrict__ Z, int64_t B,
+                                                              double2* __restrict__ ivb, double* __restrict__ ivp,
+                                                              double2* __restrict__ ivn)
+{
+    extern __shared__ double2 fsm[];
+    constexpr int L = 1 << LOGL;
+    const int N = t.N;
+    double2* zf = fsm;      // FFT(z), kept across passes v
+    double2* y = fsm + L;   // work buffer
+    double* red = (double*)(fsm + 2 * L);  // [5 sums][8 warps]
+    const int64_t ma = 2 * (int64_t)blockIdx.x, mb = ma + 1;
+    const bool has_b = mb < B;
+    const double* Wa = Z + ma * NS * (int64_t)N;
+    const double* Wb = Z + mb * NS * (int64_t)N;
+    for (int k = threadIdx.x; k < L; k += kFftThreads)
+        zf[k] = k < N ? make_double2(Wa[k], has_b ? Wb[k] : 0.0) : make_double2(0.0, 0.0);
+    __syncthreads();
+    fft_forward<LOGL>(zf, t.tw);
+    // this thread's path and steps in the variance loops
+    const int half = threadIdx.x >> 7, jt = threadIdx.x & 127;
+    const int64_t m = half ? mb : ma;
+    const bool active = half ? has_b : true;
+    const double* W1 = Z + m * NS * (int64_t)N;  // valid only when active
+    for (int v = 0; v < t.n_vol; ++v) {
+        const double2* sp = t.spec + (size_t)v * L;
+        for (int k = threadIdx.x; k < L; k += kFftThreads) {
+            const double2 u = cmul(zf[k], __ldg(sp + k));
+            y[k] = make_double2(u.x, -u.y);
+        }
+        __syncthreads();
+        fft_forward<LOGL>(y, t.tw);
+        // X = Y2 + a1 W1 + a2 W1perp: Y2_a = Re y = Re FFT(w), Y2_b = Im y = -Im FFT(w)
+        const VolDev vol = t.vols[v];
+        for (int j = threadIdx.x; j < N; j += kFftThreads) {
+            const double2 q = y[j];
+            const double xa = q.x + (vol.a1 * Wa[j] + vol.a2 * Wa[N + j]);
+            const double xb = has_b ? -q.y + (vol.a1 * Wb[j] + vol.a2 * Wb[N + j]) : 0.0;
+            y[j] = make_double2(xa, xb);
+        }
+        __syncthreads();
+        for (int g = vol.vg_begin; g < vol.vg_end; ++g) {
+            const VGDev vg = t.vgs[g];
+            const double* comp = t.comp + (size_t)g * N;
+            double sv = 0.0, sw = 0.0, sp2 = 0.0, nv = 0.0, nw = 0.0;
+            if (active) {
+                for (int j = jt; j < vg.nsteps; j += 128) {
+                    const double xp = (j == 0) ? 0.0 : (half ? y[j - 1].y : y[j - 1].x);
+                    const double vj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * xp) - comp[j - 1]);
+                    sv += vj;
+                    const double sq = sqrt(vj) * vg.sdt;
+                    sw += sq * W1[j];
+                    if (NS == 3) sp2 += sq * W1[2 * N + j];
+                    if (ANTI) {
+                        const double uj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * -xp) - comp[j - 1]);
+                        nv += uj;
+                        nw += sqrt(uj) * vg.sdt * -W1[j];
+                    }
+                }
+            }
+            sv = half_sum(sv, red, 0);
+            sw = half_sum(sw, red, 1);
+            if (NS == 3) sp2 = half_sum(sp2, red, 2);
+            if (ANTI) {
+                nv = half_sum(nv, red, 3);
+                nw = half_sum(nw, red, 4);
+            }
+            if (jt == 0 && active) {
+                ivb[(size_t)g * B + m] = make_double2(vg.dt * sv, sw);
+                if (NS == 3) ivp[(size_t)g * B + m] = sp2;
+                if (ANTI) ivn[(size_t)g * B + m] = make_double2(vg.dt * nv, nw);
+            }
+            __syncthreads();  // red is reused by the next group
+        }
+    }
+}
+
+size_t path_fp64_fft_smem(int logL) { return (size_t)2 * (16u << logL) + 5 * 8 * sizeof(double); }
+
+int fp64_fft_log2_len(int N)
+{
+    int logL = kFp64FftMinLogL;
+    while ((1 << logL) < 2 * N - 1) ++logL;
+    return (N >= 2 && logL <= kFp64FftMaxLogL) ? logL : 0;
+}
+
+template <int LOGL>
+static void launch_fp64_fft(const Fp64Tables& t, const double* Z, int64_t B, double* ivb, cudaStream_t st,
+                            double* ivp, double* ivn)
+{
+    const size_t smem = path_fp64_fft_smem(LOGL);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_path_fp64_fft<LOGL, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_path_fp64_fft<LOGL, 3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_path_fp64_fft<LOGL, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = true;
+    }
+    const unsigned pairs = (unsigned)((B + 1) / 2);
+    if (ivn)
+        k_path_fp64_fft<LOGL, 2, true><<<pairs, kFftThreads, smem, st>>>(t, Z, B, (double2*)ivb, nullptr,
+                                                                         (double2*)ivn);
+    else if (ivp)
+        k_path_fp64_fft<LOGL, 3, false><<<pairs, kFftThreads, smem, st>>>(t, Z, B, (double2*)ivb, ivp, nullptr);
+    else
+        k_path_fp64_fft<LOGL, 2, false><<<pairs, kFftThreads, smem, st>>>(t, Z, B, (double2*)ivb, nullptr, nullptr);
+}
+
 int path_fp64_warps(int N)
 {
     const size_t budget = 200 * 1024;
@@ -166,8 +375,19 @@ void launch_path_fp64(const Fp64Tables& t, const double* Z, int64_t B, double* i
         cudaFuncSetAttribute(k_path_fp64<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = smem;
     }
-    const int64_t blocks = (B + warps - 1) / warps;
     cudaStream_t st = (cudaStream_t)stream;
+    if (t.logL > 0) {
+        switch (t.logL) {
+        case 8: launch_fp64_fft<8>(t, Z, B, ivb, st, ivp, ivn); break;
+        case 9: launch_fp64_fft<9>(t, Z, B, ivb, st, ivp, ivn); break;
+        case 10: launch_fp64_fft<10>(t, Z, B, ivb, st, ivp, ivn); break;
+        case 11: launch_fp64_fft<11>(t, Z, B, ivb, st, ivp, ivn); break;
+        default: launch_fp64_fft<12>(t, Z, B, ivb, st, ivp, ivn); break;
+        }
+        count_launch();
+        return;
+    }
+    const int64_t blocks = (B + warps - 1) / warps;
     if (ivn)
         k_path_fp64<2, true><<<(unsigned)blocks, warps * 32, smem, st>>>(t, Z, B, (double2*)ivb, nullptr,
                                                                          (double2*)ivn);

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include <vector_types.h>
+
 #include "rbergomi_gb300.h"
 
 namespace rbg {
@@ -88,7 +90,21 @@ struct Fp64Tables {
     const double* comp;
     int n_vol, n_vg, n_out, N;
     double xi;
+    // FFT convolution (logL > 0): per pass v the spectrum FFT(Gamma_v, zero-
+    // padded to L = 2^logL, Gamma_v[0] = 0) / L, and exp(-2 pi i q / L)
+    const double2* spec;
+    const double2* tw;
+    int logL;
 };
+
+// FP64 Volterra sum by FFT from this many steps (the direct sum below);
+// transforms up to 2^kFp64FftMaxLogL points
+constexpr int kFp64FftMinN = 200;
+constexpr int kFp64FftMaxLogL = 12;
+// log2 L of the FP64 form's FFT for N steps (L >= 2N - 1), 0 when it cannot run
+int fp64_fft_log2_len(int N);
+// host tables of the FP64 FFT: spec [n_vol][L], tw [L] (complex doubles)
+void fp64_fft_tables(const double* gamma, int n_vol, int N, int logL, double* spec, double* tw);
 
 // ns normal streams per path: 2 (W1, W1perp) for RT, 3 (+ Wperp) for plain MC
 void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream, int ns = 2);
