@@ -1,6 +1,6 @@
 """The FP64 form's FFT Volterra convolution (k_path_fp64_fft): Stockham
 radix-4/2 transforms in FP64, two paths per complex transform, used by AUTO
-from 256 steps.  Against the oracle (a direct causal sum) on identical
+from 200 steps.  Against the oracle (a direct causal sum) on identical
 normals at the same 1e-12 as the direct kernel, and against the direct
 kernel itself, for RT, plain Monte Carlo, the control-variate form (the
 antithetic variant) and the per-path quadrature."""
