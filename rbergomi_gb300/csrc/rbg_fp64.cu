@@ -6,6 +6,9 @@
 //                  causal FP64 sum, X = Y2 + a1 W1 + a2 W1perp, then for every
 //                  variance group v, Ivdt = dt sum v, IsvdW = sum sqrt(v) sdt W1
 //                  (rBergLib/rBergomiMT.cpp:73-109, 163-167, 427-436)
+//   k_path_fp64_fft  the same pass with Y2 as an FP64 FFT convolution, two
+//                  paths per complex transform (from 200 steps; the direct
+//                  sum's N^2 / 2 DFMA per path outgrow it there)
 //   k_payoff_sums  conditional BS per (path, output) and compensated per-chunk
 //                  sums of x and x^2 (rBergomiMT.cpp:598-602, 404-409)
 //   k_accumulate   fixed-order Neumaier merge of chunk sums (deterministic)
