@@ -113,16 +113,19 @@ __global__ void k_path_fp64(Fp64Tables t, const double* __restrict__ Z, int64_t 
             const VGDev vg = t.vgs[g];
             const double* comp = t.comp + (size_t)g * N;
             double sv = 0.0, sw = 0.0, sp = 0.0, nv = 0.0, nw = 0.0;
+            // sqrt(v_j) = sqrt(xi) exp(a_j / 2) and v_j = sqrt(v_j)^2: one exp, no sqrt per step
+            const double sxi = sqrt(vg.xi);
             for (int j = lane; j < vg.nsteps; j += 32) {
-                const double vj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * X[j - 1]) - comp[j - 1]);
+                const double su = (j == 0) ? sxi : sxi * exp(0.5 * (vg.eta * (vg.scale * X[j - 1]) - comp[j - 1]));
+                const double vj = (j == 0) ? vg.xi : su * su;
                 sv += vj;
-                const double sq = sqrt(vj) * vg.sdt;
+                const double sq = su * vg.sdt;
                 sw += sq * W1s[j];
                 if (NS == 3) sp += sq * Wperp[j];
                 if (ANTI) {
-                    const double uj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * -X[j - 1]) - comp[j - 1]);
-                    nv += uj;
-                    nw += sqrt(uj) * vg.sdt * -W1s[j];
+                    const double sa = (j == 0) ? sxi : sxi * exp(0.5 * (vg.eta * (vg.scale * -X[j - 1]) - comp[j - 1]));
+                    nv += (j == 0) ? vg.xi : sa * sa;
+                    nw += sa * vg.sdt * -W1s[j];
                 }
             }
 #pragma unroll
@@ -292,17 +295,19 @@ __global__ void __launch_bounds__(kFftThreads) k_path_fp64_fft(Fp64Tables t, con
             const double* comp = t.comp + (size_t)g * N;
             double sv = 0.0, sw = 0.0, sp2 = 0.0, nv = 0.0, nw = 0.0;
             if (active) {
+                const double sxi = sqrt(vg.xi);
                 for (int j = jt; j < vg.nsteps; j += 128) {
                     const double xp = (j == 0) ? 0.0 : (half ? y[j - 1].y : y[j - 1].x);
-                    const double vj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * xp) - comp[j - 1]);
+                    const double su = (j == 0) ? sxi : sxi * exp(0.5 * (vg.eta * (vg.scale * xp) - comp[j - 1]));
+                    const double vj = (j == 0) ? vg.xi : su * su;
                     sv += vj;
-                    const double sq = sqrt(vj) * vg.sdt;
+                    const double sq = su * vg.sdt;
                     sw += sq * W1[j];
                     if (NS == 3) sp2 += sq * W1[2 * N + j];
                     if (ANTI) {
-                        const double uj = (j == 0) ? vg.xi : vg.xi * exp(vg.eta * (vg.scale * -xp) - comp[j - 1]);
-                        nv += uj;
-                        nw += sqrt(uj) * vg.sdt * -W1[j];
+                        const double sa = (j == 0) ? sxi : sxi * exp(0.5 * (vg.eta * (vg.scale * -xp) - comp[j - 1]));
+                        nv += (j == 0) ? vg.xi : sa * sa;
+                        nw += sa * vg.sdt * -W1[j];
                     }
                 }
             }
