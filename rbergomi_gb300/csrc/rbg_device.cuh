@@ -123,19 +123,7 @@ __device__ __forceinline__ float sobol_normal_f32(unsigned int q)
     return __uint_as_float(__float_as_uint(z) ^ (up & 0x80000000u));
 }
 
-// FP64 Box-Muller on uniforms (x + 1/2) 2^-32.
-__device__ __forceinline__ void box_muller_f64(uint32_t a, uint32_t b, double& z0, double& z1)
-{
-    const double u0 = ((double)a + 0.5) * 2.3283064365386963e-10;
-    const double u1 = ((double)b + 0.5) * 2.3283064365386963e-10;
-    const double r = sqrt(-2.0 * log(u0));
-    double s, c;
-    sincospi(2.0 * u1, &s, &c);
-    z0 = r * c;
-    z1 = r * s;
-}
-
-// FP32 Box-Muller on the same uniforms (mixed form), on the MUFU pipe:
+// FP32 Box-Muller on uniforms (x + 1/2) 2^-32 (mixed form), on the MUFU pipe:
 // r = sqrt(-2 ln 2 log2 u0); the angle is taken as t = 2 pi u1 - pi, which
 // lies in (-pi, pi) where sin/cos.approx are accurate, and
 // cos(2 pi u1) = -cos t, sin(2 pi u1) = -sin t.

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <mutex>
 
 #include "rbg_device.cuh"
 #include "rbg_internal.hpp"
@@ -26,6 +27,77 @@
 namespace rbg {
 
 // ------------------------------------------------------------------ normals
+// FP64 Box-Muller by table-driven logarithm and sine/cosine (P. T. P. Tang's
+// table method, ACM TOMS 15 (1989) and 16 (1990)): the same normals as
+// sqrt(-2 ln u0) (cos, sin)(2 pi u1) on uniforms (x + 1/2) 2^-32 to a few
+// 1e-16, with about 40 FP64 operations per pair instead of the library log
+// and sincospi's 60-odd -- this kernel is bound by GB300's FP64 pipe.
+//   ln u0: u0 = q 2^-33 with q = 2a + 1 odd; q = 2^e m, m in [1, 2), and
+//     ln m = ln c_k + log1p((m - c_k) / c_k) at the nearest of 128 centres
+//     c_k = 1 + (k + 1/2) / 128 (|t| <= 2^-8, Mercator series to t^7).  The top
+//     interval, u0 >= 1 - 2^-8, takes log1p(u0 - 1) with u0 - 1 exact, so
+//     sqrt(-2 ln u0) keeps its relative accuracy as u0 -> 1.
+//   2 pi u1 = pi p 2^-32 with p = 2b + 1: the nearest table angle pi k / 128
+//     plus |d| <= pi / 256, whose sine and cosine are Taylor series to d^7.
+// The tables come from CUDA's own sincospi, division and log, once per device.
+__device__ double2 g_bm_trig[256];  // (cos, sin)(pi k / 128)
+__device__ double2 g_bm_logt[128];  // (1 / c_k, ln c_k)
+
+__global__ void k_bm_tables()
+{
+    const int k = threadIdx.x;
+    double sn, cs;
+    sincospi(k / 128.0, &sn, &cs);
+    g_bm_trig[k] = make_double2(cs, sn);
+    if (k < 128) {
+        const double c = 1.0 + (k + 0.5) / 128.0;
+        g_bm_logt[k] = make_double2(1.0 / c, log(c));
+    }
+}
+
+// log1p(t) for |t| <= 2^-8: t - t^2/2 + ... + t^7/7 (truncation below 2^-66)
+__device__ __forceinline__ double log1p_small(double t)
+{
+    double p = 1.0 / 7;
+    p = fma(p, t, -1.0 / 6);
+    p = fma(p, t, 1.0 / 5);
+    p = fma(p, t, -1.0 / 4);
+    p = fma(p, t, 1.0 / 3);
+    p = fma(p, t, -1.0 / 2);
+    p = fma(p, t, 1.0);
+    return p * t;
+}
+
+__device__ __forceinline__ void box_muller_f64_tab(uint32_t a, uint32_t b, double& z0, double& z1)
+{
+    // ln 2 split so that (e - 33) ln2_hi is exact for |e - 33| <= 33 (the fdlibm constants)
+    constexpr double kLn2Hi = 6.93147180369123816490e-01, kLn2Lo = 1.90821492927058770002e-10;
+    const uint64_t q = 2ull * a + 1ull;  // u0 = q 2^-33, q < 2^33
+    double lnu;
+    if (q >= 0x1FE000000ull) {
+        lnu = log1p_small((double)(int64_t)(q - (1ull << 33)) * 0x1p-33);
+    } else {
+        const uint64_t bits = (uint64_t)__double_as_longlong((double)q);
+        const int e = (int)(bits >> 52) - 1023;
+        const int k = (int)(bits >> 45) & 127;
+        const double m = __longlong_as_double((long long)((bits & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull));
+        const double2 lc = g_bm_logt[k];
+        const double t = (m - (1.0 + (k + 0.5) * 0.0078125)) * lc.x;
+        const double ef = (double)(e - 33);
+        lnu = fma(ef, kLn2Hi, lc.y + fma(ef, kLn2Lo, log1p_small(t)));
+    }
+    const double r = sqrt(-2.0 * lnu);
+    const uint64_t p = 2ull * b + 1ull;  // 2 pi u1 = pi p 2^-32
+    const uint64_t kk = (p + (1ull << 24)) >> 25;
+    const double d = (double)(int64_t)(p - (kk << 25)) * (3.14159265358979323846 * 0x1p-32);
+    const double d2 = d * d;
+    const double sd = d * fma(fma(fma(-1.0 / 5040, d2, 1.0 / 120), d2, -1.0 / 6), d2, 1.0);
+    const double cd = fma(fma(fma(-1.0 / 720, d2, 1.0 / 24), d2, -0.5), d2, 1.0);
+    const double2 cs = g_bm_trig[kk & 255];
+    z0 = r * fma(cs.x, cd, -cs.y * sd);
+    z1 = r * fma(cs.y, cd, cs.x * sd);
+}
+
 // Z[m][s][j], s < ns: W1, W1perp and (plain MC) Wperp on Philox streams 0, 1, 2.
 template <int F32>
 __global__ void k_normals(uint64_t seed, int64_t path0, int64_t B, int N, int ns, double* __restrict__ Z)
@@ -46,8 +118,8 @@ __global__ void k_normals(uint64_t seed, int64_t path0, int64_t B, int N, int ns
             box_muller_f32(x.z, x.w, f2, f3);
             z[0] = f0; z[1] = f1; z[2] = f2; z[3] = f3;
         } else {
-            box_muller_f64(x.x, x.y, z[0], z[1]);
-            box_muller_f64(x.z, x.w, z[2], z[3]);
+            box_muller_f64_tab(x.x, x.y, z[0], z[1]);
+            box_muller_f64_tab(x.z, x.w, z[2], z[3]);
         }
         double* o = Z + (m * ns + s) * (int64_t)N + 4 * g;
         const int left = N - 4 * g;
@@ -61,6 +133,20 @@ __global__ void k_normals(uint64_t seed, int64_t path0, int64_t B, int N, int ns
 
 void launch_normals(uint64_t seed, int64_t path0, int64_t B, int N, int f32, double* Z, void* stream, int ns)
 {
+    if (!f32) {
+        // the Box-Muller tables, once per device (the stream is synchronised so that
+        // launches on other streams find them written)
+        static std::mutex mu;
+        static bool ready[64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        std::lock_guard<std::mutex> lk(mu);
+        if (dev >= 0 && dev < 64 && !ready[dev]) {
+            k_bm_tables<<<1, 256, 0, (cudaStream_t)stream>>>();
+            count_launch();
+            if (cudaStreamSynchronize((cudaStream_t)stream) == cudaSuccess) ready[dev] = true;
+        }
+    }
     const int64_t total = B * ns * ((N + 3) / 4);
     const int threads = 256;
     int64_t blocks = (total + threads - 1) / threads;
