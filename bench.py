@@ -13,9 +13,15 @@ the mixed form timed with CUDA events on the launching stream, L2 flushed
 (256 MiB write) before every timed step.  `e2e` is the same metric through
 the drop-in C-ABI call computeIVRT_tensor with host buffers.  The FP64 form
 is timed on the same workload, and the mixed prices are compared with the
-FP64 form on identical normals.  `--impl reference` times the CPU oracle
-(the C restatement of the reference's OpenMP path) on a bounded sample of
-the same workload on all host cores.
+FP64 form on identical normals.  At one GPU the line also carries a
+`serving` object: the 10,000-request Poisson stream (200 requests/s, mixed
+parameters, N and M log-uniform) replayed through the serving loop, with
+p50 / p99 / max latency, prices/s and path-steps/s delivered, the sampled
+clocks of that window, and the plain FP64 form one request at a time on a
+sample of the same stream (`--skip-serving` leaves it out).
+`--impl reference` times the CPU oracle (the C restatement of the
+reference's OpenMP path) on a bounded sample of the same workload on all
+host cores.
 """
 from __future__ import annotations
 
@@ -416,6 +422,10 @@ def run_gpu(args, w):
     if prec == R.MIXED:
         roof["issue"] = issue_roofline(kname, path_steps(w) / max(1, kn // args.steps), avg_kernel_ms, line["clocks"])
     line.update(extra)
+    if ws == 1 and not args.skip_serving:
+        # the serving workload (10,000 Poisson requests at 200/s, about a minute),
+        # after the timed region of the headline workload
+        line["serving"] = serve_stream(args, local)
     print(json.dumps(line))
 
 
@@ -560,21 +570,20 @@ def serving_requests(n: int, rate: float, seed: int = 20261203):
     return reqs
 
 
-def run_serving(args):
+def serve_stream(args, local: int) -> dict:
+    """Replays the Poisson request stream through the serving loop
+    (rbg_server_*) and returns its latency, throughput and server figures,
+    with the plain FP64 form one request at a time on a sample beside it."""
     import threading
 
     import rbergomi_gb300 as R
 
-    ws, rank, local = dist_env()
-    import torch
-    torch.cuda.set_device(local)
-    R.lib()
     reqs = serving_requests(args.requests, args.rate)
     # warm the kernels and the allocator on a few off-schedule requests
     with R.Server() as srv:
         for r in reqs[:8]:
             srv.wait(srv.submit(r["xi"], r["H"], r["eta"], r["rho"], r["T"], r["K"], r["N"], 1 << 14, seed=r["seed"]))
-    lat = [None] * len(reqs)
+    lat = np.zeros((len(reqs), 3))
     n0 = R.launch_count()
     with ClockSampler(local) as clk:
         with R.Server(use_graphs=0 if args.no_graphs else 1) as srv:
@@ -596,14 +605,21 @@ def run_serving(args):
             th.start()
             for i in range(len(reqs)):
                 ready.acquire()
-                _, _, _, lat[i] = srv.wait(tickets[i])
+                lat[i] = srv.wait_timed(tickets[i])[3]
             th.join()
             wall = time.perf_counter() - wall0
             st = srv.stats()
     launches = R.launch_count() - n0
-    lat = np.array(lat)
+    total = lat[:, 2]
     prices = sum(len(r["K"]) for r in reqs)
     psteps = sum(r["M"] * r["N"] for r in reqs)
+    worst = int(np.argmax(total))
+    w = reqs[worst]
+    # what was in flight when the slowest request arrived: requests submitted in
+    # the 50 ms before it that had not finished by its arrival
+    t_w = w["t"]
+    overlap = [i for i in range(max(0, worst - 200), worst)
+               if reqs[i]["t"] + total[i] / 1e3 > t_w]
     # FP64 one-request-at-a-time form on a sample of the same stream
     fp64 = None
     if args.fp64_sample > 0:
@@ -619,17 +635,39 @@ def run_serving(args):
                 "path_steps_per_s": sum(r["M"] * r["N"] for r in samp) / dt,
                 "p50_ms_alone": float(np.percentile(tl, 50)), "max_ms_alone": float(np.max(tl)),
                 "note": "one request at a time, no queueing: latency is service time only"}
-    line = {
-        "metric": "serving prices/s (p50/p99 latency ms)", "value": prices / wall, "unit": "prices/s",
-        "n_gpus": ws, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * wall, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3+f32+f64", "data": "synthetic request stream",
-        "config": {"workload": "serving-poisson", "requests": len(reqs), "rate_per_s": args.rate,
-                   "graphs": not args.no_graphs},
-        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-        "max_ms": float(np.max(lat)), "mean_ms": float(np.mean(lat)),
-        "path_steps_per_s": psteps / wall, "requests_per_s": len(reqs) / wall,
+    return {
+        "workload": "serving-poisson", "requests": len(reqs), "rate_per_s": args.rate, "graphs": not args.no_graphs,
+        "p50_ms": float(np.percentile(total, 50)), "p99_ms": float(np.percentile(total, 99)),
+        "max_ms": float(np.max(total)), "mean_ms": float(np.mean(total)),
+        "queue_p99_ms": float(np.percentile(lat[:, 0], 99)), "service_p99_ms": float(np.percentile(lat[:, 1], 99)),
+        "prices_per_s": prices / wall, "path_steps_per_s": psteps / wall, "requests_per_s": len(reqs) / wall,
+        "wall_s": wall,
+        "slowest": {"index": worst, "N": w["N"], "M": w["M"], "strikes": len(w["K"]), "path_steps": w["M"] * w["N"],
+                    "queue_ms": float(lat[worst, 0]), "service_ms": float(lat[worst, 1]),
+                    "in_flight_at_arrival": len(overlap),
+                    "in_flight_path_steps": float(sum(reqs[i]["M"] * reqs[i]["N"] for i in overlap))},
         "server": st, "gpu_launches": launches, "clocks": clk.summary(), "fp64_one_at_a_time": fp64,
     }
+
+
+def run_serving(args):
+    import torch
+
+    import rbergomi_gb300 as R
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    R.lib()
+    sv = serve_stream(args, local)
+    line = {
+        "metric": "serving prices/s (p50/p99 latency ms)", "value": sv["prices_per_s"], "unit": "prices/s",
+        "n_gpus": ws, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * sv["wall_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3+f32+f64", "data": "synthetic request stream",
+        "config": {"workload": "serving-poisson", "requests": sv["requests"], "rate_per_s": args.rate,
+                   "graphs": not args.no_graphs},
+        "gpu_launches": sv["gpu_launches"], "clocks": sv["clocks"],
+    }
+    line.update({k: v for k, v in sv.items() if k not in line})
     if rank == 0:
         print(json.dumps(line))
 
@@ -656,6 +694,8 @@ def main():
     ap.add_argument("--fp64-sample", type=int, default=20, help="serving: FP64 one-at-a-time sample size")
     ap.add_argument("--no-graphs", action="store_true", help="serving: launch without CUDA graphs")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-serving", action="store_true",
+                    help="headline workload: leave out the serving replay that the default line carries")
     args = ap.parse_args()
     if args.workload == "serving-poisson":
         run_serving(args)

@@ -194,6 +194,16 @@ int rbg_price_rt_cv_normals(const rbg_cv_params* p, const double* Zc, const doub
  * sum2[i] = sum_m x^2 over this call's paths (for merging shards/replicas). */
 int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, double* sum2);
 
+/* Merges path shards (or replicas on disjoint path ranges): sum and sum2 are
+ * [n_shards][n] arrays of rbg_price_rt_sums outputs (n_shards = 1 after the
+ * caller's own all-reduce), M the total path count over all shards.  Adds
+ * the shards in index order with Neumaier compensation, then applies the
+ * reference's moment formula (rBergLib/rBergomiMT.cpp:404-409):
+ * price = S / M, stat = sqrt(S2 / M - price^2) / sqrt(M).  Host-only; no GPU
+ * needed.  Implied vols of the merged prices: rbg_implied_vol. */
+int rbg_merge_sums(int n_shards, int n, const double* sum, const double* sum2, int64_t M, double* price,
+                   double* stat);
+
 /* Per-path payoffs for caller-supplied normals (quadrature layout).  Z and
  * payoff are host pointers unless device_ptrs != 0, in which case both are
  * device pointers on the current device.  o->precision RBG_MIXED runs the
@@ -359,6 +369,10 @@ int rbg_server_poll(rbg_server* s, uint64_t ticket, int* done);
  * implied vols (any may be NULL) and the latency from submit to completion,
  * and forgets the ticket.  Returns the request's status. */
 int rbg_server_wait(rbg_server* s, uint64_t ticket, double* price, double* stat, double* iv, double* latency_ms);
+/* rbg_server_wait with the latency split: times[0] = submit to admission
+ * (queueing), times[1] = admission to results on the host (service),
+ * times[2] = their sum, all in ms (times may be NULL). */
+int rbg_server_wait_timed(rbg_server* s, uint64_t ticket, double* price, double* stat, double* iv, double* times);
 int rbg_server_get_stats(rbg_server* s, rbg_server_stats* st);
 /* Finishes the queued work and frees the server. */
 int rbg_server_destroy(rbg_server* s);
@@ -374,11 +388,16 @@ const char* rbg_server_last_error(void);
  * until exit; no device memory is allocated or freed.  Limits: at most 4096
  * outputs, and the job's tables must fit the array (RBG_ERR_ARG with a
  * message from rbg_static_last_error() otherwise); M is unbounded (paths are
- * processed in batches that fit).  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) and should come before any
- * stream capture.  All calls share the array and see the previous call's
- * contents; each call clears what must start at zero.  Calls that overlap on
- * the GPU race on the array: serialise them. */
+ * processed in batches that fit, cut at the same payoff-chunk boundaries as
+ * rbg_price_rt's, so prices agree to FP64 roundoff).  A NULL o->stream runs
+ * on the calling thread's per-thread default stream.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and
+ * should come before any stream capture; the address is kept for the life
+ * of the process, so cudaDeviceReset between calls is not supported.  All
+ * calls share the array and see the previous call's contents; each call
+ * clears what must start at zero.  Calls that overlap on the GPU race on the
+ * array: serialise them.  A call that fails after queuing work waits for
+ * that work before returning. */
 int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv);
 size_t rbg_static_scratch_bytes(void);
 const char* rbg_static_last_error(void);

@@ -11,7 +11,7 @@
  *     (deterministic inputs W1 = W1perp = cos(i*m)), reproduced to the dump's
  *     6 printed digits;
  *   - the reference library itself, compiled from its own sources against
- *     from-scratch FFTW/Boost shims (oracle/build_ref.sh), on seeded normals;
+ *     from-scratch FFTW/Boost shims (the `ref` target of oracle/Makefile), on seeded normals;
  *     the outputs of that build are frozen in tests/golden/.
  *
  * Every function cites the reference file:line it restates.  The one deliberate

@@ -2,7 +2,7 @@
  * fftw3.h -- minimal, from-scratch stand-in for the FFTW3 API subset the
  * reference rBergLib sources call (fftw_complex, fftw_plan_dft_1d,
  * fftw_execute, FFTW_FORWARD/BACKWARD, FFTW_ESTIMATE).  TEST INFRASTRUCTURE:
- * it exists only so oracle/build_ref.sh can compile the unmodified reference
+ * it exists only so oracle/Makefile (target `ref`) can compile the unmodified reference
  * sources into oracle/_ref/ on a machine without FFTW.
  *
  * Semantics follow FFTW's documented unnormalised complex DFT of arbitrary

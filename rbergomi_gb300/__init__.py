@@ -66,7 +66,8 @@ EXPORTS = [
     "rbg_server_poll", "rbg_server_wait", "rbg_server_get_stats", "rbg_server_destroy", "rbg_server_last_error",
     "rbg_price_rt_unordered", "computeIV_tensor", "rbg_price_mc", "rbg_payoffs_mc", "rbg_generate_normals_streams",
     "rbg_plan_info_mc", "rbg_plan_info_unordered", "rbg_price_rt_cv", "rbg_price_rt_cv_normals",
-    "rbg_price_rt_sobol", "rbg_sobol_normals", "rbg_debug_wait_timeout",
+    "rbg_price_rt_sobol", "rbg_sobol_normals", "rbg_debug_wait_timeout", "rbg_merge_sums",
+    "rbg_server_wait_timed",
 ]
 
 STAGE_NORMALS, STAGE_PATH_FP64, STAGE_MIXED, STAGE_PAYOFF, STAGE_REDUCE = 0, 1, 2, 3, 4
@@ -95,6 +96,8 @@ def lib():
         L.rbg_price_rt.restype = C.c_int
         L.rbg_price_rt_sums.argtypes = [P, O, _dp, _dp]
         L.rbg_price_rt_sums.restype = C.c_int
+        L.rbg_merge_sums.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int64, _dp, _dp]
+        L.rbg_merge_sums.restype = C.c_int
         L.rbg_payoffs_rt.argtypes = [P, O, C.c_void_p, C.c_void_p, C.c_int]
         L.rbg_payoffs_rt.restype = C.c_int
         L.rbg_price_mc.argtypes = [P, O, _dp, _dp, _dp]
@@ -299,6 +302,21 @@ def price_rt_sums(xi, H, eta, rho, T, K, N, M, **opts):
     s1, s2 = np.empty(p.out), np.empty(p.out)
     _check(lib().rbg_price_rt_sums(C.byref(p.s), C.byref(o), s1.ctypes.data_as(_dp), s2.ctypes.data_as(_dp)))
     return s1, s2
+
+
+def merge_sums(s1, s2, M):
+    """(price, stat) of path shards through rbg_merge_sums: s1, s2 are
+    [n_shards, out] (or [out] after an all-reduce) arrays of price_rt_sums
+    outputs, M the total path count.  Host-only."""
+    s1 = np.ascontiguousarray(np.atleast_2d(np.asarray(s1, dtype=np.float64)))
+    s2 = np.ascontiguousarray(np.atleast_2d(np.asarray(s2, dtype=np.float64)))
+    if s1.shape != s2.shape:
+        raise ValueError("sum and sum2 must have the same shape")
+    n_shards, n = s1.shape
+    price, stat = np.empty(n), np.empty(n)
+    _check(lib().rbg_merge_sums(n_shards, n, s1.ctypes.data_as(_dp), s2.ctypes.data_as(_dp), int(M),
+                                price.ctypes.data_as(_dp), stat.ctypes.data_as(_dp)))
+    return price, stat
 
 
 def payoffs_rt(xi, H, eta, rho, T, K, Z, device_ptrs=False, M=None, N=None, **opts):
@@ -533,6 +551,8 @@ def _server_lib():
         L.rbg_server_poll.restype = C.c_int
         L.rbg_server_wait.argtypes = [SP, C.c_uint64, _dp, _dp, _dp, _dp]
         L.rbg_server_wait.restype = C.c_int
+        L.rbg_server_wait_timed.argtypes = [SP, C.c_uint64, _dp, _dp, _dp, _dp]
+        L.rbg_server_wait_timed.restype = C.c_int
         L.rbg_server_get_stats.argtypes = [SP, C.POINTER(RbgServerStats)]
         L.rbg_server_get_stats.restype = C.c_int
         L.rbg_server_destroy.argtypes = [SP]
@@ -579,6 +599,18 @@ class Server:
         if rc:
             raise RbgError(f"request status {rc}: {_server_lib().rbg_server_last_error().decode()}")
         return price, stat, iv, lat.value
+
+    def wait_timed(self, ticket):
+        """wait() with the latency split: (price, stat, iv, (queue_ms,
+        service_ms, total_ms)), queue = submit to admission onto a slot."""
+        n = self._nout.pop(ticket)
+        price, stat, iv, t = np.empty(n), np.empty(n), np.empty(n), np.empty(3)
+        rc = _server_lib().rbg_server_wait_timed(self._h, ticket, price.ctypes.data_as(_dp),
+                                                 stat.ctypes.data_as(_dp), iv.ctypes.data_as(_dp),
+                                                 t.ctypes.data_as(_dp))
+        if rc:
+            raise RbgError(f"request status {rc}: {_server_lib().rbg_server_last_error().decode()}")
+        return price, stat, iv, (float(t[0]), float(t[1]), float(t[2]))
 
     def stats(self) -> dict:
         s = RbgServerStats()

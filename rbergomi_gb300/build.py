@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 SOURCES = ["rbg_plan.cpp", "rbg_api.cpp", "rbg_fp64.cu", "rbg_mixed.cu", "rbg_fft.cu", "rbg_static.cu", "rbg_qmc.cu",
-           "rbg_server.cpp"]
+           "rbg_server.cpp", "rbg_cxx.cpp"]
 
 
 def nvcc() -> str:
@@ -36,7 +36,7 @@ def _compile(src: str) -> str:
     obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     deps = [path] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hpp", ".cuh"))]
-    deps.append(os.path.join(ROOT, "include", "rbergomi_gb300.h"))
+    deps += [os.path.join(ROOT, "include", h) for h in ("rbergomi_gb300.h", "rbergomi_gb300.hpp")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc()] + ARCH + COMMON + ["-c", path, "-o", obj]

@@ -89,6 +89,14 @@ static void prof_collect()
 static thread_local uint64_t g_h2d = 0, g_d2h = 0;
 
 
+static void host_neumaier_add(double& s, double& c, double x)
+{
+    const double t = s + x;
+    if (std::fabs(s) >= std::fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+}
+
 static int fail(int code, const std::string& msg)
 {
     g_err = msg;
@@ -261,7 +269,42 @@ static int upload_tables(Ctx& c, const Plan& plan, cudaStream_t st, TableSet& ts
 }
 
 // ------------------------------------------------------------ FP64 form
-static const int64_t kChunkTarget = 608;  // ~4 chunks per SM of a 152-SM part
+uint64_t fold_seed(const uint64_t* seed, int seed_size)
+{
+    if (!seed || seed_size <= 0) return 0;
+    uint64_t h = seed[0];
+    for (int i = 1; i < seed_size; ++i) {
+        uint64_t x = h + seed[i];
+        x += 0x9E3779B97F4A7C15ull;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        h = x ^ (x >> 31);
+    }
+    return h;
+}
+
+// SMs per device, looked up once per ordinal (the attribute query is cheap,
+// but this runs on every call)
+int device_sms()
+{
+    static std::mutex mu;
+    static std::map<int, int> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = 1;
+    }
+    cache[dev] = n;
+    return n;
+}
 
 static int64_t fp64_batch(const Plan& plan, int64_t M, int ns = 2)
 {
@@ -293,7 +336,7 @@ static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M,
     if ((rc = ensure(c.ivb, sizeof(double) * 2 * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
     if (mc && (rc = ensure(c.ivp, sizeof(double) * plan.vgs.size() * (size_t)B, "variance sums"))) return rc;
     double* ivp = mc ? c.ivp.as<double>() : nullptr;
-    const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
+    const int G = payoff_paths_per_thread(B, device_sms());
     const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
     if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
     if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
@@ -353,7 +396,7 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
         return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend (N <= 1024)");
     const int64_t B = job.batch;
     if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
-    const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
+    const int G = payoff_paths_per_thread(B, job.sms);
     const int64_t max_chunks = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
     if (!job.fused && (rc = ensure(c.ivb, sizeof(float) * 2 * plan.vgs.size() * (size_t)B, "variance sums")))
         return rc;
@@ -465,7 +508,7 @@ static int price_cv(Ctx& c, const Plan& plan, const rbg_cv_params& p, const rbg_
     double* Q = alpha + no;
     unsigned long long* count = (unsigned long long*)(Q + no);
     double* xy = (double*)(count + no);
-    const int G = (int)std::max<int64_t>(1, (B + 256 * kChunkTarget - 1) / (256 * kChunkTarget));
+    const int G = payoff_paths_per_thread(B, device_sms());
     const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
     if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
     if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
@@ -730,6 +773,31 @@ int rbg_price_rt_sums(const rbg_params* p, const rbg_options* o, double* sum, do
     const size_t no = res.size() / 5;
     if (sum) std::memcpy(sum, res.data() + 3 * no, no * sizeof(double));
     if (sum2) std::memcpy(sum2, res.data() + 4 * no, no * sizeof(double));
+    return RBG_OK;
+}
+
+int rbg_merge_sums(int n_shards, int n, const double* sum, const double* sum2, int64_t M, double* price,
+                   double* stat)
+{
+    if (n_shards < 1 || n < 0 || M < 1 || (n > 0 && (!sum || !sum2 || !price || !stat)))
+        return fail(RBG_ERR_ARG, "rbg_merge_sums: need n_shards >= 1, n >= 0, M >= 1 and non-null arrays");
+    const double invM = 1.0 / (double)M, isq = 1.0 / std::sqrt((double)M);
+    for (int i = 0; i < n; ++i) {
+        // shard order, Neumaier-compensated: the merge does not depend on how
+        // the caller's collective ordered its additions
+        double S = 0, C = 0, S2 = 0, C2 = 0;
+        for (int k = 0; k < n_shards; ++k) {
+            host_neumaier_add(S, C, sum[(size_t)k * n + i]);
+            host_neumaier_add(S2, C2, sum2[(size_t)k * n + i]);
+        }
+        S += C;
+        S2 += C2;
+        // rBergLib/rBergomiMT.cpp:404-409
+        const double pr = S * invM;
+        const double var = std::fma(-pr, pr, S2 * invM);
+        price[i] = pr;
+        stat[i] = std::sqrt(var > 0.0 ? var : 0.0) * isq;
+    }
     return RBG_OK;
 }
 
@@ -1158,19 +1226,6 @@ static void fill_tot(double* H, double* eta, double* rho, int par_size, double* 
     }
 }
 
-static uint64_t fold_seed(const uint64_t* seed, int seed_size)
-{
-    if (!seed || seed_size <= 0) return 0;
-    uint64_t h = seed[0];
-    for (int i = 1; i < seed_size; ++i) {
-        uint64_t x = h + seed[i];
-        x += 0x9E3779B97F4A7C15ull;
-        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-        h = x ^ (x >> 31);
-    }
-    return h;
-}
 
 static void check_dropin_sizes(int par_size, int op_size, int num_threads, int out_size)
 {
@@ -1202,7 +1257,7 @@ void computeIV_tensor(double xi, double* H, double* eta, double* rho, int par_si
     rbg_default_options(&o);
     const char* prec = std::getenv("RBG_PRECISION");
     if (prec && std::strcmp(prec, "mixed") == 0) o.precision = RBG_MIXED;
-    o.seed = fold_seed(seed, seed_size);
+    o.seed = rbg::fold_seed(seed, seed_size);
     die_on(rbg_price_mc(&p, &o, price, stat, iv));
     fill_tot(H, eta, rho, par_size, T, K, op_size, H_tot, rho_tot, eta_tot, T_tot, K_tot);
 }
@@ -1219,7 +1274,7 @@ void computeIVRT_tensor(double xi, double* H, double* eta, double* rho, int par_
     rbg_default_options(&o);
     const char* prec = std::getenv("RBG_PRECISION");
     if (prec && std::strcmp(prec, "mixed") == 0) o.precision = RBG_MIXED;
-    o.seed = fold_seed(seed, seed_size);
+    o.seed = rbg::fold_seed(seed, seed_size);
     die_on(rbg_price_rt(&p, &o, price, stat, iv));
     fill_tot(H, eta, rho, par_size, T, K, op_size, H_tot, eta_tot, rho_tot, T_tot, K_tot);
 }

@@ -154,4 +154,23 @@ void launch_implied_vol(int n, const double* price, const double* K, const doubl
 // Kernel-launch counter shared by all launchers.
 void count_launch(int n = 1);
 
+// The drop-in layer's seed folding: seed[0] for one word, splitmix64
+// chaining of the words otherwise, 0 for none (one 64-bit Philox key).
+uint64_t fold_seed(const uint64_t* seed, int seed_size);
+
+// SMs of the current device (cached per device ordinal; 1 if unknown).
+int device_sms();
+
+// Payoff-reduction chunking of a batch of B paths: chunks of 256 G paths,
+// one 256-thread block each, every thread summing G paths in FP32 (stride
+// 256).  G is the smallest that keeps the chunk count at about four per SM.
+// Results depend on G, so every entry point that must reproduce another's
+// sums takes G from this one rule and the same B.
+inline int payoff_paths_per_thread(int64_t B, int sms)
+{
+    const int64_t target = 4 * (int64_t)(sms > 0 ? sms : 1);
+    const int64_t g = (B + 256 * target - 1) / (256 * target);
+    return (int)(g > 1 ? g : 1);
+}
+
 }  // namespace rbg

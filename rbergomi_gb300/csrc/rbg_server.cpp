@@ -216,7 +216,7 @@ int Server::launch(Slot& s, Req& r, std::string& err)
     MixedJob& job = r.job;
     const int no = (int)r.plan.outs.size();
     const int64_t B = job.batch;
-    const int G = (int)std::max<int64_t>(1, (B + 256 * 608 - 1) / (256 * 608));
+    const int G = payoff_paths_per_thread(B, job.sms);
     const int64_t rows = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
     cudaError_t e = s.ws.ensure(job.workspace_bytes, st);
     if (e == cudaSuccess && !job.fused) e = s.ivb.ensure(sizeof(float) * 2 * r.plan.vgs.size() * (size_t)B, st);
@@ -549,6 +549,14 @@ int rbg_server_poll(rbg_server* srv, uint64_t ticket, int* done)
 
 int rbg_server_wait(rbg_server* srv, uint64_t ticket, double* price, double* stat, double* iv, double* latency_ms)
 {
+    double t[3];
+    const int rc = rbg_server_wait_timed(srv, ticket, price, stat, iv, t);
+    if (latency_ms) *latency_ms = t[2];
+    return rc;
+}
+
+int rbg_server_wait_timed(rbg_server* srv, uint64_t ticket, double* price, double* stat, double* iv, double* times)
+{
     if (!srv) return srv_fail(RBG_ERR_ARG, "null server");
     Server& s = *srv->s;
     std::unique_lock<std::mutex> lk(s.mu);
@@ -565,8 +573,14 @@ int rbg_server_wait(rbg_server* srv, uint64_t ticket, double* price, double* sta
     } else {
         g_srv_err = r->err;
     }
-    if (latency_ms)
-        *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    if (times) {
+        using ms = std::chrono::duration<double, std::milli>;
+        // a request that failed before admission has no start time
+        const Clock::time_point start = r->t_start.time_since_epoch().count() ? r->t_start : r->t_done;
+        times[0] = ms(start - r->t_submit).count();
+        times[1] = ms(r->t_done - start).count();
+        times[2] = ms(r->t_done - r->t_submit).count();
+    }
     s.reqs.erase(it);
     return status;
 }

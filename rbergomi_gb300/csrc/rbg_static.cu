@@ -12,11 +12,20 @@
 //
 // The device address of that array is looked up once per device, with the
 // device current, on the first call on that device (cudaGetSymbolAddress);
-// that first call should therefore come before any stream capture.  All
-// calls share the array and it keeps the last call's contents; what must
-// start at zero (the kernel error word and the running sums) is cleared by
-// every call.  Calls whose work overlaps on the GPU race on the array, so
-// callers serialise them (one stream, or their own ordering).
+// that first call should therefore come before any stream capture.  The
+// address stays cached for the life of the process, so a cudaDeviceReset
+// between calls is not supported.  All calls share the array and it keeps
+// the last call's contents; what must start at zero (the kernel error word
+// and the running sums) is cleared by every call.  Calls whose work overlaps
+// on the GPU race on the array, so callers serialise them (one stream, or
+// their own ordering).  A call that fails after it has queued work waits for
+// that work before it returns, so the next call never meets it on the array.
+//
+// The results equal rbg_price_rt's: the same batch size B and paths per
+// payoff thread G where the buffers fit; where they do not, B is cut to a
+// smaller whole number of 256 G-path payoff chunks, so every path is summed
+// in the same FP32 chunk as in rbg_price_rt and only the order of the FP64
+// merges of whole chunks changes.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -106,27 +115,38 @@ int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price
     const size_t off_part = up256(off_res + sizeof(double) * 5 * n_out);
     if (off_part >= kStaticScratchBytes)
         return static_fail(RBG_ERR_ARG, "tables of this job exceed the 16 MiB static scratch");
-    // batch B and per-thread path count G chosen as rbg_price_rt chooses them
-    // (G = ceil(B / (256 * 608))), halving B until ivb + partials fit; fused
-    // jobs need no ivb and one partial row per CTA
+    // batch B and paths per payoff thread G as rbg_price_rt chooses them; if
+    // the (Ivdt, IsvdW) buffer and partials do not fit, B is halved and cut
+    // down to whole payoff chunks of 256 G paths, G kept.  Fused jobs need no
+    // (Ivdt, IsvdW) buffer and one partial row per CTA.
     int64_t B = std::min<int64_t>(p->M, job.batch);
-    int G = 1;
+    const int G = payoff_paths_per_thread(B, job.sms);
+    const int64_t chunk = 256 * (int64_t)G;
     int64_t nchunk_max = 1;
     size_t off_ivb = 0;
     for (;;) {
-        G = (int)std::max<int64_t>(1, (B + 256 * 608 - 1) / (256 * 608));
-        nchunk_max = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+        nchunk_max = job.fused ? mixed_part_rows(job, B) : (B + chunk - 1) / chunk;
         off_ivb = up256(off_part + (size_t)32 * n_out * nchunk_max);
         const size_t ivb_bytes = job.fused ? 0 : (size_t)8 * plan.vgs.size() * B;
         if (off_ivb + ivb_bytes <= kStaticScratchBytes) break;
-        if (job.fused || B <= 256)
+        if (job.fused || B <= chunk)
             return static_fail(RBG_ERR_ARG, "variance groups / outputs of this job exceed the static scratch");
-        B = (B + 1) / 2;
+        B = std::max<int64_t>(chunk, (B / 2) / chunk * chunk);
     }
     void* base = nullptr;
     if ((rc = static_scratch(&base))) return rc;
     unsigned char* s = (unsigned char*)base;
-    cudaStream_t st = (cudaStream_t)o->stream;
+    // a null stream means the calling thread's per-thread default stream, which
+    // does not synchronise with the other streams of the process as the legacy
+    // default stream would
+    cudaStream_t st = o->stream ? (cudaStream_t)o->stream : cudaStreamPerThread;
+    // error exits once work is queued: let that work finish first, so that the
+    // caller's next call does not race it on the shared array
+    auto fail_queued = [&](int code, const std::string& msg) {
+        cudaStreamSynchronize(st);
+        cudaGetLastError();
+        return static_fail(code, msg);
+    };
 
     std::vector<OutDev> outs(n_out);
     std::vector<double> Tv(n_out);
@@ -139,33 +159,28 @@ int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price
         e = cudaMemcpyAsync(s + off_outs, outs.data(), sizeof(OutDev) * n_out, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s + off_T, Tv.data(), sizeof(double) * n_out, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(s + off_acc, 0, sizeof(double) * 4 * n_out, st);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return static_fail(RBG_ERR_CUDA, std::string("static scratch upload: ") + cudaGetErrorString(e));
-    }
+    if (e != cudaSuccess) return fail_queued(RBG_ERR_CUDA, std::string("static scratch upload: ") + cudaGetErrorString(e));
     for (int64_t m0 = 0; m0 < p->M; m0 += B) {
         const int64_t b = std::min(B, p->M - m0);
         if (job.fused) {
             const int rows = mixed_part_rows(job, b);
             e = cudaMemsetAsync(s + off_part, 0, (size_t)32 * n_out * rows, st);
-            if (e != cudaSuccess) {
-                cudaGetLastError();
-                return static_fail(RBG_ERR_CUDA, std::string("static scratch clear: ") + cudaGetErrorString(e));
-            }
+            if (e != cudaSuccess)
+                return fail_queued(RBG_ERR_CUDA, std::string("static scratch clear: ") + cudaGetErrorString(e));
             rc = mixed_launch(job, s + off_ws, o->seed, o->path_offset + m0, b, nullptr, st, err, nullptr, nullptr,
                               (double*)(s + off_part));
-            if (rc) return static_fail(rc, err);
+            if (rc) return fail_queued(rc, err);
             launch_accumulate((const double*)(s + off_part), rows, n_out, (double*)(s + off_acc), st);
             continue;
         }
         rc = mixed_launch(job, s + off_ws, o->seed, o->path_offset + m0, b, s + off_ivb, st, err);
-        if (rc) return static_fail(rc, err);
-        const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
+        if (rc) return fail_queued(rc, err);
+        const int nchunks = (int)((b + chunk - 1) / chunk);
         launch_payoff_sums_f32((const OutDev*)(s + off_outs), n_out, s + off_ivb, b, G, (double*)(s + off_part),
                                nchunks, st);
         launch_accumulate((const double*)(s + off_part), nchunks, n_out, (double*)(s + off_acc), st);
     }
-    if ((rc = mixed_check(job, s + off_ws, st, err))) return static_fail(rc, err);
+    if ((rc = mixed_check(job, s + off_ws, st, err))) return fail_queued(rc, err);
     launch_finalize((const double*)(s + off_acc), n_out, p->M, (const OutDev*)(s + off_outs),
                     (const double*)(s + off_T), o->compute_iv, (double*)(s + off_res), st);
     std::vector<double> res(5 * (size_t)n_out);
@@ -173,10 +188,7 @@ int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(res.data(), s + off_res, sizeof(double) * 5 * n_out, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return static_fail(RBG_ERR_CUDA, std::string("static pricing: ") + cudaGetErrorString(e));
-    }
+    if (e != cudaSuccess) return fail_queued(RBG_ERR_CUDA, std::string("static pricing: ") + cudaGetErrorString(e));
     std::memcpy(price, res.data(), sizeof(double) * n_out);
     std::memcpy(stat, res.data() + n_out, sizeof(double) * n_out);
     if (iv) std::memcpy(iv, res.data() + 2 * n_out, sizeof(double) * n_out);

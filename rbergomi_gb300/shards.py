@@ -4,10 +4,12 @@ Monte Carlo paths are independent, and a path's normals depend only on
 (seed, global path index, step).  So a run over M paths splits into
 contiguous path blocks, one per rank, with no data exchange during pricing.
 The one exchange is at the end: a sum of the per-output (sum x, sum x^2)
-pairs, 2 x out FP64 values, after which every rank applies the reference's
-mean / standard-error formula (rBergLib/rBergomiMT.cpp:404-409).  The
-merged result equals a single-process run over all M paths up to the order
-of the final FP64 additions.
+pairs, 2 x out FP64 values (torch.distributed, gloo or NCCL), after which
+every rank applies the reference's mean / standard-error formula
+(rBergLib/rBergomiMT.cpp:404-409) through the library's C++ merge,
+rbg_merge_sums.  The merged result equals a single-process run over all M
+paths up to the order of the final FP64 additions, when the shard
+boundaries fall on the payoff chunks (multiples of 256 G paths).
 """
 from __future__ import annotations
 
@@ -24,13 +26,13 @@ def shard_range(M: int, world_size: int, rank: int) -> tuple[int, int]:
 
 
 def merge_sums(s1, s2, M: int):
-    """(price, stat) from summed payoffs: price = sum x / M,
-    stat = sqrt(sum x^2 / M - price^2) / sqrt(M), as the reference computes them."""
-    s1 = np.asarray(s1, dtype=np.float64)
-    s2 = np.asarray(s2, dtype=np.float64)
-    price = s1 / M
-    var = s2 / M - price * price
-    return price, np.sqrt(np.maximum(var, 0.0)) / np.sqrt(M)
+    """(price, stat) from summed payoffs, by the library's C-ABI merge
+    (rbg_merge_sums): price = sum x / M, stat = sqrt(sum x^2 / M - price^2) /
+    sqrt(M), as the reference computes them.  s1, s2: [out] after an
+    all-reduce, or [n_shards, out] gathered per shard (merged in shard order)."""
+    from . import merge_sums as _merge
+
+    return _merge(s1, s2, M)
 
 
 def allreduce_sums(s1, s2, group=None):

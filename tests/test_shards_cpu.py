@@ -1,8 +1,12 @@
-"""Path sharding across ranks (the multi-GPU form of the pricer), tested on
-CPU with a world-size-2 gloo group: each rank prices its contiguous block of
+"""Path sharding across ranks (the multi-GPU form of the pricer).
+
+On CPU, a world-size-2 gloo group: each rank prices its contiguous block of
 paths (here with the oracle standing in for its GPU), one all-reduce merges
-the (sum x, sum x^2) pairs, and the merged price equals a single-process run
-over all paths."""
+the (sum x, sum x^2) pairs, the library's C-ABI merge (rbg_merge_sums)
+applies the moment formula, and the merged price equals a single-process run
+over all paths.  On the GPU, two gloo ranks both price their blocks with the
+real pricer (rbg_price_rt_sums) on cuda:0 -- their kernels never wait on
+each other -- and the merge equals one call over all paths."""
 import os
 import socket
 
@@ -52,6 +56,27 @@ def test_shard_ranges_cover_paths_once():
         shard_range(10, 2, 2)
 
 
+def test_merge_sums_c_abi_matches_reference_formula():
+    """rbg_merge_sums (host-only): shard-order merge of gathered sums and the
+    reference's moment formula, against the same arithmetic in numpy."""
+    import rbergomi_gb300 as R
+    rng = np.random.default_rng(5)
+    pay = rng.lognormal(-2.0, 0.7, size=(4, 1000, 6))  # 4 shards x 1000 paths x 6 outputs
+    s1, s2 = pay.sum(1), (pay * pay).sum(1)
+    M = 4000
+    price, stat = R.merge_sums(s1, s2, M)
+    want_p = s1.sum(0) / M
+    want_s = np.sqrt(s2.sum(0) / M - want_p ** 2) / np.sqrt(M)
+    np.testing.assert_allclose(price, want_p, rtol=1e-14, atol=0)
+    np.testing.assert_allclose(stat, want_s, rtol=1e-10, atol=0)
+    # one shard after an all-reduce: the same numbers
+    p1, st1 = R.merge_sums(s1.sum(0), s2.sum(0), M)
+    np.testing.assert_allclose(p1, price, rtol=1e-15, atol=0)
+    np.testing.assert_allclose(st1, stat, rtol=1e-12, atol=0)
+    with pytest.raises(R.RbgError):
+        R.merge_sums(s1, s2, 0)
+
+
 def test_two_rank_merge_equals_single_process(oracle):
     import torch.multiprocessing as mp
 
@@ -89,3 +114,53 @@ def test_sharded_single_rank_matches_direct():
             np.testing.assert_allclose(s, ds, rtol=1e-8, atol=0)
     finally:
         dist.destroy_process_group()
+
+
+def _gpu_rank(rank, ws, port, prec, q):
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import torch
+    import torch.distributed as dist
+
+    import rbergomi_gb300 as R
+    from rbergomi_gb300 import shards
+
+    torch.cuda.set_device(0)
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        price, stat = shards.price_rt_sharded(XI, H, ETA, RHO, T, K, 256, GPU_M, seed=SEED, precision=prec)
+        q.put((rank, price, stat, R.launch_count()))
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+GPU_M = 1 << 16  # two blocks of 2^15 paths: whole payoff chunks on both ranks
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec_name", ["FP64", "MIXED"])
+def test_two_rank_gpu_shards_equal_one_call(prec_name):
+    """Two gloo ranks, both on cuda:0, each price their contiguous path block
+    through rbg_price_rt_sums; one all-reduce plus rbg_merge_sums equals one
+    call over all paths (FP64 and mixed) to FP64 roundoff."""
+    import torch.multiprocessing as mp
+
+    import rbergomi_gb300 as R
+    prec = getattr(R, prec_name)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_gpu_rank, args=(r, 2, port, prec, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = [q.get(timeout=600) for _ in procs]
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    want_p, want_s, _ = R.price_rt(XI, H, ETA, RHO, T, K, 256, GPU_M, seed=SEED, precision=prec)
+    for _, price, stat, launches in got:
+        assert launches > 0  # each rank ran its own kernels
+        np.testing.assert_allclose(price, want_p, rtol=1e-13, atol=0)
+        np.testing.assert_allclose(stat, want_s, rtol=1e-9, atol=0)

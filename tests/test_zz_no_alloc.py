@@ -53,6 +53,10 @@ CASES = [
          seed=3),
     # longer horizon: the batched-FFT backend
     dict(xi=0.05, H=[0.1], eta=[1.5], rho=[-0.7], T=[2.0, 2.0, 2.0], K=[0.8, 1.0, 1.2], N=1500, M=3001, seed=4),
+    # eight variance groups over 300,001 paths: the (Ivdt, IsvdW) buffer (8 B per group and path, 19.2 MB)
+    # does not fit the 16 MiB array, so the paths run in smaller batches than rbg_price_rt's single one
+    dict(xi=0.04, H=[0.1], eta=[1.9], rho=[-0.9], T=[0.25, 0.5, 0.75, 1.0, 1.25, 1.5, 1.75, 2.0],
+         K=[0.8, 0.9, 1.0, 1.1, 1.2, 1.0, 0.95, 1.05], N=128, M=300001, seed=5),
 ]
 
 
