@@ -356,6 +356,9 @@ typedef struct rbg_server_config {
 typedef struct rbg_server_stats {
     uint64_t completed, failed, pending, in_flight, hbm_in_use;
     uint64_t table_cache_hits, table_cache_misses, graph_launches;
+    uint64_t graph_instantiations, graph_updates; /* executable graphs built / updated in place */
+    uint64_t max_launch_us;                       /* longest admission-to-launched time on the scheduler */
+    uint64_t pin_growths;                         /* pinned result buffers regrown (a device-wide wait each) */
 } rbg_server_stats;
 
 void rbg_server_default_config(rbg_server_config* cfg);

@@ -535,7 +535,8 @@ class RbgServerConfig(C.Structure):
 
 class RbgServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("completed", "failed", "pending", "in_flight", "hbm_in_use",
-                                          "table_cache_hits", "table_cache_misses", "graph_launches")]
+                                          "table_cache_hits", "table_cache_misses", "graph_launches",
+                                          "graph_instantiations", "graph_updates", "max_launch_us", "pin_growths")]
 
 
 def _server_lib():

@@ -49,22 +49,27 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-// Stream-ordered, grow-only device buffer.
+// Stream-ordered, grow-only device buffer from the server's memory pool.
 struct SBuf {
     void* p = nullptr;
     size_t n = 0;
-    cudaError_t ensure(size_t bytes, cudaStream_t st)
+    cudaError_t ensure(size_t bytes, cudaStream_t st, cudaMemPool_t pool)
     {
         if (bytes <= n) return cudaSuccess;
         if (p) cudaFreeAsync(p, st);
         p = nullptr;
         n = 0;
         const size_t want = std::max(bytes, (size_t)4096);
-        cudaError_t e = cudaMallocAsync(&p, want, st);
+        cudaError_t e = cudaMallocFromPoolAsync(&p, want, pool, st);
         if (e == cudaSuccess) n = want;
         return e;
     }
 };
+
+// Outputs the pinned result buffer of every slot holds from the start: a
+// slot that had to grow it would call cudaFreeHost, which waits for the
+// whole device (every request in flight) on the scheduler thread.
+constexpr size_t kPinOutputs = 4096;
 
 struct Req {
     uint64_t id = 0;
@@ -81,7 +86,7 @@ struct Req {
     std::string err;
     bool done = false;
     std::vector<int> cache_keys;  // cache entries pinned while in flight
-    Clock::time_point t_submit, t_start, t_done;
+    Clock::time_point t_submit, t_start, t_launched, t_done;
 };
 
 struct Slot {
@@ -119,12 +124,17 @@ struct Server {
     bool stop = false;
     std::thread thr;
     cudaStream_t copy_st = nullptr;
+    // device memory of slots and tables: a pool that keeps freed memory
+    // mapped (release threshold = all), so growing a buffer or replacing a
+    // table does not map new pages on the scheduler's path
+    cudaMemPool_t pool = nullptr;
     // table cache
     std::map<std::tuple<int, uint64_t, int, int>, int> cache_index;
     std::vector<CacheEntry> cache;
     std::list<int> lru;
     // statistics
     uint64_t completed = 0, failed = 0, cache_hits = 0, cache_misses = 0, graph_launches = 0;
+    uint64_t graph_instantiations = 0, graph_updates = 0, max_launch_us = 0, pin_growths = 0;
     double busy_since_ms = -1;
 
     void run();
@@ -179,7 +189,7 @@ int Server::acquire_tables(Req& r, cudaStream_t st, std::string& err)
                 cudaEventCreateWithFlags(&cache[idx].ready, cudaEventDisableTiming);
             }
             CacheEntry& e = cache[idx];
-            cudaError_t ce = cudaMallocAsync(&e.dev, bytes, copy_st);
+            cudaError_t ce = cudaMallocFromPoolAsync(&e.dev, bytes, pool, copy_st);
             if (ce == cudaSuccess)
                 ce = cudaMemcpyAsync(e.dev, job.host_ws.data() + off, bytes, cudaMemcpyHostToDevice, copy_st);
             if (ce == cudaSuccess) ce = cudaEventRecord(e.ready, copy_st);
@@ -218,14 +228,17 @@ int Server::launch(Slot& s, Req& r, std::string& err)
     const int64_t B = job.batch;
     const int G = payoff_paths_per_thread(B, job.sms);
     const int64_t rows = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
-    cudaError_t e = s.ws.ensure(job.workspace_bytes, st);
-    if (e == cudaSuccess && !job.fused) e = s.ivb.ensure(sizeof(float) * 2 * r.plan.vgs.size() * (size_t)B, st);
-    if (e == cudaSuccess) e = s.part.ensure(sizeof(double) * 4 * no * (size_t)rows, st);
-    if (e == cudaSuccess) e = s.acc.ensure(sizeof(double) * 4 * no, st);
-    if (e == cudaSuccess) e = s.res.ensure(sizeof(double) * 5 * no, st);
-    if (e == cudaSuccess) e = s.outs.ensure(sizeof(OutDev) * no + sizeof(double) * no + 256, st);
+    cudaError_t e = s.ws.ensure(job.workspace_bytes, st, pool);
+    if (e == cudaSuccess && !job.fused)
+        e = s.ivb.ensure(sizeof(float) * 2 * r.plan.vgs.size() * (size_t)B, st, pool);
+    if (e == cudaSuccess) e = s.part.ensure(sizeof(double) * 4 * no * (size_t)rows, st, pool);
+    if (e == cudaSuccess) e = s.acc.ensure(sizeof(double) * 4 * no, st, pool);
+    if (e == cudaSuccess) e = s.res.ensure(sizeof(double) * 5 * no, st, pool);
+    if (e == cudaSuccess) e = s.outs.ensure(sizeof(OutDev) * no + sizeof(double) * no + 256, st, pool);
     const size_t pin_need = sizeof(double) * (1 + 5 * (size_t)no);
     if (e == cudaSuccess && s.pin_n < pin_need) {
+        // beyond kPinOutputs outputs only: cudaFreeHost waits for the device
+        ++pin_growths;
         if (s.pin) cudaFreeHost(s.pin);
         s.pin = nullptr;
         s.pin_n = 0;
@@ -291,14 +304,19 @@ int Server::launch(Slot& s, Req& r, std::string& err)
         e = cudaStreamEndCapture(st, &g);
         if (rc == RBG_OK && e == cudaSuccess) {
             // one executable graph per launch shape, updated in place for new parameters
+            // keyed by the graph's topology and node shapes (kernel variant, launches
+            // per batch, batches, outputs): requests of other M, N or parameters
+            // with the same key update the executable graph in place
             char key[128];
-            std::snprintf(key, sizeof key, "%d/%d/%lld/%lld/%d/%d", job.backend, (int)job.launches.size(),
-                          (long long)B, (long long)r.M, no, job.fused ? 1 : 0);
+            const MixedArgs& A0 = job.launches[0].args;
+            std::snprintf(key, sizeof key, "%d/%d/%d/%d/%lld/%d/%d", job.backend, A0.n0 > 0 ? 1 : 0, A0.logL,
+                          (int)job.launches.size(), (long long)((r.M + B - 1) / B), no, job.fused ? 1 : 0);
             auto it = s.graphs.find(key);
             bool ok = false;
             if (it != s.graphs.end()) {
                 cudaGraphExecUpdateResultInfo info;
                 ok = cudaGraphExecUpdate(it->second, g, &info) == cudaSuccess;
+                if (ok) ++graph_updates;
                 if (!ok) {
                     cudaGetLastError();
                     cudaGraphExecDestroy(it->second);
@@ -311,6 +329,7 @@ int Server::launch(Slot& s, Req& r, std::string& err)
                 if (e == cudaSuccess) {
                     s.graphs[key] = ex;
                     ok = true;
+                    ++graph_instantiations;
                 }
             }
             if (ok) {
@@ -411,6 +430,10 @@ void Server::run()
             r->t_start = Clock::now();
             std::string err;
             const int rc = launch(*free_slot, *r, err);
+            r->t_launched = Clock::now();
+            max_launch_us = std::max<uint64_t>(
+                max_launch_us,
+                (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(r->t_launched - r->t_start).count());
             if (rc != RBG_OK) {
                 r->status = rc;
                 r->err = err;
@@ -493,6 +516,25 @@ int rbg_server_create(const rbg_server_config* cfg_in, rbg_server** out)
     }
     if (cudaStreamCreateWithFlags(&s->copy_st, cudaStreamNonBlocking) != cudaSuccess)
         return srv_fail(RBG_ERR_CUDA, "stream creation failed");
+    cudaMemPoolProps pp;
+    std::memset(&pp, 0, sizeof pp);
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = dev;
+    uint64_t keep = ~(uint64_t)0;
+    if (cudaMemPoolCreate(&s->pool, &pp) != cudaSuccess ||
+        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+        cudaGetLastError();
+        return srv_fail(RBG_ERR_CUDA, "memory pool creation failed");
+    }
+    for (Slot& sl : s->slots) {
+        const size_t bytes = sizeof(double) * (1 + 5 * kPinOutputs);
+        if (cudaMallocHost((void**)&sl.pin, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return srv_fail(RBG_ERR_NOMEM, "pinned result buffers");
+        }
+        sl.pin_n = bytes;
+    }
     Server* raw = s.get();
     s->thr = std::thread([raw] { raw->run(); });
     *out = new rbg_server{std::move(s)};
@@ -599,6 +641,10 @@ int rbg_server_get_stats(rbg_server* srv, rbg_server_stats* st)
     st->table_cache_hits = s.cache_hits;
     st->table_cache_misses = s.cache_misses;
     st->graph_launches = s.graph_launches;
+    st->graph_instantiations = s.graph_instantiations;
+    st->graph_updates = s.graph_updates;
+    st->max_launch_us = s.max_launch_us;
+    st->pin_growths = s.pin_growths;
     return RBG_OK;
 }
 
@@ -629,6 +675,7 @@ int rbg_server_destroy(rbg_server* srv)
     }
     cudaStreamSynchronize(s.copy_st);
     cudaStreamDestroy(s.copy_st);
+    if (s.pool) cudaMemPoolDestroy(s.pool);
     delete srv;
     return RBG_OK;
 }
