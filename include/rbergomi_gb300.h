@@ -93,8 +93,9 @@ enum rbg_status {
 enum rbg_precision { RBG_FP64 = 0, RBG_MIXED = 1 };
 
 /* Volterra convolution backend.  In mixed mode AUTO picks the tcgen05
- * Toeplitz GEMM for N <= 1024 (one TMEM pass up to 512 steps, two above) and
- * the batched FFT convolution above.  The FP64 form has two: the direct
+ * Toeplitz GEMM for N <= 4096 (one TMEM pass up to 512 steps, one more per
+ * further 512; measured faster than the batched FFT convolution at every N
+ * up to 4096); FFT selects the batched FFT convolution (N <= 4096).  The FP64 form has two: the direct
  * causal sum (DIRECT) and an FP64 FFT convolution (FFT, 2 <= N <= 2048); AUTO
  * takes the FFT from 200 steps to 2048.  GEMM is mixed-mode only. */
 enum rbg_conv { RBG_CONV_AUTO = 0, RBG_CONV_GEMM = 1, RBG_CONV_FFT = 2, RBG_CONV_DIRECT = 3 };
@@ -213,7 +214,7 @@ int rbg_payoffs_rt(const rbg_params* p, const rbg_options* o, const double* Z, d
 
 /* Plain Monte Carlo on the Philox stream (streams W1, W1perp, Wperp): the
  * estimator of computeIV_tensor with status codes.  FP64, or the mixed form
- * (tcgen05 GEMM for N <= 1024, batched FFT above). */
+ * (tcgen05 GEMM for N <= 4096, or the batched FFT by option). */
 int rbg_price_mc(const rbg_params* p, const rbg_options* o, double* price, double* stat, double* iv);
 
 /* Plain Monte Carlo per-path payoffs for caller-supplied normals: Z holds

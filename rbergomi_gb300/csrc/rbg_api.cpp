@@ -392,8 +392,8 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
     MixedJob job;
     if ((rc = mixed_prepare(plan, o, M, job, g_err, 0, mc))) return rc;
     job.sob = sob;
-    if (sob && job.backend != RBG_CONV_GEMM)
-        return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend (N <= 1024)");
+    if (sob && (job.backend != RBG_CONV_GEMM || plan.N > 1024))
+        return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend and N <= 1024");
     const int64_t B = job.batch;
     if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
     const int G = payoff_paths_per_thread(B, job.sms);
@@ -941,8 +941,8 @@ int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t
     if (o->precision != RBG_FP64 && o->precision != RBG_MIXED) return fail(RBG_ERR_ARG, "unknown precision");
     if (o->precision == RBG_MIXED && bridge)
         return fail(RBG_ERR_UNSUPPORTED, "the Brownian bridge runs in the FP64 form only");
-    if (o->precision == RBG_MIXED && o->conv == RBG_CONV_FFT)
-        return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend (N <= 1024)");
+    if (o->precision == RBG_MIXED && (o->conv == RBG_CONV_FFT || p->N > 1024))
+        return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend and N <= 1024");
     g_h2d = g_d2h = 0;
     Plan plan;
     std::string err;

@@ -25,12 +25,17 @@
 // (Np + 16) x 16 (65 KB at N = 1024).  After chunk c's MMAs, columns
 // [32c, 32c+32) are final and the epilogue reads them.
 //
-// TMEM holds 128 lanes x 512 FP32 columns.  For 512 < Np <= 1024 a tile runs
-// two passes: pass 0 accumulates columns [0, P0), P0 = Np - 512, from chunks
-// 0 .. n0-1 (n0 = P0 / 32); pass 1 accumulates the last 512 columns from the
-// A tiles of chunks 0 .. n0-1 drawn again (W1 only, no epilogue work), then
-// from chunks n0 .. nc-1.  Per tile the producers' virtual chunk sequence is
-//   [0, n0) real | [0, n0) redrawn | [n0, nc) real      (n0 = 0: one pass).
+// TMEM holds 128 lanes x 512 FP32 columns.  For Np > 512 a tile runs np =
+// ceil(Np / 512) passes: pass 0 accumulates columns [0, 32 n0), n0 = (Np -
+// 512 (np - 1)) / 32, from chunks 0 .. n0-1; every later pass accumulates the
+// next 512 columns, first from the A tiles of all earlier chunks drawn again
+// (W1 only, no epilogue work), then from its own chunks.  For two passes the
+// producers' chunk sequence per tile is
+//   [0, n0) real | [0, n0) redrawn | [n0, nc) real.
+// Up to Np = 1024 the whole narrow strip stays in shared memory.  Above that
+// (up to 4096, eight passes) only its first 528 rows do -- all that a chunk
+// drawn for real reads -- and each redrawn chunk brings the 528-row window it
+// reads into its stage's FP32-tile region by a bulk copy (33 KB, from L2).
 //
 // Warp roles (544 threads, one CTA per SM, persistent over 128-path tiles):
 //   warps 0-7   producers, two threads per path, 16 steps each per chunk:
@@ -74,7 +79,8 @@ constexpr int kEpiWarp0 = kProdWarps;               // warps 8..15: TMEM lane qu
 constexpr int kMmaWarp = kProdWarps + kEpiWarps;    // warp 16
 constexpr int kThreads = (kMmaWarp + 1) * 32;       // 544
 constexpr int kPassCols = 512;                      // TMEM: 128 lanes x 512 FP32 columns per pass
-constexpr int kMaxNp = 2 * kPassCols;               // two passes
+constexpr int kMaxNp = 2 * kPassCols;               // two passes with the whole narrow strip resident
+constexpr int kMaxNpMulti = 8 * kPassCols;          // up to eight passes with streamed strip windows
 constexpr int kStripK = 16;                         // narrow strip width: one K = 16 MMA step
 constexpr int kHPerPath = kProdWarps * 32 / kTileM; // producer threads per path
 constexpr uint64_t kWaitNs = 2000000000ull;         // 2 s per wait
@@ -99,6 +105,14 @@ __host__ __device__ constexpr int stage_f_bytes(int ns) { return (ns == 3 ? kFWq
 // column) where one TMEM pass covers Np; 16 (SW32, 16 leading zero rows)
 // for two-pass tiles, whose Np-row strip would not fit shared memory at 32.
 __host__ __device__ inline int strip_k(int Np) { return Np <= kPassCols ? kChunk : kStripK; }
+// Pass mode of a tile: 0 one TMEM pass, 1 two passes over the resident
+// narrow strip, 2 up to eight passes where only the strip's first
+// kWindowRows rows stay resident and the chunks drawn again for a later pass
+// bring their strip window into shared memory by bulk copy.
+__host__ __device__ inline int pass_mode(int Np) { return Np <= kPassCols ? 0 : (Np <= kMaxNp ? 1 : 2); }
+// Narrow-strip rows one pass of one chunk reads: 512 columns + 16 (K halves).
+constexpr int kWindowRows = kPassCols + kStripK;
+constexpr int kWindowBytes = kWindowRows * kStripK * 2;  // one 16-bit half, 16896 B
 // FP32 tiles are path-major, [128 paths][32 steps], with the 16-byte chunk
 // index XORed by (path mod 8): a thread's 4 consecutive steps are one vector
 // access and the 8 threads of a vector phase hit distinct banks.
@@ -110,18 +124,30 @@ __host__ __device__ inline int strip_bytes(int Np)
 }
 
 struct SmemLayout {
-    int strip, a0, f0, stages, acc, beta, otab, osum, bars, total;
+    int strip, a0, f0, fstride, stages, acc, beta, otab, osum, bars, total;
 };
 
-// ns: normal streams per path, 2 (RT) or 3 (plain Monte Carlo: ns sums per group)
+// Resident strip bytes: the whole image (pass modes 0, 1) or the first
+// kWindowRows rows of each half (pass mode 2).
+__host__ __device__ inline int strip_smem_bytes(int Np)
+{
+    return pass_mode(Np) == 2 ? 2 * kWindowBytes : strip_bytes(Np);
+}
+
+// ns: normal streams per path, 2 (RT) or 3 (plain Monte Carlo: ns sums per group).
+// In pass mode 2 a stage's FP32-tile region also holds a redrawn chunk's strip
+// window (hi and lo halves), so it is at least 2 kWindowBytes (a multiple of
+// the 256-byte SW32 swizzle atom).
 __host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, int n_o, int ns = 2)
 {
     SmemLayout L;
     L.strip = 0;
-    L.a0 = (strip_bytes(Np) + 1023) / 1024 * 1024;
+    L.a0 = (strip_smem_bytes(Np) + 1023) / 1024 * 1024;
     L.stages = stages;
     L.f0 = L.a0 + stages * kStageA;
-    L.acc = L.f0 + stages * stage_f_bytes(ns);
+    L.fstride = stage_f_bytes(ns);
+    if (pass_mode(Np) == 2 && L.fstride < 2 * kWindowBytes) L.fstride = 2 * kWindowBytes;
+    L.acc = L.f0 + stages * L.fstride;
     L.beta = L.acc + 2 * n_g * ns * kTileM * 4 + (ns - 1) * kTileM * 4;  // per warpgroup, then W1_0 (Wperp_0)
     L.otab = L.beta + n_g * Np * 4;
     L.osum = (L.otab + n_o * 16 + 15) / 16 * 16;
@@ -153,6 +179,21 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Adds `bytes` to the phase's expected transaction count without arriving.
+__device__ __forceinline__ void mbar_expect_tx_only(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Bulk copy global -> shared memory of this CTA (16-byte aligned addresses,
+// a multiple of 16 bytes), completing `bytes` transactions on `bar`.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
 }
 
 // One wait attempt; the hardware may suspend the thread for up to 20 us
@@ -345,7 +386,7 @@ __device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rh
 // W1perp Philox streams stay interleaved in the common case.
 template <int BF16, bool REDRAW, bool MC>
 __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKeys& keys, uint64_t gpath, bool valid,
-                                              int64_t m, int p, int h, int c, int n0, unsigned char* st,
+                                              int64_t m, int p, int h, int c, bool bnd, unsigned char* st,
                                               float* w1s)
 {
     constexpr int SPT = kStepsPerThread;
@@ -399,16 +440,16 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
             *(float4*)(w1ps + at) = make_float4(wp[q], wp[q + 1], wp[q + 2], wp[q + 3]);
             if (MC) *(float4*)(w1s + kFWq + at) = make_float4(wq[q], wq[q + 1], wq[q + 2], wq[q + 3]);
         }
-        // last chunk of the first pass: its successor (chunk n0) follows the
-        // redrawn chunks, so W1 at step 32 n0 for the last column's sqrt(v) dW
-        // goes into this stage's boundary row
-        if (c == n0 - 1 && h == kHPerPath - 1) {
-            const uint4 xb = philox_group(keys, gpath, (uint32_t)(8 * n0), 0);
+        // last real chunk of a pass that is not the last: its successor (chunk
+        // c + 1) follows the next pass's redrawn chunks, so W1 at step 32 (c + 1)
+        // for the last column's sqrt(v) dW goes into this stage's boundary row
+        if (bnd && h == kHPerPath - 1) {
+            const uint4 xb = philox_group(keys, gpath, (uint32_t)(8 * (c + 1)), 0);
             float b0, b1;
             box_muller_f32(xb.x, xb.y, b0, b1);
             w1s[kFBnd + p] = valid ? b0 : 0.f;
             if (MC) {
-                const uint4 xq = philox_group(keys, gpath, (uint32_t)(8 * n0), 2);
+                const uint4 xq = philox_group(keys, gpath, (uint32_t)(8 * (c + 1)), 2);
                 box_muller_f32(xq.x, xq.y, b0, b1);
                 w1s[kFWqBnd + p] = valid ? b0 : 0.f;
             }
@@ -478,7 +519,7 @@ __device__ __forceinline__ void sobol_point(const MixedArgs& a, int p, int64_t m
 }
 
 template <int BF16, bool REDRAW>
-__device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t tile, int c, int n0, unsigned char* st,
+__device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t tile, int c, bool bnd, unsigned char* st,
                                                     float* w1s)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -531,9 +572,9 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
             }
         }
     }
-    // last chunk of the first pass: W1 at step 32 n0 for the boundary row
-    if (!REDRAW && c == n0 - 1 && lane < 16) {
-        const int p = 16 * w + lane, jb = kChunk * n0;
+    // last real chunk of a pass before the last: W1 at step 32 (c + 1) for the boundary row
+    if (!REDRAW && bnd && lane < 16) {
+        const int p = 16 * w + lane, jb = kChunk * (c + 1);
         const unsigned long long sb = s0 + lane;
         unsigned int q = 0;
         for (unsigned long long g = sb ^ (sb >> 1); g; g &= g - 1)
@@ -550,7 +591,7 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
 // doubles' own).  Writes the FP32 W1 / W1perp (/ Wperp) tiles and the 16-bit
 // hi/lo A tile (REDRAW: W1 and the A tile only).
 template <int BF16, bool REDRAW, bool MC>
-__device__ __forceinline__ void produce_chunk_ext(const MixedArgs& a, int64_t tile, int c, int n0, unsigned char* st,
+__device__ __forceinline__ void produce_chunk_ext(const MixedArgs& a, int64_t tile, int c, bool bnd, unsigned char* st,
                                                   float* w1s)
 {
     constexpr int NS = MC ? 3 : 2;
@@ -595,26 +636,46 @@ __device__ __forceinline__ void produce_chunk_ext(const MixedArgs& a, int64_t ti
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(z + (size_t)s * N));
         }
     }
-    // last chunk of the first pass: W1 (and Wperp) at step 32 n0 for the boundary rows
-    if (!REDRAW && c == n0 - 1 && lane < 16) {
+    // last real chunk of a pass before the last: W1 (and Wperp) at step 32 (c + 1)
+    // for the boundary rows
+    if (!REDRAW && bnd && lane < 16) {
         const int p = 16 * w + lane;
         const int64_t m = m0 + lane;
-        const double* z = a.ext + (size_t)m * NS * N + kChunk * n0;
+        const double* z = a.ext + (size_t)m * NS * N + kChunk * (c + 1);
         w1s[kFBnd + p] = m < a.B ? (float)__ldg(z) : 0.f;
         if (MC) w1s[kFWqBnd + p] = m < a.B ? (float)__ldg(z + 2 * N) : 0.f;
     }
 }
 
-// TWO: two TMEM passes per tile (512 < Np <= 1024).  The one-pass
-// instantiation has n0 = 0 at compile time, so the virtual-chunk bookkeeping
-// folds away there.
+// Pass schedule of a tile.  TMEM holds 512 accumulator columns, so a tile of
+// Np > 512 columns runs np passes: pass 0 covers chunks [0, n0) (columns
+// [0, 32 n0), n0 = (Np - 512 (np - 1)) / 32), pass p >= 1 the 16 chunks from
+// pass_begin(p) = n0 + 16 (p - 1).  Pass p takes chunks 0 .. pass_end(p) - 1 in
+// order: those below pass_begin(p) are drawn again (W1 only) and add their
+// whole contribution to the pass's columns; the rest are drawn for real and
+// their columns become final one chunk at a time, as in one pass.  Every role
+// walks this same (pass, chunk) sequence, one pipeline stage per chunk.
+template <int PM>
+struct PassPlan {
+    int np, n0, nc;
+    __device__ __forceinline__ PassPlan(const MixedArgs& a)
+        : np(PM == 0 ? 1 : (PM == 1 ? 2 : a.np)), n0(PM == 0 ? 0 : a.n0), nc(a.nc) {}
+    __device__ __forceinline__ int begin(int p) const { return p == 0 ? 0 : n0 + kPassCols / kChunk * (p - 1); }
+    __device__ __forceinline__ int end(int p) const { return p + 1 >= np ? nc : n0 + kPassCols / kChunk * p; }
+};
+
+// PM: pass mode (pass_mode(Np)): 0 one TMEM pass; 1 two passes, the narrow
+// strip resident; 2 up to eight passes, the strip's first kWindowRows rows
+// resident and each redrawn chunk's window brought into its stage's FP32-tile
+// region by a bulk copy that the stage's `full` barrier waits for.
 // SRC: where the normals come from: 0 Philox, 1 Sobol' (produce_chunk_sobol,
 // RT only), 2 the caller's FP64 normals (a.ext, quadrature layout).
-template <int BF16, bool TWO, bool MC, int SRC = 0>
+template <int BF16, int PM, bool MC, int SRC = 0>
 __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
     constexpr int NS = MC ? 3 : 2;  // normal streams per path = sums per variance group
     constexpr int kStageFB = stage_f_bytes(NS);
+    static_assert(PM >= 0 && PM <= 2, "pass mode");
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -636,10 +697,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     uint32_t* tmem_holder = (uint32_t*)(bars + 12);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int Np = a.Np, nc = a.nc, n0 = TWO ? a.n0 : 0;
-    const int nv = nc + n0;  // virtual chunks per tile
+    const int Np = a.Np, nc = a.nc;
+    const PassPlan<PM> pp(a);
+    const int FB = (PM == 2) ? L.fstride : kStageFB;  // bytes per stage of the FP32-tile region
     const int64_t ntiles = (a.B + kTileM - 1) / kTileM;
-    const uint32_t sbytes = (uint32_t)strip_bytes(Np);
+    const uint32_t sbytes = (uint32_t)strip_smem_bytes(Np);
+    const uint32_t half_g = (uint32_t)(strip_bytes(Np) / 2);  // hi -> lo in the global image
 
     if (threadIdx.x == kMmaWarp * 32) {
         for (int s = 0; s < S; ++s) {
@@ -652,11 +715,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         mbar_init(smem_u32(final_bar), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         mbar_expect_tx(smem_u32(strip_bar), sbytes);
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_u32(strip)),
-            "l"(a.strip), "r"(sbytes), "r"(smem_u32(strip_bar))
-            : "memory");
+        if (PM == 2) {
+            // the first kWindowRows rows of each half
+            bulk_g2s(smem_u32(strip), a.strip, kWindowBytes, smem_u32(strip_bar));
+            bulk_g2s(smem_u32(strip) + kWindowBytes, a.strip + half_g, kWindowBytes, smem_u32(strip_bar));
+        } else {
+            bulk_g2s(smem_u32(strip), a.strip, sbytes, smem_u32(strip_bar));
+        }
     }
     if (warp == kMmaWarp) {
         __syncwarp();
@@ -686,31 +751,46 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
             const int64_t m = tile * kTileM + p;
             const bool valid = m < a.B;
             const uint64_t gpath = (uint64_t)(a.path0 + m);
-            for (int v = 0; v < nv; ++v, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
-                // redrawn chunks of the second pass feed only the MMA (W1 A tile)
-                const bool redraw = v >= n0 && v < 2 * n0;
-                const int c = (v < n0) ? v : v - n0;
-                if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
-                unsigned char* st = base + L.a0 + s * kStageA;
-                float* w1s = (float*)(base + L.f0 + s * kStageFB);
-                if (SRC == 1) {
-                    if (TWO && redraw)
-                        produce_chunk_sobol<BF16, true>(a, tile, c, n0, st, w1s);
-                    else
-                        produce_chunk_sobol<BF16, false>(a, tile, c, n0, st, w1s);
-                } else if (SRC == 2) {
-                    if (TWO && redraw)
-                        produce_chunk_ext<BF16, true, MC>(a, tile, c, n0, st, w1s);
-                    else
-                        produce_chunk_ext<BF16, false, MC>(a, tile, c, n0, st, w1s);
-                } else if (TWO && redraw) {
-                    produce_chunk<BF16, true, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
-                } else {
-                    produce_chunk<BF16, false, MC>(a, keys, gpath, valid, m, p, h, c, n0, st, w1s);
+            for (int q = 0; q < pp.np; ++q) {
+                const int cb = pp.begin(q), ce = pp.end(q);
+                for (int c = 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+                    // redrawn chunks of a later pass feed only the MMA (W1 A tile)
+                    const bool redraw = c < cb;
+                    // last real chunk of a pass before the last: boundary row for its successor
+                    const bool bnd = !redraw && c == ce - 1 && q + 1 < pp.np;
+                    if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
+                    unsigned char* st = base + L.a0 + s * kStageA;
+                    float* w1s = (float*)(base + L.f0 + s * FB);
+                    if (PM == 2 && redraw && threadIdx.x == 0) {
+                        // this chunk's strip window, rows [32 (cb - c), + kWindowRows) of each half,
+                        // into the stage's FP32-tile region (unused by redrawn chunks); the MMA
+                        // issuer's wait on `full` covers the bytes
+                        const uint32_t dst = smem_u32(w1s), bar = smem_u32(full + s);
+                        const unsigned char* src = a.strip + (size_t)(kChunk * (cb - c)) * (kStripK * 2);
+                        fence_proxy_async();
+                        mbar_expect_tx_only(bar, 2 * kWindowBytes);
+                        bulk_g2s(dst, src, kWindowBytes, bar);
+                        bulk_g2s(dst + kWindowBytes, src + half_g, kWindowBytes, bar);
+                    }
+                    if (SRC == 1) {
+                        if (PM > 0 && redraw)
+                            produce_chunk_sobol<BF16, true>(a, tile, c, bnd, st, w1s);
+                        else
+                            produce_chunk_sobol<BF16, false>(a, tile, c, bnd, st, w1s);
+                    } else if (SRC == 2) {
+                        if (PM > 0 && redraw)
+                            produce_chunk_ext<BF16, true, MC>(a, tile, c, bnd, st, w1s);
+                        else
+                            produce_chunk_ext<BF16, false, MC>(a, tile, c, bnd, st, w1s);
+                    } else if (PM > 0 && redraw) {
+                        produce_chunk<BF16, true, MC>(a, keys, gpath, valid, m, p, h, c, bnd, st, w1s);
+                    } else {
+                        produce_chunk<BF16, false, MC>(a, keys, gpath, valid, m, p, h, c, bnd, st, w1s);
+                    }
+                    fence_proxy_async();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(smem_u32(full + s));
                 }
-                fence_proxy_async();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(full + s));
             }
         }
     } else if (warp < kMmaWarp) {
@@ -732,11 +812,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
             for (int g = 0; g < a.n_g; ++g)
 #pragma unroll
                 for (int t = 0; t < NS; ++t) my_acc[(NS * g + t) * kTileM + p] = 0.f;
-            for (int v = 0; v < nv; ++v, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+            for (int q = 0; q < pp.np; ++q) {
+              const int cb = pp.begin(q), ce = pp.end(q);
+              for (int c = 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
                 // the producers' FP32 tiles of this stage (the upper half also pairs
                 // its last column with the next chunk's first W1), then the MMA results
                 if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7, a.prof)) goto done;
-                if (v >= n0 && v < 2 * n0) {
+                if (c < cb) {
                     // redrawn chunk: no column becomes final.  Its MMA completion is still
                     // awaited, so that every accf phase is observed in order.
                     if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
@@ -744,18 +826,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     if (lane == 0) mbar_arrive(smem_u32(empty + s));
                     continue;
                 }
-                const int c = (v < n0) ? v : v - n0;
-                const uint32_t tcol0 = (c >= n0) ? (uint32_t)(kChunk * n0) : 0u;  // TMEM column of output 0
-                const bool pass_end = (c == nc - 1) || (c == n0 - 1);
+                const uint32_t tcol0 = (uint32_t)(kChunk * cb);  // TMEM column of output 0 of this pass
+                const bool pass_end = c == ce - 1;
                 const bool has_next = c + 1 < nc;
-                const bool bnd = (c == n0 - 1);  // successor W1 in this stage's boundary row
+                const bool bnd = pass_end && q + 1 < pp.np;  // successor W1 in this stage's boundary row
                 const int sn = (s + 1 == S) ? 0 : s + 1;
                 if ((kEpiWGs == 1 || wg == 1) && has_next && !bnd &&
                     !mbar_wait_warp(smem_u32(full + sn), sn == 0 ? ph ^ 1u : ph, a.err, 8, a.prof))
                     goto done;
                 if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
                 tc_fence_after();
-                const float* w1s = (const float*)(base + L.f0 + s * kStageFB);
+                const float* w1s = (const float*)(base + L.f0 + s * FB);
                 const float* w1ps = w1s + kFW1p;
                 const float* wqs = w1s + kFWq;  // plain Monte Carlo only
 #pragma unroll 1
@@ -771,7 +852,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                         w1v[jj] = u.x; w1v[jj + 1] = u.y; w1v[jj + 2] = u.z; w1v[jj + 3] = u.w;
                         w1pv[jj] = v.x; w1pv[jj + 1] = v.y; w1pv[jj + 2] = v.z; w1pv[jj + 3] = v.w;
                     }
-                    const float* nexts = (const float*)(base + L.f0 + sn * kStageFB);
+                    const float* nexts = (const float*)(base + L.f0 + sn * FB);
                     const float w_after = (hh == 0) ? w1s[ftile_at(p, 16)]
                                                     : (!has_next ? 0.f
                                                        : bnd     ? w1s[kFBnd + p]
@@ -857,6 +938,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 }
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(empty + s));
+              }
             }
             // both warpgroups' column sums of this tile are in shared memory
             asm volatile("bar.sync 1, %0;" ::"r"(kEpiWarps * 32) : "memory");
@@ -918,62 +1000,68 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     } else if (lane == 0) {
         // ------------------------------------------------------ MMA issuer
         const uint32_t strip_hi = smem_u32(strip);
-        const uint32_t strip_lo = strip_hi + (uint32_t)(strip_bytes(Np) / 2);
-        constexpr bool wide = !TWO;  // strip_k(Np) == kChunk exactly when one pass covers Np
-        const int P0 = kChunk * n0;  // first column of the last pass
+        const uint32_t strip_lo = strip_hi + (uint32_t)(strip_smem_bytes(Np) / 2);
+        constexpr bool wide = PM == 0;  // strip_k(Np) == kChunk exactly when one pass covers Np
         if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
             int64_t pass = 0;
             int s = 0;
             uint32_t ph = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-                for (int v = 0; v < nv; ++v, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
-                    // output columns [lo, hi) of this chunk; TMEM column = output column - toff
-                    int c, lo, hi, toff;
-                    if (v < n0) { c = v; lo = kChunk * c; hi = P0; toff = 0; }
-                    else if (v < 2 * n0) { c = v - n0; lo = P0; hi = Np; toff = P0; }
-                    else { c = v - n0; lo = kChunk * c; hi = Np; toff = P0; }
-                    const bool first = (v == 0) || (v == n0);  // first chunk of a pass overwrites
-                    if (first) {
-                        // the epilogue has read every column of the previous pass
-                        if (pass > 0 &&
-                            !mbar_wait(smem_u32(tmem_empty), (uint32_t)((pass - 1) & 1), a.err, 4, a.prof)) {
-                            ok = false;
-                            break;
-                        }
-                        ++pass;
-                        tc_fence_after();
-                    }
-                    if (!mbar_wait(smem_u32(full + s), ph, a.err, 5, a.prof)) { ok = false; break; }
-                    tc_fence_after();
-                    const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
-                    const uint32_t alo = ahi + kTileBytes;
-                    for (int col0 = lo; col0 < hi; col0 += 256) {
-                        const int n = (hi - col0 < 256) ? (hi - col0) : 256;
-                        const uint32_t id = idesc_f16(n, BF16);
-                        const uint32_t jrow = (uint32_t)(col0 - kChunk * c);
-                        const uint32_t d = tmem + (uint32_t)(col0 - toff);
-#pragma unroll
-                        for (int ks = 0; ks < 2; ++ks) {
-                            // K half ks: A columns [16 ks, 16 ks + 16); wide strip: row jrow, bytes
-                            // [32 ks, 32 ks + 32); narrow strip: rows from jrow + 16 - 16 ks
-                            const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
-                            uint64_t dbh, dbl;
-                            if (wide) {
-                                dbh = sdesc_sw64(strip_hi + jrow * 64 + 32 * ks);
-                                dbl = sdesc_sw64(strip_lo + jrow * 64 + 32 * ks);
-                            } else {
-                                const uint32_t boff = (jrow + (uint32_t)(kStripK * (1 - ks))) * (kStripK * 2);
-                                dbh = sdesc_sw32(strip_hi + boff);
-                                dbl = sdesc_sw32(strip_lo + boff);
+                for (int q = 0; q < pp.np && ok; ++q) {
+                    const int cb = pp.begin(q), ce = pp.end(q);
+                    for (int c = 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+                        // output columns [lo, hi) of this chunk; TMEM column = output column - toff
+                        const bool redraw = c < cb;
+                        const int lo = redraw ? kChunk * cb : kChunk * c, hi = kChunk * ce, toff = kChunk * cb;
+                        const bool first = c == 0;  // first chunk of a pass overwrites
+                        if (first) {
+                            // the epilogue has read every column of the previous pass
+                            if (pass > 0 &&
+                                !mbar_wait(smem_u32(tmem_empty), (uint32_t)((pass - 1) & 1), a.err, 4, a.prof)) {
+                                ok = false;
+                                break;
                             }
-                            umma_f16(d, dah, dbh, id, (first && ks == 0) ? 0u : 1u);
-                            umma_f16(d, dah, dbl, id, 1u);
-                            umma_f16(d, dal, dbh, id, 1u);
+                            ++pass;
+                            tc_fence_after();
                         }
+                        if (!mbar_wait(smem_u32(full + s), ph, a.err, 5, a.prof)) { ok = false; break; }
+                        tc_fence_after();
+                        const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
+                        const uint32_t alo = ahi + kTileBytes;
+                        // B operand: the resident strip, or (pass mode 2, redrawn chunk) the window
+                        // in this stage whose row 0 is strip row lo - 32 c
+                        const bool win = PM == 2 && redraw;
+                        const uint32_t bhi = win ? smem_u32(base + L.f0 + s * FB) : strip_hi;
+                        const uint32_t blo = win ? bhi + (uint32_t)kWindowBytes : strip_lo;
+                        const int rbase = win ? lo : kChunk * c;
+                        for (int col0 = lo; col0 < hi; col0 += 256) {
+                            const int n = (hi - col0 < 256) ? (hi - col0) : 256;
+                            const uint32_t id = idesc_f16(n, BF16);
+                            const uint32_t jrow = (uint32_t)(col0 - rbase);
+                            const uint32_t d = tmem + (uint32_t)(col0 - toff);
+#pragma unroll
+                            for (int ks = 0; ks < 2; ++ks) {
+                                // K half ks: A columns [16 ks, 16 ks + 16); wide strip: row jrow, bytes
+                                // [32 ks, 32 ks + 32); narrow strip: rows from jrow + 16 - 16 ks
+                                const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
+                                uint64_t dbh, dbl;
+                                if (wide) {
+                                    dbh = sdesc_sw64(bhi + jrow * 64 + 32 * ks);
+                                    dbl = sdesc_sw64(blo + jrow * 64 + 32 * ks);
+                                } else {
+                                    const uint32_t boff = (jrow + (uint32_t)(kStripK * (1 - ks))) * (kStripK * 2);
+                                    dbh = sdesc_sw32(bhi + boff);
+                                    dbl = sdesc_sw32(blo + boff);
+                                }
+                                umma_f16(d, dah, dbh, id, (first && ks == 0) ? 0u : 1u);
+                                umma_f16(d, dah, dbl, id, 1u);
+                                umma_f16(d, dal, dbh, id, 1u);
+                            }
+                        }
+                        umma_commit(smem_u32(empty + s));
+                        umma_commit(smem_u32(accf + s));
                     }
-                    umma_commit(smem_u32(empty + s));
-                    umma_commit(smem_u32(accf + s));
                 }
             }
         }
@@ -1259,9 +1347,9 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     const int N = plan.N;
     const int Np = (N + kChunk - 1) / kChunk * kChunk;
     int backend = o.conv;
-    if (backend == RBG_CONV_AUTO) backend = (Np <= kMaxNp) ? RBG_CONV_GEMM : RBG_CONV_FFT;
-    if (backend == RBG_CONV_GEMM && Np > kMaxNp) {
-        err = "mixed GEMM form supports N <= 1024 (two passes over 128 x 512 FP32 TMEM columns); use the FFT backend";
+    if (backend == RBG_CONV_AUTO) backend = (Np <= kMaxNpMulti) ? RBG_CONV_GEMM : RBG_CONV_FFT;
+    if (backend == RBG_CONV_GEMM && Np > kMaxNpMulti) {
+        err = "mixed GEMM form supports N <= 4096 (eight passes over 128 x 512 FP32 TMEM columns)";
         return RBG_ERR_UNSUPPORTED;
     }
     if (backend == RBG_CONV_FFT && N > 4096) {
@@ -1304,7 +1392,8 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             A.N = N;
             A.Np = Np;
             A.nc = Np / kChunk;
-            A.n0 = (backend == RBG_CONV_GEMM && Np > kPassCols) ? (Np - kPassCols) / kChunk : 0;
+            A.np = (backend == RBG_CONV_GEMM) ? (Np + kPassCols - 1) / kPassCols : 1;
+            A.n0 = (backend == RBG_CONV_GEMM && Np > kPassCols) ? (Np - kPassCols * (A.np - 1)) / kChunk : 0;
             A.n_g = ng;
             A.g0 = g0;
             A.tmem_cols = tcols;
@@ -1436,6 +1525,18 @@ int mixed_part_rows(const MixedJob& job, int64_t B)
     return (int)std::min<int64_t>(ntiles, job.sms);
 }
 
+// The path kernel of a (split, estimator, normal source) for pass mode pm.
+// Sobol' normals run up to two passes (N <= 1024; mixed_launch rejects more).
+template <int BF16, bool MC, int SRC>
+static void (*gemm_kernel(int pm))(MixedArgs)
+{
+    if constexpr (SRC == 1)
+        return pm == 0 ? k_mixed_gemm<BF16, 0, MC, SRC> : k_mixed_gemm<BF16, 1, MC, SRC>;
+    else
+        return pm == 0 ? k_mixed_gemm<BF16, 0, MC, SRC>
+                       : (pm == 1 ? k_mixed_gemm<BF16, 1, MC, SRC> : k_mixed_gemm<BF16, 2, MC, SRC>);
+}
+
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
                  cudaStream_t st, std::string& err, float* dbg_w, float* dbg_x, double* part,
                  unsigned long long* prof, float* ivq, const double* ext)
@@ -1448,8 +1549,8 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         err = "plain Monte Carlo launch without an IsvdWp buffer";
         return RBG_ERR_ARG;
     }
-    if (job.sob && (job.mc || job.backend != RBG_CONV_GEMM)) {
-        err = "Sobol' normals in the mixed form need the RT estimator and the GEMM backend";
+    if (job.sob && (job.mc || job.backend != RBG_CONV_GEMM || job.N > kMaxNp)) {
+        err = "Sobol' normals in the mixed form need the RT estimator and the GEMM backend with N <= 1024";
         return RBG_ERR_UNSUPPORTED;
     }
     unsigned char* base = (unsigned char*)ws;
@@ -1483,24 +1584,20 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         if (job.backend == RBG_CONV_FFT) {
             e = launch_mixed_fft(A, job.sms, st);
         } else {
+            const int pm = pass_mode(A.Np);
             void (*kern)(MixedArgs);
-            const bool two = A.n0 > 0;
             if (job.sob && job.split == RBG_SPLIT_BF16X3)
-                kern = two ? k_mixed_gemm<1, true, false, 1> : k_mixed_gemm<1, false, false, 1>;
+                kern = gemm_kernel<1, false, 1>(pm);
             else if (job.sob)
-                kern = two ? k_mixed_gemm<0, true, false, 1> : k_mixed_gemm<0, false, false, 1>;
+                kern = gemm_kernel<0, false, 1>(pm);
             else if (ext && job.split == RBG_SPLIT_BF16X3)
-                kern = job.mc ? (two ? k_mixed_gemm<1, true, true, 2> : k_mixed_gemm<1, false, true, 2>)
-                              : (two ? k_mixed_gemm<1, true, false, 2> : k_mixed_gemm<1, false, false, 2>);
+                kern = job.mc ? gemm_kernel<1, true, 2>(pm) : gemm_kernel<1, false, 2>(pm);
             else if (ext)
-                kern = job.mc ? (two ? k_mixed_gemm<0, true, true, 2> : k_mixed_gemm<0, false, true, 2>)
-                              : (two ? k_mixed_gemm<0, true, false, 2> : k_mixed_gemm<0, false, false, 2>);
+                kern = job.mc ? gemm_kernel<0, true, 2>(pm) : gemm_kernel<0, false, 2>(pm);
             else if (job.split == RBG_SPLIT_BF16X3)
-                kern = job.mc ? (two ? k_mixed_gemm<1, true, true> : k_mixed_gemm<1, false, true>)
-                              : (two ? k_mixed_gemm<1, true, false> : k_mixed_gemm<1, false, false>);
+                kern = job.mc ? gemm_kernel<1, true, 0>(pm) : gemm_kernel<1, false, 0>(pm);
             else
-                kern = job.mc ? (two ? k_mixed_gemm<0, true, true> : k_mixed_gemm<0, false, true>)
-                              : (two ? k_mixed_gemm<0, true, false> : k_mixed_gemm<0, false, false>);
+                kern = job.mc ? gemm_kernel<0, true, 0>(pm) : gemm_kernel<0, false, 0>(pm);
             e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e == cudaSuccess) kern<<<grid, kThreads, smem, st>>>(A);
         }

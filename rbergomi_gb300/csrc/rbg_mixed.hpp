@@ -18,7 +18,7 @@ constexpr int kMixedMaxFused = 64;   // outputs whose payoffs one launch can pri
 
 // Kernel arguments (passed by value as a __grid_constant__).
 struct MixedArgs {
-    const unsigned char* strip;  // [hi | lo], each Np*64 bytes, SW64 K-major image
+    const unsigned char* strip;  // [hi | lo]: Np rows x 64 B (SW64, one pass) or Np + 16 rows x 32 B (SW32)
     const float* beta;           // [n_g][Np] (log2 compensator - log2 xi) / 2
     float2* ivb;                 // [n_vg_total][B] (Ivdt, IsvdW)
     float* ivq;                  // plain Monte Carlo: [n_vg_total][B] IsvdWp = sum sqrt(v) sdt Wperp
@@ -37,6 +37,7 @@ struct MixedArgs {
     int64_t path0, B;
     int N, Np, nc, n_g, g0, tmem_cols, stages;
     int n0;                // GEMM backend, Np > 512: chunks of the first TMEM pass (0: one pass)
+    int np;                // GEMM backend: TMEM passes per tile (1 .. 8)
     int n_o, n_out_total;  // fused outputs of this launch; all outputs of the job
     int L, logL;  // FFT backend transform length
     float a1, a2, xi, sqrt_xi;

@@ -20,7 +20,7 @@
 //   * optionally captures each request's device work (everything after the
 //     table upload) as a CUDA graph and launches the graph;
 //   * records per-request latency (submit -> results on the host).
-// Every request runs the mixed form (tcgen05 GEMM for N <= 1024, FFT above).
+// Every request runs the mixed form (the tcgen05 Toeplitz GEMM, N <= 4096).
 #include <cuda_runtime.h>
 
 #include <algorithm>

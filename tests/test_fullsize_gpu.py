@@ -65,8 +65,8 @@ def test_workload2_headline_mixed_vs_fp64(R):
 
 @pytest.mark.parametrize("N", [1024, 2048])
 def test_workload3_long_horizon_mixed_vs_fp64(R, N):
-    """N=1024 (two-pass tensor-core GEMM) and N=2048 (batched FFT), 2^20 paths,
-    three H, 11 strikes on [0.5, 1.5], seed 3."""
+    """N=1024 (two-pass tensor-core GEMM) and N=2048 (four passes, strip
+    windows streamed), 2^20 paths, three H, 11 strikes on [0.5, 1.5], seed 3."""
     K = list(np.round(np.linspace(0.5, 1.5, 11), 10))
     assert_mixed_matches(R, (0.04, [0.03, 0.1, 0.4], [1.5] * 3, [-0.7] * 3, [2.0] * 11, K, N, 1 << 20), 3)
 

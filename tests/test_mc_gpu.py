@@ -100,13 +100,14 @@ def test_mc_mixed_vs_fp64_identical_normals(R, N):
     assert np.all(np.abs(ms / fs - 1) < 1e-3)
 
 
-@pytest.mark.parametrize("N,conv", [(1500, "auto"), (700, "fft")])
-def test_mc_mixed_fft_backend_vs_fp64(R, N, conv):
-    """Mixed plain MC on the batched-FFT backend (automatic above N = 1024)."""
+@pytest.mark.parametrize("N,conv", [(1500, "fft"), (700, "fft"), (1500, "auto"), (2048, "gemm")])
+def test_mc_mixed_long_horizon_vs_fp64(R, N, conv):
+    """Mixed plain MC on the batched-FFT backend and on the multi-pass GEMM
+    (three and four TMEM passes with streamed strip windows)."""
     xi, H, eta, rho = 0.05, [0.1], [1.5], [-0.7]
     T, K = [2.0, 2.0], [0.9, 1.2]
     M = 1 << 13
-    cv = R.CONV_FFT if conv == "fft" else R.CONV_AUTO
+    cv = {"fft": R.CONV_FFT, "auto": R.CONV_AUTO, "gemm": R.CONV_GEMM}[conv]
     mp, ms, _ = R.price_mc(xi, H, eta, rho, T, K, N, M, seed=4, precision=R.MIXED, conv=cv)
     fp, fs, _ = R.price_mc(xi, H, eta, rho, T, K, N, M, seed=4, normals=R.NORMALS_F32)
     err = np.abs(mp - fp)

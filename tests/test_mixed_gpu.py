@@ -30,22 +30,27 @@ GRID = dict(xi=0.04, H=[0.05, 0.1, 0.1, 0.3, 0.1], eta=[1.0, 1.5, 1.5, 2.5, 1.5]
 
 def fp64_x(W1, W1p, H, N):
     """X_j = sum_{k<j} W1_k Gamma_{j-k} + a1 W1_j + a2 W1perp_j in FP64 and
-    the magnitude sum_{k<j} |W1_k Gamma_{j-k}| (rBergLib/rBergomiMT.cpp:83-109)."""
+    the magnitude sum_{k<j} |W1_k Gamma_{j-k}| (rBergLib/rBergomiMT.cpp:83-109),
+    both as FP64 FFT convolutions (roundoff ~1e-15 of the magnitude)."""
     from oracle import oracle as O
-    G = O.gamma(H, N)
+    G = O.gamma(H, N).copy()
+    G[0] = 0.0
     s2H = np.sqrt(2 * H)
     rhoH = s2H / (H + 0.5)
     a1, a2 = rhoH / s2H, np.sqrt(1 - rhoH ** 2) / s2H
-    M = W1.shape[0]
-    Y = np.zeros((M, N))
-    A = np.zeros((M, N))
-    for k in range(N):
-        Y[:, k + 1:] += W1[:, k:k + 1] * G[None, 1:N - k]
-        A[:, k + 1:] += np.abs(W1[:, k:k + 1] * G[None, 1:N - k])
-    return Y + a1 * W1[:, :N] + a2 * W1p[:, :N], A
+    L = 1 << int(np.ceil(np.log2(2 * N)))
+    W = W1[:, :N]
+
+    def conv(a, g):
+        return np.fft.irfft(np.fft.rfft(a, L) * np.fft.rfft(g, L)[None, :], L)[:, :N]
+
+    Y = conv(W, G)
+    A = conv(np.abs(W), np.abs(G))
+    return Y + a1 * W + a2 * W1p[:, :N], A
 
 
-@pytest.mark.parametrize("N,M", [(100, 300), (512, 256), (33, 129), (700, 200), (1024, 130)])
+@pytest.mark.parametrize("N,M", [(100, 300), (512, 256), (33, 129), (700, 200), (1024, 130), (1500, 100),
+                                 (4096, 40)])
 def test_fused_normals_are_the_exported_stream(R, N, M):
     w, _, _ = R.debug_mixed_paths(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], N, M, seed=11, path_offset=7)
     Z = R.generate_normals(11, M, N, precision=R.MIXED, path_offset=7)
@@ -54,10 +59,12 @@ def test_fused_normals_are_the_exported_stream(R, N, M):
 
 
 @pytest.mark.parametrize("split,tol", [(0, 4e-5), (1, 1e-6)])
-@pytest.mark.parametrize("N", [64, 100, 512, 513, 700, 1024])
+@pytest.mark.parametrize("N", [64, 100, 512, 513, 700, 1024, 1025, 1500, 2048, 3001, 4096])
 def test_toeplitz_gemm_columns(R, split, tol, N):
-    """Columns of one TMEM pass (N <= 512) and of two (512 < N <= 1024, the
-    second pass fed by redrawn A tiles) against the FP64 convolution."""
+    """Columns of one TMEM pass (N <= 512), of two (512 < N <= 1024, the
+    second pass fed by redrawn A tiles over the resident strip) and of up to
+    eight (N > 1024: redrawn chunks read their strip window, copied into the
+    stage, every later pass) against the FP64 convolution."""
     H = 0.1
     M = 256
     w, x, _ = R.debug_mixed_paths(0.04, [H], [1.5], [-0.7], [1.0], [1.0], N, M, seed=3, split=split)
@@ -116,15 +123,16 @@ def test_mixed_grid_multi_pass(R):
     assert np.all(np.abs(mp - fp) < 0.2 * np.maximum(fs, 1e-12) + 1e-9)
 
 
-def test_gemm_backend_rejects_long_horizon(R):
+def test_gemm_backend_rejects_longer_horizon(R):
     with pytest.raises(R.RbgError):
-        R.price_rt(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 1025, 256, precision=R.MIXED, conv=R.CONV_GEMM)
+        R.price_rt(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 4097, 256, precision=R.MIXED, conv=R.CONV_GEMM)
 
 
-@pytest.mark.parametrize("N", [544, 1024])
-def test_two_pass_gemm_prices_vs_fp64_identical_normals(R, N):
-    """Long-horizon shape on the two-pass GEMM: error vs the FP64 form on the
-    same FP32 normals <= 1e-4 relative and < 0.2 standard errors."""
+@pytest.mark.parametrize("N", [544, 1024, 1056, 1500, 2048, 4096])
+def test_multi_pass_gemm_prices_vs_fp64_identical_normals(R, N):
+    """Long-horizon shape on the multi-pass GEMM (two passes up to N = 1024,
+    up to eight with streamed strip windows above): error vs the FP64 form on
+    the same FP32 normals <= 1e-4 relative and < 0.2 standard errors."""
     H, eta, rho, xi, T = [0.1], [1.5], [-0.7], 0.04, 2.0
     K = list(np.linspace(0.5, 1.5, 11))
     M = 1 << 13
@@ -135,10 +143,12 @@ def test_two_pass_gemm_prices_vs_fp64_identical_normals(R, N):
     assert np.all(err < 0.2 * fs)
 
 
-def test_two_pass_gemm_multi_group_grid(R):
-    """Several variance groups and Volterra passes at N = 800 (two TMEM passes)."""
+@pytest.mark.parametrize("N", [800, 2500])
+def test_multi_pass_gemm_multi_group_grid(R, N):
+    """Several variance groups and Volterra passes at N = 800 (two TMEM
+    passes) and N = 2500 (five, strip windows streamed)."""
     g = GRID
-    N, M = 800, 1 << 12
+    M = 1 << 12
     mp, ms, _ = R.price_rt(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, seed=23,
                            precision=R.MIXED, split=1, conv=R.CONV_GEMM)
     fp, fs, _ = R.price_rt(g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, seed=23,

@@ -46,10 +46,12 @@ def test_mixed_quadrature_vs_reference_fixture(R, name):
     check(pay, c["payoff"])
 
 
-@pytest.mark.parametrize("N,M,conv", [(512, 20000, 0), (700, 5000, 0), (1500, 3000, 0), (100, 4099, 2)])
+@pytest.mark.parametrize("N,M,conv", [(512, 20000, 0), (700, 5000, 0), (1500, 3000, 0), (1500, 3000, 2),
+                                      (100, 4099, 2)])
 def test_mixed_quadrature_vs_fp64(R, N, M, conv):
-    """One TMEM pass (N=512), two passes (N=700), the FFT backend (N=1500 by
-    the crossover, N=100 forced); ragged path counts."""
+    """One TMEM pass (N=512), two passes (N=700), three passes with streamed
+    strip windows (N=1500), the FFT backend (N=1500 and N=100 forced); ragged
+    path counts."""
     xi, H, eta, rho = 0.04, [0.05, 0.1, 0.3], [1.0, 1.5, 2.5], [-0.95, -0.7, -0.5]
     T, K = [0.25, 1.0, 2.0], [0.9, 1.0, 1.3]
     Z = R.generate_normals(5, M, N)

@@ -51,8 +51,10 @@ CASES = [
     # two Volterra passes, several variance groups, N = 1024 (two TMEM passes of the tensor-core GEMM)
     dict(xi=0.04, H=[0.07, 0.3], eta=[1.5, 2.0], rho=[-0.7, -0.5], T=[0.5, 2.0], K=[0.9, 1.2], N=1024, M=5000,
          seed=3),
-    # longer horizon: the batched-FFT backend
+    # longer horizon: three TMEM passes with streamed strip windows, and the batched-FFT backend
     dict(xi=0.05, H=[0.1], eta=[1.5], rho=[-0.7], T=[2.0, 2.0, 2.0], K=[0.8, 1.0, 1.2], N=1500, M=3001, seed=4),
+    dict(xi=0.05, H=[0.1], eta=[1.5], rho=[-0.7], T=[2.0, 2.0, 2.0], K=[0.8, 1.0, 1.2], N=1500, M=3001, seed=4,
+         conv=2),
     # eight variance groups over 300,001 paths: the (Ivdt, IsvdW) buffer (8 B per group and path, 19.2 MB)
     # does not fit the 16 MiB array, so the paths run in smaller batches than rbg_price_rt's single one
     dict(xi=0.04, H=[0.1], eta=[1.9], rho=[-0.9], T=[0.25, 0.5, 0.75, 1.0, 1.25, 1.5, 1.75, 2.0],
@@ -64,10 +66,11 @@ CASES = [
 def test_static_entry_point_matches_regular(R, case):
     c = dict(CASES[case])
     seed = c.pop("seed")
+    conv = c.pop("conv", 0)
     args = (c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], c["N"], c["M"])
-    want_p, want_s, want_iv = R.price_rt(*args, seed=seed, precision=R.MIXED)
+    want_p, want_s, want_iv = R.price_rt(*args, seed=seed, precision=R.MIXED, conv=conv)
     for _ in range(2):  # second call runs on the contents the first call left behind
-        p, s, iv = static_price(R, *args, seed=seed)
+        p, s, iv = static_price(R, *args, seed=seed, conv=conv)
         np.testing.assert_allclose(p, want_p, rtol=RTOL, atol=0)
         np.testing.assert_allclose(s, want_s, rtol=1e-9, atol=0)
         np.testing.assert_allclose(iv, want_iv, rtol=1e-9, atol=0)
