@@ -755,9 +755,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 const int cb = pp.begin(q), ce = pp.end(q);
                 for (int c = 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
                     // redrawn chunks of a later pass feed only the MMA (W1 A tile)
-                    const bool redraw = c < cb;
+                    const bool redraw = PM > 0 && c < cb;
                     // last real chunk of a pass before the last: boundary row for its successor
-                    const bool bnd = !redraw && c == ce - 1 && q + 1 < pp.np;
+                    const bool bnd = PM > 0 && !redraw && c == ce - 1 && q + 1 < pp.np;
                     if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
                     unsigned char* st = base + L.a0 + s * kStageA;
                     float* w1s = (float*)(base + L.f0 + s * FB);
@@ -818,7 +818,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 // the producers' FP32 tiles of this stage (the upper half also pairs
                 // its last column with the next chunk's first W1), then the MMA results
                 if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7, a.prof)) goto done;
-                if (c < cb) {
+                if (PM > 0 && c < cb) {
                     // redrawn chunk: no column becomes final.  Its MMA completion is still
                     // awaited, so that every accf phase is observed in order.
                     if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
@@ -826,10 +826,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     if (lane == 0) mbar_arrive(smem_u32(empty + s));
                     continue;
                 }
-                const uint32_t tcol0 = (uint32_t)(kChunk * cb);  // TMEM column of output 0 of this pass
+                const uint32_t tcol0 = PM > 0 ? (uint32_t)(kChunk * cb) : 0u;  // TMEM column of output 0 of this pass
                 const bool pass_end = c == ce - 1;
                 const bool has_next = c + 1 < nc;
-                const bool bnd = pass_end && q + 1 < pp.np;  // successor W1 in this stage's boundary row
+                const bool bnd = PM > 0 && pass_end && q + 1 < pp.np;  // successor W1 in this stage's boundary row
                 const int sn = (s + 1 == S) ? 0 : s + 1;
                 if ((kEpiWGs == 1 || wg == 1) && has_next && !bnd &&
                     !mbar_wait_warp(smem_u32(full + sn), sn == 0 ? ph ^ 1u : ph, a.err, 8, a.prof))
@@ -1012,8 +1012,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     const int cb = pp.begin(q), ce = pp.end(q);
                     for (int c = 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
                         // output columns [lo, hi) of this chunk; TMEM column = output column - toff
-                        const bool redraw = c < cb;
-                        const int lo = redraw ? kChunk * cb : kChunk * c, hi = kChunk * ce, toff = kChunk * cb;
+                        const bool redraw = PM > 0 && c < cb;
+                        const int lo = redraw ? kChunk * cb : kChunk * c, hi = kChunk * ce;
+                        const int toff = PM > 0 ? kChunk * cb : 0;
                         const bool first = c == 0;  // first chunk of a pass overwrites
                         if (first) {
                             // the epilogue has read every column of the previous pass
