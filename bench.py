@@ -345,7 +345,8 @@ def run_gpu(args, w):
     achieved_tf = algo_flops / (avg_kernel_ms / 1e3) / 1e12
     Np = (w["N"] + 31) // 32 * 32
     nc = Np // 32
-    exec_flops = 6.0 * 32 * 32 * nc * (nc + 1) / 2 * w["M"] / max(1, kn // args.steps)
+    # split products on the tensor pipe: three (16-bit splits) or two (TF32 with one compensation term)
+    exec_flops = (4.0 if args.split == 2 else 6.0) * 32 * 32 * nc * (nc + 1) / 2 * w["M"] / max(1, kn // args.steps)
     fp64_fft = args.conv == "fft" or (args.conv == "auto" and 200 <= w["N"] <= 2048)
     kname = ("k_mixed_fft" if (args.conv == "fft" or (args.conv == "auto" and w["N"] > 1024))
              else "k_mixed_gemm") if prec == R.MIXED else ("k_path_fp64_fft" if fp64_fft else "k_path_fp64")
@@ -409,7 +410,7 @@ def run_gpu(args, w):
         "metric": METRIC, "value": value, "unit": "path-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": ("bf16x3" if args.split == 0 else "f16x3") + "+f32+f64" if prec == R.MIXED else "f64",
+        "dtype": ("bf16x3", "f16x3", "tf32x2")[args.split] + "+f32+f64" if prec == R.MIXED else "f64",
         "data": "synthetic (Philox4x32-10 normals generated on device)",
         "config": {"workload": args.workload, "N": w["N"], "M": w["M"], "strikes": len(w["K"]),
                    "H": w["H"], "eta": w["eta"], "rho": w["rho"], "xi": w["xi"], "T": w["T"][0],
@@ -681,7 +682,8 @@ def main():
     ap.add_argument("--workload", default=DEFAULT,
                     choices=sorted(WORKLOADS) + ["serving-poisson", "paramtot-grid-m1m", "sobol-fp64-n256-m1m"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
-    ap.add_argument("--split", type=int, default=0, help="0 = BF16x3, 1 = FP16x3")
+    ap.add_argument("--split", type=int, default=0,
+                    help="0 = BF16x3, 1 = FP16x3, 2 = TF32 with one compensation term")
     ap.add_argument("--cpu-paths", type=int, default=1 << 18,
                     help="CPU legs: paths per sample (about 20 core-seconds on 16 cores at N = 512)")
     ap.add_argument("--paths", type=int, default=None, help="override M (small cases for ncu captures)")

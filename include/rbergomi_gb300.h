@@ -95,9 +95,10 @@ enum rbg_precision { RBG_FP64 = 0, RBG_MIXED = 1 };
 /* Volterra convolution backend.  In mixed mode AUTO picks the tcgen05
  * Toeplitz GEMM for N <= 4096 (one TMEM pass up to 512 steps, one more per
  * further 512; measured faster than the batched FFT convolution at every N
- * up to 4096); FFT selects the batched FFT convolution (N <= 4096).  The FP64 form has two: the direct
- * causal sum (DIRECT) and an FP64 FFT convolution (FFT, 2 <= N <= 2048); AUTO
- * takes the FFT from 200 steps to 2048.  GEMM is mixed-mode only. */
+ * up to 4096); FFT selects the batched FFT convolution (N <= 4096).  The
+ * FP64 form has two: the direct causal sum (DIRECT) and an FP64 FFT
+ * convolution (FFT, 2 <= N <= 2048); AUTO takes the FFT from 200 steps to
+ * 2048.  GEMM is mixed-mode only. */
 enum rbg_conv { RBG_CONV_AUTO = 0, RBG_CONV_GEMM = 1, RBG_CONV_FFT = 2, RBG_CONV_DIRECT = 3 };
 
 /* Normal transform used by the FP64 form: its own FP64 Box-Muller (default),
@@ -105,8 +106,12 @@ enum rbg_conv { RBG_CONV_AUTO = 0, RBG_CONV_GEMM = 1, RBG_CONV_FFT = 2, RBG_CONV
  * run sees exactly the normals a mixed run with the same seed sees. */
 enum rbg_normals { RBG_NORMALS_F64 = 0, RBG_NORMALS_F32 = 1 };
 
-/* Split used by the mixed-form tensor-core convolution. */
-enum rbg_split { RBG_SPLIT_BF16X3 = 0, RBG_SPLIT_F16X3 = 1 };
+/* Split used by the mixed-form tensor-core convolution: BF16x3 and FP16x3
+ * split both operands into 16-bit hi + lo and sum three products (lo x lo
+ * dropped); TF32X2 rounds the normals to TF32 (kind::tf32, round to nearest)
+ * and splits the kernel table Gamma into TF32 hi + lo: two products, one
+ * compensation term. */
+enum rbg_split { RBG_SPLIT_BF16X3 = 0, RBG_SPLIT_F16X3 = 1, RBG_SPLIT_TF32X2 = 2 };
 
 typedef struct rbg_params {
     double xi;

@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(_HERE, "librbergomi_gb300.so")
 FP64, MIXED = 0, 1
 CONV_AUTO, CONV_GEMM, CONV_FFT, CONV_DIRECT = 0, 1, 2, 3
 NORMALS_F64, NORMALS_F32 = 0, 1
-SPLIT_BF16X3, SPLIT_F16X3 = 0, 1
+SPLIT_BF16X3, SPLIT_F16X3, SPLIT_TF32X2 = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _u64p = C.POINTER(C.c_uint64)

@@ -113,6 +113,15 @@ __host__ __device__ inline int pass_mode(int Np) { return Np <= kPassCols ? 0 : 
 // Narrow-strip rows one pass of one chunk reads: 512 columns + 16 (K halves).
 constexpr int kWindowRows = kPassCols + kStripK;
 constexpr int kWindowBytes = kWindowRows * kStripK * 2;  // one 16-bit half, 16896 B
+// TF32 split (split kind 2): the strip is always narrow, P[r][k] = Gamma[r -
+// 24 - k], Np + 24 rows of 8 FP32 (32 B, SW32); the four K = 8 steps of a
+// chunk read it at row offsets 8 apart.  Its window is 512 + 24 rows.
+constexpr int kStripKT = 8;
+constexpr int kLeadT = kChunk - kStripKT;                   // 24 leading zero rows
+constexpr int kWindowRowsT = kPassCols + kLeadT;            // 536
+constexpr int kWindowBytesT = kWindowRowsT * kStripKT * 4;  // one TF32 half, 17152 B
+// Kernel split kind of an rbg_split: 0 FP16x3, 1 BF16x3, 2 TF32x2.
+inline int split_kind(int split) { return split == RBG_SPLIT_BF16X3 ? 1 : (split == RBG_SPLIT_F16X3 ? 0 : 2); }
 // FP32 tiles are path-major, [128 paths][32 steps], with the 16-byte chunk
 // index XORed by (path mod 8): a thread's 4 consecutive steps are one vector
 // access and the 8 threads of a vector phase hit distinct banks.
@@ -127,26 +136,35 @@ struct SmemLayout {
     int strip, a0, f0, fstride, stages, acc, beta, otab, osum, bars, total;
 };
 
+__host__ __device__ inline int strip_bytes_t32(int Np) { return 2 * (Np + kLeadT) * kStripKT * 4; }
+__host__ __device__ inline int strip_bytes_sk(int Np, bool tf32) { return tf32 ? strip_bytes_t32(Np) : strip_bytes(Np); }
+
 // Resident strip bytes: the whole image (pass modes 0, 1) or the first
 // kWindowRows rows of each half (pass mode 2).
 __host__ __device__ inline int strip_smem_bytes(int Np)
 {
     return pass_mode(Np) == 2 ? 2 * kWindowBytes : strip_bytes(Np);
 }
+__host__ __device__ inline int strip_smem_bytes_t32(int Np)
+{
+    return pass_mode(Np) == 2 ? 2 * kWindowBytesT : strip_bytes_t32(Np);
+}
 
 // ns: normal streams per path, 2 (RT) or 3 (plain Monte Carlo: ns sums per group).
 // In pass mode 2 a stage's FP32-tile region also holds a redrawn chunk's strip
 // window (hi and lo halves), so it is at least 2 kWindowBytes (a multiple of
 // the 256-byte SW32 swizzle atom).
-__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, int n_o, int ns = 2)
+// tf32: the TF32 strip geometry (split kind 2).
+__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, int n_o, int ns = 2, bool tf32 = false)
 {
     SmemLayout L;
     L.strip = 0;
-    L.a0 = (strip_smem_bytes(Np) + 1023) / 1024 * 1024;
+    L.a0 = ((tf32 ? strip_smem_bytes_t32(Np) : strip_smem_bytes(Np)) + 1023) / 1024 * 1024;
     L.stages = stages;
     L.f0 = L.a0 + stages * kStageA;
     L.fstride = stage_f_bytes(ns);
-    if (pass_mode(Np) == 2 && L.fstride < 2 * kWindowBytes) L.fstride = 2 * kWindowBytes;
+    const int win2 = tf32 ? 2 * kWindowBytesT : 2 * kWindowBytes;
+    if (pass_mode(Np) == 2 && L.fstride < win2) L.fstride = win2;
     L.acc = L.f0 + stages * L.fstride;
     L.beta = L.acc + 2 * n_g * ns * kTileM * 4 + (ns - 1) * kTileM * 4;  // per warpgroup, then W1_0 (Wperp_0)
     L.otab = L.beta + n_g * Np * 4;
@@ -269,6 +287,30 @@ __device__ __forceinline__ uint64_t sdesc_sw32(uint32_t addr)
            ((uint64_t)1 << 46) | ((uint64_t)6 << 61);
 }
 
+// SW128 K-major descriptor for the TF32 A tile: 128-byte rows (32 FP32), SBO
+// = 8 rows x 128 B, layout type SWIZZLE_128B (2).  A K = 8 step starts 32 B
+// further into the row; the tile base is 1024-aligned, so the swizzle phase
+// (address bits 7-9, the row) is unchanged and the base offset stays 0.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t addr)
+{
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor, kind::tf32: D = F32, A = B = TF32 (2), both K-major.
+__device__ __forceinline__ uint32_t idesc_tf32(int n)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+}
+
+// FP32 -> TF32 rounded to nearest even (the low 13 bits of the result are 0).
+__device__ __forceinline__ uint32_t tf32_rn(float x)
+{
+    uint32_t r;
+    asm("cvt.rn.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16 (1) or F16 (0),
 // both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
 __device__ __forceinline__ uint32_t idesc_f16(int n, int ab_bf16)
@@ -282,6 +324,15 @@ __device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a, uint64_t b
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
         "l"(a), "l"(b), "r"(idesc), "r"(acc)
         : "memory");
 }
@@ -323,6 +374,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Split kinds of the mixed-form convolution: 0 FP16x3, 1 BF16x3 (A and B
+// each split into 16-bit hi + lo, three products), 2 TF32 with one
+// compensation term (A rounded to TF32, B = hi + lo in TF32, two products).
 // 16-bit split x = hi + lo (+ O(2^-16 |x|) for BF16, O(2^-22 |x|) for FP16)
 template <int BF16>
 __device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_t& lo)
@@ -339,6 +393,24 @@ __device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_
         __half2 l = __floats2half2_rn(x0 - hf.x, x1 - hf.y);
         hi = *reinterpret_cast<uint32_t*>(&h);
         lo = *reinterpret_cast<uint32_t*>(&l);
+    }
+}
+
+// One element (path row p, step k of the chunk) of the A tile: hi / lo
+// 16-bit halves in SW64 rows of 64 B, or (SK = 2) one TF32 in SW128 rows of
+// 128 B.
+template <int SK>
+__device__ __forceinline__ void a_tile_store1(unsigned char* st, int p, int k, float z)
+{
+    if constexpr (SK == 2) {
+        const int off = p * 128 + ((((k >> 2)) ^ (p & 7)) << 4) + ((k & 3) << 2);
+        *(uint32_t*)(st + off) = tf32_rn(z);
+    } else {
+        uint32_t hi, lo;
+        split2<SK>(z, 0.f, hi, lo);
+        const int off = p * 64 + ((((k >> 3)) ^ ((p >> 1) & 3)) << 4) + ((k & 7) << 1);
+        *(unsigned short*)(st + off) = (unsigned short)hi;
+        *(unsigned short*)(st + kTileBytes + off) = (unsigned short)lo;
     }
 }
 
@@ -384,7 +456,7 @@ __device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rh
 // REDRAW (a first-pass chunk drawn again for the second pass), the FP32 W1 /
 // W1perp tiles the epilogue reads.  Compiled per REDRAW so that the W1 and
 // W1perp Philox streams stay interleaved in the common case.
-template <int BF16, bool REDRAW, bool MC>
+template <int SK, bool REDRAW, bool MC>
 __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKeys& keys, uint64_t gpath, bool valid,
                                               int64_t m, int p, int h, int c, bool bnd, unsigned char* st,
                                               float* w1s)
@@ -422,15 +494,26 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
             }
         }
     }
-    // A tile: row p, logical 16-byte chunks covering steps [SPT h, SPT h + SPT), SW64 swizzle
-    uint32_t hi[SPT / 2], lo[SPT / 2];
+    if constexpr (SK == 2) {
+        // A tile: row p, 128 B of TF32 (rounded to nearest), 16-byte chunks covering
+        // steps [SPT h, SPT h + SPT), SW128 swizzle (chunk XOR row mod 8)
 #pragma unroll
-    for (int q = 0; q < SPT / 2; ++q) split2<BF16>(w[2 * q], w[2 * q + 1], hi[q], lo[q]);
+        for (int e = 0; e < SPT / 4; ++e) {
+            const int off = p * 128 + ((((SPT / 4) * h + e) ^ (p & 7)) << 4);
+            *(uint4*)(st + off) = make_uint4(tf32_rn(w[4 * e]), tf32_rn(w[4 * e + 1]), tf32_rn(w[4 * e + 2]),
+                                             tf32_rn(w[4 * e + 3]));
+        }
+    } else {
+        // A tile: row p, logical 16-byte chunks covering steps [SPT h, SPT h + SPT), SW64 swizzle
+        uint32_t hi[SPT / 2], lo[SPT / 2];
 #pragma unroll
-    for (int e = 0; e < SPT / 8; ++e) {
-        const int off = p * 64 + ((((SPT / 8) * h + e) ^ sw) << 4);
-        *(uint4*)(st + off) = make_uint4(hi[4 * e], hi[4 * e + 1], hi[4 * e + 2], hi[4 * e + 3]);
-        *(uint4*)(st + kTileBytes + off) = make_uint4(lo[4 * e], lo[4 * e + 1], lo[4 * e + 2], lo[4 * e + 3]);
+        for (int q = 0; q < SPT / 2; ++q) split2<SK>(w[2 * q], w[2 * q + 1], hi[q], lo[q]);
+#pragma unroll
+        for (int e = 0; e < SPT / 8; ++e) {
+            const int off = p * 64 + ((((SPT / 8) * h + e) ^ sw) << 4);
+            *(uint4*)(st + off) = make_uint4(hi[4 * e], hi[4 * e + 1], hi[4 * e + 2], hi[4 * e + 3]);
+            *(uint4*)(st + kTileBytes + off) = make_uint4(lo[4 * e], lo[4 * e + 1], lo[4 * e + 2], lo[4 * e + 3]);
+        }
     }
     if (!REDRAW) {
 #pragma unroll
@@ -495,7 +578,7 @@ __device__ __forceinline__ void sobol_gray_start(const uint2* tab, int N, int j,
 
 // One point of the Sobol' producer: lane's step j of path row p (path m),
 // from the point's coordinates q0 (W1) and q1 (W1perp).
-template <int BF16, bool REDRAW>
+template <int SK, bool REDRAW>
 __device__ __forceinline__ void sobol_point(const MixedArgs& a, int p, int64_t m, int j, int lane, bool jin,
                                             unsigned int q0, unsigned int q1, unsigned char* st, float* w1s)
 {
@@ -511,14 +594,10 @@ __device__ __forceinline__ void sobol_point(const MixedArgs& a, int p, int64_t m
             a.dbg_w[(m * 2 + 1) * a.Np + j] = z1;
         }
     }
-    uint32_t hi, lo;
-    split2<BF16>(z0, 0.f, hi, lo);
-    const int off = p * 64 + ((((lane >> 3)) ^ ((p >> 1) & 3)) << 4) + ((lane & 7) << 1);
-    *(unsigned short*)(st + off) = (unsigned short)hi;
-    *(unsigned short*)(st + kTileBytes + off) = (unsigned short)lo;
+    a_tile_store1<SK>(st, p, lane, z0);
 }
 
-template <int BF16, bool REDRAW>
+template <int SK, bool REDRAW>
 __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t tile, int c, bool bnd, unsigned char* st,
                                                     float* w1s)
 {
@@ -550,20 +629,20 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
 #pragma unroll 1
         for (int t = 0; t < 4; ++t) {
             const int i0 = 4 * t, p0 = 16 * w + i0;
-            sobol_point<BF16, REDRAW>(a, p0, m0 + i0, j, lane, jin, q0, q1, st, w1s);
+            sobol_point<SK, REDRAW>(a, p0, m0 + i0, j, lane, jin, q0, q1, st, w1s);
             q0 ^= r[1].x; q1 ^= r[1].y;
-            sobol_point<BF16, REDRAW>(a, p0 + 1, m0 + i0 + 1, j, lane, jin, q0, q1, st, w1s);
+            sobol_point<SK, REDRAW>(a, p0 + 1, m0 + i0 + 1, j, lane, jin, q0, q1, st, w1s);
             q0 ^= r[0].x; q1 ^= r[0].y;
-            sobol_point<BF16, REDRAW>(a, p0 + 2, m0 + i0 + 2, j, lane, jin, q0, q1, st, w1s);
+            sobol_point<SK, REDRAW>(a, p0 + 2, m0 + i0 + 2, j, lane, jin, q0, q1, st, w1s);
             const uint2 v = t == 1 ? r[3] : t == 3 ? rb : r[2];
             q0 ^= v.x; q1 ^= v.y;
-            sobol_point<BF16, REDRAW>(a, p0 + 3, m0 + i0 + 3, j, lane, jin, q0, q1, st, w1s);
+            sobol_point<SK, REDRAW>(a, p0 + 3, m0 + i0 + 3, j, lane, jin, q0, q1, st, w1s);
             q0 ^= r[0].x; q1 ^= r[0].y;
         }
     } else {
 #pragma unroll 4
         for (int i = 0; i < 16; ++i) {
-            sobol_point<BF16, REDRAW>(a, 16 * w + i, m0 + i, j, lane, jin, q0, q1, st, w1s);
+            sobol_point<SK, REDRAW>(a, 16 * w + i, m0 + i, j, lane, jin, q0, q1, st, w1s);
             if (i < 15) {
                 const int k = __ffsll((long long)(s0 + i + 1)) - 1;
                 const uint2 v = k == 0 ? r[0] : k == 1 ? r[1] : k == 2 ? r[2] : k == 3 ? r[3] : rb;
@@ -590,7 +669,7 @@ __device__ __forceinline__ void produce_chunk_sobol(const MixedArgs& a, int64_t 
 // consecutive doubles of one row (256 B, coalesced; no alignment beyond the
 // doubles' own).  Writes the FP32 W1 / W1perp (/ Wperp) tiles and the 16-bit
 // hi/lo A tile (REDRAW: W1 and the A tile only).
-template <int BF16, bool REDRAW, bool MC>
+template <int SK, bool REDRAW, bool MC>
 __device__ __forceinline__ void produce_chunk_ext(const MixedArgs& a, int64_t tile, int c, bool bnd, unsigned char* st,
                                                   float* w1s)
 {
@@ -617,11 +696,7 @@ __device__ __forceinline__ void produce_chunk_ext(const MixedArgs& a, int64_t ti
                 a.dbg_w[(m * 2 + 1) * Np + j] = w1ps[ftile_at(p, lane)];
             }
         }
-        uint32_t hi, lo;
-        split2<BF16>(z0, 0.f, hi, lo);
-        const int off = p * 64 + ((((lane >> 3)) ^ ((p >> 1) & 3)) << 4) + ((lane & 7) << 1);
-        *(unsigned short*)(st + off) = (unsigned short)hi;
-        *(unsigned short*)(st + kTileBytes + off) = (unsigned short)lo;
+        a_tile_store1<SK>(st, p, lane, z0);
     }
     // the next chunk's rows into L2 while this one is consumed: the loads above
     // keep too few bytes in flight to cover HBM latency on their own.  One
@@ -665,21 +740,24 @@ struct PassPlan {
 };
 
 // PM: pass mode (pass_mode(Np)): 0 one TMEM pass; 1 two passes, the narrow
-// strip resident; 2 up to eight passes, the strip's first kWindowRows rows
+// strip resident; 2 up to eight passes, the strip's first window of rows
 // resident and each redrawn chunk's window brought into its stage's FP32-tile
 // region by a bulk copy that the stage's `full` barrier waits for.
 // SRC: where the normals come from: 0 Philox, 1 Sobol' (produce_chunk_sobol,
 // RT only), 2 the caller's FP64 normals (a.ext, quadrature layout).
-template <int BF16, int PM, bool MC, int SRC = 0>
+// SK: split kind (0 FP16x3, 1 BF16x3, 2 TF32 with one compensation term).
+template <int SK, int PM, bool MC, int SRC = 0>
 __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
     constexpr int NS = MC ? 3 : 2;  // normal streams per path = sums per variance group
     constexpr int kStageFB = stage_f_bytes(NS);
-    static_assert(PM >= 0 && PM <= 2, "pass mode");
+    constexpr bool T32 = SK == 2;
+    constexpr int WB = T32 ? kWindowBytesT : kWindowBytes;  // one half of a strip window
+    static_assert(PM >= 0 && PM <= 2 && SK >= 0 && SK <= 2, "pass mode / split kind");
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g, a.n_o, NS);
+    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g, a.n_o, NS, T32);
     unsigned char* strip = base + L.strip;
     float* acc_s = (float*)(base + L.acc);
     float* beta_s = (float*)(base + L.beta);
@@ -701,8 +779,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     const PassPlan<PM> pp(a);
     const int FB = (PM == 2) ? L.fstride : kStageFB;  // bytes per stage of the FP32-tile region
     const int64_t ntiles = (a.B + kTileM - 1) / kTileM;
-    const uint32_t sbytes = (uint32_t)strip_smem_bytes(Np);
-    const uint32_t half_g = (uint32_t)(strip_bytes(Np) / 2);  // hi -> lo in the global image
+    const uint32_t sbytes = (uint32_t)(T32 ? strip_smem_bytes_t32(Np) : strip_smem_bytes(Np));
+    const uint32_t half_g = (uint32_t)((T32 ? strip_bytes_t32(Np) : strip_bytes(Np)) / 2);  // hi -> lo in the global image
 
     if (threadIdx.x == kMmaWarp * 32) {
         for (int s = 0; s < S; ++s) {
@@ -716,9 +794,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         mbar_expect_tx(smem_u32(strip_bar), sbytes);
         if (PM == 2) {
-            // the first kWindowRows rows of each half
-            bulk_g2s(smem_u32(strip), a.strip, kWindowBytes, smem_u32(strip_bar));
-            bulk_g2s(smem_u32(strip) + kWindowBytes, a.strip + half_g, kWindowBytes, smem_u32(strip_bar));
+            // the first window of each half
+            bulk_g2s(smem_u32(strip), a.strip, WB, smem_u32(strip_bar));
+            bulk_g2s(smem_u32(strip) + WB, a.strip + half_g, WB, smem_u32(strip_bar));
         } else {
             bulk_g2s(smem_u32(strip), a.strip, sbytes, smem_u32(strip_bar));
         }
@@ -762,30 +840,31 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     unsigned char* st = base + L.a0 + s * kStageA;
                     float* w1s = (float*)(base + L.f0 + s * FB);
                     if (PM == 2 && redraw && threadIdx.x == 0) {
-                        // this chunk's strip window, rows [32 (cb - c), + kWindowRows) of each half,
-                        // into the stage's FP32-tile region (unused by redrawn chunks); the MMA
-                        // issuer's wait on `full` covers the bytes
+                        // this chunk's strip window, rows [32 (cb - c), + the window's rows) of each
+                        // half (32-byte rows in both narrow strips), into the stage's FP32-tile
+                        // region (unused by redrawn chunks); the MMA issuer's wait on `full`
+                        // covers the bytes
                         const uint32_t dst = smem_u32(w1s), bar = smem_u32(full + s);
-                        const unsigned char* src = a.strip + (size_t)(kChunk * (cb - c)) * (kStripK * 2);
+                        const unsigned char* src = a.strip + (size_t)(kChunk * (cb - c)) * 32;
                         fence_proxy_async();
-                        mbar_expect_tx_only(bar, 2 * kWindowBytes);
-                        bulk_g2s(dst, src, kWindowBytes, bar);
-                        bulk_g2s(dst + kWindowBytes, src + half_g, kWindowBytes, bar);
+                        mbar_expect_tx_only(bar, 2 * WB);
+                        bulk_g2s(dst, src, WB, bar);
+                        bulk_g2s(dst + WB, src + half_g, WB, bar);
                     }
                     if (SRC == 1) {
                         if (PM > 0 && redraw)
-                            produce_chunk_sobol<BF16, true>(a, tile, c, bnd, st, w1s);
+                            produce_chunk_sobol<SK, true>(a, tile, c, bnd, st, w1s);
                         else
-                            produce_chunk_sobol<BF16, false>(a, tile, c, bnd, st, w1s);
+                            produce_chunk_sobol<SK, false>(a, tile, c, bnd, st, w1s);
                     } else if (SRC == 2) {
                         if (PM > 0 && redraw)
-                            produce_chunk_ext<BF16, true, MC>(a, tile, c, bnd, st, w1s);
+                            produce_chunk_ext<SK, true, MC>(a, tile, c, bnd, st, w1s);
                         else
-                            produce_chunk_ext<BF16, false, MC>(a, tile, c, bnd, st, w1s);
+                            produce_chunk_ext<SK, false, MC>(a, tile, c, bnd, st, w1s);
                     } else if (PM > 0 && redraw) {
-                        produce_chunk<BF16, true, MC>(a, keys, gpath, valid, m, p, h, c, bnd, st, w1s);
+                        produce_chunk<SK, true, MC>(a, keys, gpath, valid, m, p, h, c, bnd, st, w1s);
                     } else {
-                        produce_chunk<BF16, false, MC>(a, keys, gpath, valid, m, p, h, c, bnd, st, w1s);
+                        produce_chunk<SK, false, MC>(a, keys, gpath, valid, m, p, h, c, bnd, st, w1s);
                     }
                     fence_proxy_async();
                     __syncwarp();
@@ -1000,8 +1079,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     } else if (lane == 0) {
         // ------------------------------------------------------ MMA issuer
         const uint32_t strip_hi = smem_u32(strip);
-        const uint32_t strip_lo = strip_hi + (uint32_t)(strip_smem_bytes(Np) / 2);
-        constexpr bool wide = PM == 0;  // strip_k(Np) == kChunk exactly when one pass covers Np
+        const uint32_t strip_lo = strip_hi + (uint32_t)((T32 ? strip_smem_bytes_t32(Np) : strip_smem_bytes(Np)) / 2);
+        constexpr bool wide = PM == 0 && !T32;  // the wide 16-bit strip exactly when one pass covers Np
         if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
             int64_t pass = 0;
             int s = 0;
@@ -1034,30 +1113,48 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                         // in this stage whose row 0 is strip row lo - 32 c
                         const bool win = PM == 2 && redraw;
                         const uint32_t bhi = win ? smem_u32(base + L.f0 + s * FB) : strip_hi;
-                        const uint32_t blo = win ? bhi + (uint32_t)kWindowBytes : strip_lo;
+                        const uint32_t blo = win ? bhi + (uint32_t)WB : strip_lo;
                         const int rbase = win ? lo : kChunk * c;
-                        for (int col0 = lo; col0 < hi; col0 += 256) {
-                            const int n = (hi - col0 < 256) ? (hi - col0) : 256;
-                            const uint32_t id = idesc_f16(n, BF16);
-                            const uint32_t jrow = (uint32_t)(col0 - rbase);
-                            const uint32_t d = tmem + (uint32_t)(col0 - toff);
+                        if constexpr (T32) {
+                            // TF32: four K = 8 steps per chunk, A in TF32 (SW128) against the
+                            // narrow strip's hi and lo halves at row offsets 8 apart
+                            for (int col0 = lo; col0 < hi; col0 += 256) {
+                                const int n = (hi - col0 < 256) ? (hi - col0) : 256;
+                                const uint32_t id = idesc_tf32(n);
+                                const uint32_t jrow = (uint32_t)(col0 - rbase);
+                                const uint32_t d = tmem + (uint32_t)(col0 - toff);
 #pragma unroll
-                            for (int ks = 0; ks < 2; ++ks) {
-                                // K half ks: A columns [16 ks, 16 ks + 16); wide strip: row jrow, bytes
-                                // [32 ks, 32 ks + 32); narrow strip: rows from jrow + 16 - 16 ks
-                                const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
-                                uint64_t dbh, dbl;
-                                if (wide) {
-                                    dbh = sdesc_sw64(bhi + jrow * 64 + 32 * ks);
-                                    dbl = sdesc_sw64(blo + jrow * 64 + 32 * ks);
-                                } else {
-                                    const uint32_t boff = (jrow + (uint32_t)(kStripK * (1 - ks))) * (kStripK * 2);
-                                    dbh = sdesc_sw32(bhi + boff);
-                                    dbl = sdesc_sw32(blo + boff);
+                                for (int ks = 0; ks < kChunk / kStripKT; ++ks) {
+                                    const uint64_t da = sdesc_sw128(ahi + 32 * ks);
+                                    const uint32_t boff = (jrow + (uint32_t)(kStripKT * (3 - ks))) * 32u;
+                                    umma_tf32(d, da, sdesc_sw32(bhi + boff), id, (first && ks == 0) ? 0u : 1u);
+                                    umma_tf32(d, da, sdesc_sw32(blo + boff), id, 1u);
                                 }
-                                umma_f16(d, dah, dbh, id, (first && ks == 0) ? 0u : 1u);
-                                umma_f16(d, dah, dbl, id, 1u);
-                                umma_f16(d, dal, dbh, id, 1u);
+                            }
+                        } else {
+                            for (int col0 = lo; col0 < hi; col0 += 256) {
+                                const int n = (hi - col0 < 256) ? (hi - col0) : 256;
+                                const uint32_t id = idesc_f16(n, SK);
+                                const uint32_t jrow = (uint32_t)(col0 - rbase);
+                                const uint32_t d = tmem + (uint32_t)(col0 - toff);
+#pragma unroll
+                                for (int ks = 0; ks < 2; ++ks) {
+                                    // K half ks: A columns [16 ks, 16 ks + 16); wide strip: row jrow, bytes
+                                    // [32 ks, 32 ks + 32); narrow strip: rows from jrow + 16 - 16 ks
+                                    const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
+                                    uint64_t dbh, dbl;
+                                    if (wide) {
+                                        dbh = sdesc_sw64(bhi + jrow * 64 + 32 * ks);
+                                        dbl = sdesc_sw64(blo + jrow * 64 + 32 * ks);
+                                    } else {
+                                        const uint32_t boff = (jrow + (uint32_t)(kStripK * (1 - ks))) * (kStripK * 2);
+                                        dbh = sdesc_sw32(bhi + boff);
+                                        dbl = sdesc_sw32(blo + boff);
+                                    }
+                                    umma_f16(d, dah, dbh, id, (first && ks == 0) ? 0u : 1u);
+                                    umma_f16(d, dah, dbl, id, 1u);
+                                    umma_f16(d, dal, dbh, id, 1u);
+                                }
                             }
                         }
                         umma_commit(smem_u32(empty + s));
@@ -1281,8 +1378,39 @@ float from_f16(uint16_t u)
 // The near-field term a1 W1_j stays out of the split products: the epilogue
 // adds it from the FP32 normal, which keeps X an order of magnitude closer
 // to FP64 than folding a1 into the strip's diagonal (measured; no speed-up).
-void build_strip(const double* gamma, int N, int Np, int bf16, unsigned char* img)
+// FP32 -> TF32 (10-bit mantissa) rounded to nearest even, as the FP32 bit
+// pattern with the low 13 bits zero.
+float to_tf32(float f)
 {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    u += 0xFFFu + ((u >> 13) & 1u);
+    u &= ~0x1FFFu;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// sk: split kind, 0 FP16 / 1 BF16 halves (wide or narrow 16-bit strip) or
+// 2 TF32 halves (the narrow TF32 strip, P[r][k] = Gamma[r - 24 - k], 8 FP32 per
+// 32-byte SW32 row).
+void build_strip(const double* gamma, int N, int Np, int sk, unsigned char* img)
+{
+    if (sk == 2) {
+        const size_t half = (size_t)strip_bytes_t32(Np) / 2;
+        std::memset(img, 0, 2 * half);
+        for (int r = 0; r < Np + kLeadT; ++r)
+            for (int k = 0; k < kStripKT; ++k) {
+                const int d = r - kLeadT - k;
+                const double gv = (d >= 0 && d < N) ? gamma[d] : 0.0;
+                const float hi = to_tf32((float)gv);
+                const float lo = to_tf32((float)(gv - (double)hi));
+                const size_t off = (size_t)r * 32 + ((((k >> 2) ^ ((r >> 2) & 1))) << 4) + (k & 3) * 4;
+                std::memcpy(img + off, &hi, 4);
+                std::memcpy(img + half + off, &lo, 4);
+            }
+        return;
+    }
+    const int bf16 = sk;
     const size_t half = (size_t)strip_bytes(Np) / 2;
     std::memset(img, 0, 2 * half);
     const bool wide = strip_k(Np) == kChunk;
@@ -1313,7 +1441,7 @@ void mixed_table_range(const MixedJob& job, int i, size_t* off, size_t* bytes)
     const MixedLaunch& r = job.launches[i];
     if (job.backend == RBG_CONV_GEMM) {
         *off = r.off_strip;
-        *bytes = (size_t)strip_bytes(r.args.Np);
+        *bytes = (size_t)strip_bytes_sk(r.args.Np, job.split == RBG_SPLIT_TF32X2);
     } else {
         *off = r.off_spec;
         *bytes = (size_t)r.args.L * 8;
@@ -1366,15 +1494,21 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     job.n_vg = (int)plan.vgs.size();
     job.split = o.split;
     job.sms = prop.multiProcessorCount;
-    const int bf16 = (o.split == RBG_SPLIT_BF16X3) ? 1 : 0;
+    if (o.split != RBG_SPLIT_BF16X3 && o.split != RBG_SPLIT_F16X3 && o.split != RBG_SPLIT_TF32X2) {
+        err = "unknown split";
+        return RBG_ERR_ARG;
+    }
+    // split kind of the kernels: 0 FP16x3, 1 BF16x3, 2 TF32 with one compensation term
+    const int sk = split_kind(o.split);
+    const bool tf32 = sk == 2;
     const int optin = (int)prop.sharedMemPerBlockOptin;
     int tcols = 32;
     while (tcols < std::min(Np, kPassCols)) tcols <<= 1;
     // variance groups per GEMM launch: as many as fit two pipeline stages
     int ng_cap = kMaxG;
     if (backend == RBG_CONV_GEMM) {
-        while (ng_cap > 1 && smem_layout(Np, 2, ng_cap, 0, ns).total > optin) --ng_cap;
-        if (smem_layout(Np, 2, ng_cap, 0, ns).total > optin) {
+        while (ng_cap > 1 && smem_layout(Np, 2, ng_cap, 0, ns, tf32).total > optin) --ng_cap;
+        if (smem_layout(Np, 2, ng_cap, 0, ns, tf32).total > optin) {
             err = "mixed kernel shared memory does not fit";
             return RBG_ERR_UNSUPPORTED;
         }
@@ -1412,7 +1546,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             }
             if (backend == RBG_CONV_GEMM) {
                 r.off_strip = off;
-                off += (size_t)strip_bytes(Np);
+                off += (size_t)strip_bytes_sk(Np, tf32);
                 off = (off + 255) / 256 * 256;
             } else {
                 A.logL = fft_log2_len(N);
@@ -1450,13 +1584,13 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     // which set the kernel's pace, need.
     job.fused = RBG_FUSE_PAYOFFS && (backend == RBG_CONV_GEMM) && !mc;
     for (const MixedLaunch& r : job.launches)
-        if (r.args.n_o > kMixedMaxFused || smem_layout(Np, 2, r.args.n_g, r.args.n_o).total > optin)
+        if (r.args.n_o > kMixedMaxFused || smem_layout(Np, 2, r.args.n_g, r.args.n_o, 2, tf32).total > optin)
             job.fused = false;
     for (MixedLaunch& r : job.launches) {
         MixedArgs& A = r.args;
         const int no = job.fused ? A.n_o : 0;
-        A.stages = (smem_layout(Np, 3, A.n_g, no, ns).total <= optin) ? 3 : 2;
-        if (backend == RBG_CONV_GEMM && smem_layout(Np, A.stages, A.n_g, no, ns).total > optin) {
+        A.stages = (smem_layout(Np, 3, A.n_g, no, ns, tf32).total <= optin) ? 3 : 2;
+        if (backend == RBG_CONV_GEMM && smem_layout(Np, A.stages, A.n_g, no, ns, tf32).total > optin) {
             err = "mixed kernel shared memory does not fit";
             return RBG_ERR_UNSUPPORTED;
         }
@@ -1473,7 +1607,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         const MixedArgs& A = r.args;
         const int vol = plan.vgs[A.g0].vol;
         if (backend == RBG_CONV_GEMM)
-            build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, bf16, ws.data() + r.off_strip);
+            build_strip(plan.gamma.data() + (size_t)vol * N, N, Np, sk, ws.data() + r.off_strip);
         else
             fft_tables(plan.gamma.data() + (size_t)vol * N, N, A.logL, (float*)(ws.data() + r.off_spec),
                        (float*)(ws.data() + job.off_tw));
@@ -1528,14 +1662,22 @@ int mixed_part_rows(const MixedJob& job, int64_t B)
 
 // The path kernel of a (split, estimator, normal source) for pass mode pm.
 // Sobol' normals run up to two passes (N <= 1024; mixed_launch rejects more).
-template <int BF16, bool MC, int SRC>
-static void (*gemm_kernel(int pm))(MixedArgs)
+template <int SK, bool MC, int SRC>
+static void (*gemm_kernel_pm(int pm))(MixedArgs)
 {
     if constexpr (SRC == 1)
-        return pm == 0 ? k_mixed_gemm<BF16, 0, MC, SRC> : k_mixed_gemm<BF16, 1, MC, SRC>;
+        return pm == 0 ? k_mixed_gemm<SK, 0, MC, SRC> : k_mixed_gemm<SK, 1, MC, SRC>;
     else
-        return pm == 0 ? k_mixed_gemm<BF16, 0, MC, SRC>
-                       : (pm == 1 ? k_mixed_gemm<BF16, 1, MC, SRC> : k_mixed_gemm<BF16, 2, MC, SRC>);
+        return pm == 0 ? k_mixed_gemm<SK, 0, MC, SRC>
+                       : (pm == 1 ? k_mixed_gemm<SK, 1, MC, SRC> : k_mixed_gemm<SK, 2, MC, SRC>);
+}
+
+// The path kernel of a (split kind, estimator, normal source) for pass mode pm.
+template <bool MC, int SRC>
+static void (*gemm_kernel(int sk, int pm))(MixedArgs)
+{
+    return sk == 0 ? gemm_kernel_pm<0, MC, SRC>(pm)
+                   : (sk == 1 ? gemm_kernel_pm<1, MC, SRC>(pm) : gemm_kernel_pm<2, MC, SRC>(pm));
 }
 
 int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, int64_t B, void* ivb,
@@ -1578,27 +1720,22 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         A.seed = seed;
         A.path0 = path0;
         A.B = B;
-        const int smem = smem_layout(A.Np, A.stages, A.n_g, A.n_o, job.mc ? 3 : 2).total;
+        const int smem =
+            smem_layout(A.Np, A.stages, A.n_g, A.n_o, job.mc ? 3 : 2, job.split == RBG_SPLIT_TF32X2).total;
         const int64_t ntiles = (B + kTileM - 1) / kTileM;
         const int grid = (int)std::min<int64_t>(ntiles, job.sms);
         cudaError_t e;
         if (job.backend == RBG_CONV_FFT) {
             e = launch_mixed_fft(A, job.sms, st);
         } else {
-            const int pm = pass_mode(A.Np);
+            const int pm = pass_mode(A.Np), sk = split_kind(job.split);
             void (*kern)(MixedArgs);
-            if (job.sob && job.split == RBG_SPLIT_BF16X3)
-                kern = gemm_kernel<1, false, 1>(pm);
-            else if (job.sob)
-                kern = gemm_kernel<0, false, 1>(pm);
-            else if (ext && job.split == RBG_SPLIT_BF16X3)
-                kern = job.mc ? gemm_kernel<1, true, 2>(pm) : gemm_kernel<1, false, 2>(pm);
+            if (job.sob)
+                kern = gemm_kernel<false, 1>(sk, pm);
             else if (ext)
-                kern = job.mc ? gemm_kernel<0, true, 2>(pm) : gemm_kernel<0, false, 2>(pm);
-            else if (job.split == RBG_SPLIT_BF16X3)
-                kern = job.mc ? gemm_kernel<1, true, 0>(pm) : gemm_kernel<1, false, 0>(pm);
+                kern = job.mc ? gemm_kernel<true, 2>(sk, pm) : gemm_kernel<false, 2>(sk, pm);
             else
-                kern = job.mc ? gemm_kernel<0, true, 0>(pm) : gemm_kernel<0, false, 0>(pm);
+                kern = job.mc ? gemm_kernel<true, 0>(sk, pm) : gemm_kernel<false, 0>(sk, pm);
             e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e == cudaSuccess) kern<<<grid, kThreads, smem, st>>>(A);
         }

@@ -121,3 +121,15 @@ def test_computeIV_tensor_mixed_env(R, monkeypatch):
     res = R.computeIV_tensor(xi, H, eta, rho, T, K, 128, 1 << 14, [5])
     p, s, _ = R.price_mc(xi, H, eta, rho, T, K, 128, 1 << 14, seed=5, precision=R.MIXED)
     np.testing.assert_array_equal(res.price, p)
+
+
+def test_mc_mixed_tf32_split_vs_fp64(R):
+    """Plain MC on the TF32 split (normals rounded to TF32, Gamma in TF32 hi + lo)."""
+    xi, H, eta, rho = 0.05, [0.1], [1.5], [-0.7]
+    T, K = [1.0, 1.0], [0.9, 1.2]
+    N, M = 512, 1 << 14
+    mp, ms, _ = R.price_mc(xi, H, eta, rho, T, K, N, M, seed=6, precision=R.MIXED, split=R.SPLIT_TF32X2)
+    fp, fs, _ = R.price_mc(xi, H, eta, rho, T, K, N, M, seed=6, normals=R.NORMALS_F32)
+    err = np.abs(mp - fp)
+    assert np.all(err <= 1e-4 * fp)
+    assert np.all(err < 0.2 * fs)

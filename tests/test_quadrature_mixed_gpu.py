@@ -105,3 +105,16 @@ def test_mixed_quadrature_device_buffers(R, shift):
                  precision=R.MIXED, out_ptr=out.data_ptr())
     torch.cuda.synchronize()
     np.testing.assert_array_equal(out.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("N", [512, 1500])
+def test_mixed_quadrature_tf32_split(R, N):
+    """Caller normals through the TF32 split (one and three TMEM passes)."""
+    xi, H, eta, rho = 0.04, [0.1, 0.3], [1.5, 2.5], [-0.7, -0.5]
+    T, K = [0.5, 2.0], [0.9, 1.2]
+    Z = R.generate_normals(8, 3000, N)
+    p64 = R.payoffs_rt(xi, H, eta, rho, T, K, Z)
+    p32 = R.payoffs_rt(xi, H, eta, rho, T, K, Z, precision=R.MIXED, split=R.SPLIT_TF32X2)
+    # per path the normals carry TF32's rounding (<= 2^-11 relative each) into X, which v = xi exp(eta X)
+    # amplifies by eta (2.5 here): a few 1e-3 on the worst paths; the means stay within MEAN_TOL
+    check(p32, p64, 5e-3)
