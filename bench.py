@@ -587,7 +587,7 @@ def serve_stream(args, local: int) -> dict:
     lat = np.zeros((len(reqs), 3))
     n0 = R.launch_count()
     with ClockSampler(local) as clk:
-        with R.Server(use_graphs=0 if args.no_graphs else 1) as srv:
+        with R.Server(use_graphs=0 if args.no_graphs else 1, batch_wait_us=args.batch_wait_us) as srv:
             tickets = [None] * len(reqs)
             ready = threading.Semaphore(0)
 
@@ -638,6 +638,7 @@ def serve_stream(args, local: int) -> dict:
                 "note": "one request at a time, no queueing: latency is service time only"}
     return {
         "workload": "serving-poisson", "requests": len(reqs), "rate_per_s": args.rate, "graphs": not args.no_graphs,
+        "batch_wait_us": args.batch_wait_us,
         "p50_ms": float(np.percentile(total, 50)), "p99_ms": float(np.percentile(total, 99)),
         "max_ms": float(np.max(total)), "mean_ms": float(np.mean(total)),
         "queue_p99_ms": float(np.percentile(lat[:, 0], 99)), "service_p99_ms": float(np.percentile(lat[:, 1], 99)),
@@ -695,6 +696,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serving: Poisson arrival rate per second")
     ap.add_argument("--fp64-sample", type=int, default=20, help="serving: FP64 one-at-a-time sample size")
     ap.add_argument("--no-graphs", action="store_true", help="serving: launch without CUDA graphs")
+    ap.add_argument("--batch-wait-us", type=float, default=0.0,
+                    help="serving: batching window of the shared launches (0: launch what is pending at once)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-serving", action="store_true",
                     help="headline workload: leave out the serving replay that the default line carries")

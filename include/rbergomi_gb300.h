@@ -357,6 +357,16 @@ typedef struct rbg_server_config {
     int table_cache_entries;         /* device-resident Volterra tables kept */
     int use_graphs;                  /* launch each request as a CUDA graph */
     int device;                      /* CUDA device, -1 = current */
+    /* Shared launches: requests one one-pass launch can price (N <= 512, at
+     * most max_batch_paths paths, one distinct H) are gathered, all that are
+     * pending when a batch slot frees up, into one job-table launch of the
+     * path, payoff, merge and finalize kernels, replayed as one CUDA graph per
+     * batch slot.  0 batch slots: every request alone on its own slot. */
+    int batch_slots;                 /* shared launches in flight at once */
+    int max_batch_jobs;              /* requests per shared launch (1..64) */
+    double batch_path_steps;         /* path-steps per shared launch (a request larger than this still runs, alone) */
+    double batch_wait_us;            /* a batch slot waits up to this long after the oldest pending request's
+                                        submit for more requests (fewer than max_batch_jobs pending); 0: none */
 } rbg_server_config;
 
 typedef struct rbg_server_stats {
@@ -365,6 +375,7 @@ typedef struct rbg_server_stats {
     uint64_t graph_instantiations, graph_updates; /* executable graphs built / updated in place */
     uint64_t max_launch_us;                       /* longest admission-to-launched time on the scheduler */
     uint64_t pin_growths;                         /* pinned result buffers regrown (a device-wide wait each) */
+    uint64_t batches, batched_requests;           /* shared launches, and the requests they priced */
 } rbg_server_stats;
 
 void rbg_server_default_config(rbg_server_config* cfg);

@@ -530,13 +530,16 @@ def debug_mixed_profile(xi, H, eta, rho, T, K, N, M, **opts):
 class RbgServerConfig(C.Structure):
     _fields_ = [("slots", C.c_int), ("high_priority_slots", C.c_int), ("hbm_budget", C.c_uint64),
                 ("max_batch_paths", C.c_int64), ("small_request_path_steps", C.c_double),
-                ("table_cache_entries", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int)]
+                ("table_cache_entries", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
+                ("batch_slots", C.c_int), ("max_batch_jobs", C.c_int), ("batch_path_steps", C.c_double),
+                ("batch_wait_us", C.c_double)]
 
 
 class RbgServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("completed", "failed", "pending", "in_flight", "hbm_in_use",
                                           "table_cache_hits", "table_cache_misses", "graph_launches",
-                                          "graph_instantiations", "graph_updates", "max_launch_us", "pin_growths")]
+                                          "graph_instantiations", "graph_updates", "max_launch_us", "pin_growths",
+                                          "batches", "batched_requests")]
 
 
 def _server_lib():

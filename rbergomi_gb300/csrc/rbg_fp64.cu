@@ -563,11 +563,12 @@ void launch_payoff_sums(const Fp64Tables& t, const double* ivb, int64_t B, int64
 // acc[i * 4 + {0..3}] += the batch's chunk sums.  One block per output:
 // strided Neumaier sums per thread, then a fixed-shape tree, so the result
 // does not depend on scheduling.
-__global__ void __launch_bounds__(256) k_accumulate(const double* __restrict__ part, int nchunks, int n_out,
-                                                    double* __restrict__ acc)
+// Output i of a fixed-order merge of chunk sums into acc (fresh: acc holds
+// zeros, read as such -- the job-table launches skip the clearing memset).
+// Shared by the per-request and job-table kernels.
+__device__ __forceinline__ void accumulate_block(const double* __restrict__ part, int nchunks, int n_out,
+                                                 double* __restrict__ acc, int i, bool fresh, double (*sh)[256])
 {
-    __shared__ double sh[4][256];
-    const int i = blockIdx.x;
     double S = 0, C = 0, S2 = 0, C2 = 0;
     for (int c = threadIdx.x; c < nchunks; c += blockDim.x) {
         const double* p = part + ((size_t)c * n_out + i) * 4;
@@ -592,13 +593,40 @@ __global__ void __launch_bounds__(256) k_accumulate(const double* __restrict__ p
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        double a = acc[i * 4 + 0], ac = acc[i * 4 + 1], b = acc[i * 4 + 2], bc = acc[i * 4 + 3];
+        double a = 0, ac = 0, b = 0, bc = 0;
+        if (!fresh) { a = acc[i * 4 + 0]; ac = acc[i * 4 + 1]; b = acc[i * 4 + 2]; bc = acc[i * 4 + 3]; }
         neumaier_add(a, ac, sh[0][0]);
         neumaier_add(a, ac, sh[1][0]);
         neumaier_add(b, bc, sh[2][0]);
         neumaier_add(b, bc, sh[3][0]);
         acc[i * 4 + 0] = a; acc[i * 4 + 1] = ac; acc[i * 4 + 2] = b; acc[i * 4 + 3] = bc;
     }
+}
+
+__global__ void __launch_bounds__(256) k_accumulate(const double* __restrict__ part, int nchunks, int n_out,
+                                                    double* __restrict__ acc)
+{
+    __shared__ double sh[4][256];
+    accumulate_block(part, nchunks, n_out, acc, blockIdx.x, false, sh);
+}
+
+// Job-table form: block b merges output b - jobs[k].block0 of job k.
+__global__ void __launch_bounds__(256) k_accumulate_jobs(const AccJob* __restrict__ jobs, int n_jobs)
+{
+    __shared__ double sh[4][256];
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].block0 <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    const AccJob& J = jobs[lo];
+    accumulate_block(J.part, J.nchunks, J.n_out, J.acc, (int)((int64_t)blockIdx.x - J.block0), true, sh);
+}
+
+void launch_accumulate_jobs(const AccJob* jobs, int n_jobs, int64_t blocks, void* stream)
+{
+    k_accumulate_jobs<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(jobs, n_jobs);
+    count_launch();
 }
 
 void launch_accumulate(const double* part, int nchunks, int n_out, double* acc, void* stream)
@@ -682,11 +710,12 @@ __device__ double implied_vol_warp(double price, double K, double T)
 
 // res: [0,n) price, [n,2n) stat, [2n,3n) iv, [3n,4n) sum, [4n,5n) sum2.
 // One warp per output.
-__global__ void k_finalize(const double* __restrict__ acc, int n_out, int64_t M, const OutDev* __restrict__ outs,
-                           const double* __restrict__ Tv, int compute_iv, double* __restrict__ res)
+// Output i (one warp) of the price / stat / implied vol; shared by the
+// per-request and job-table kernels.
+__device__ __forceinline__ void finalize_warp(const double* __restrict__ acc, int n_out, int64_t M,
+                                              const OutDev* __restrict__ outs, const double* __restrict__ Tv,
+                                              int compute_iv, double* __restrict__ res, int i)
 {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= n_out) return;  // whole warps leave together
     const double S = acc[i * 4 + 0] + acc[i * 4 + 1];
     const double S2 = acc[i * 4 + 2] + acc[i * 4 + 3];
     // rBergLib/rBergomiMT.cpp:404-409
@@ -701,6 +730,33 @@ __global__ void k_finalize(const double* __restrict__ acc, int n_out, int64_t M,
         res[3 * n_out + i] = S;
         res[4 * n_out + i] = S2;
     }
+}
+
+__global__ void k_finalize(const double* __restrict__ acc, int n_out, int64_t M, const OutDev* __restrict__ outs,
+                           const double* __restrict__ Tv, int compute_iv, double* __restrict__ res)
+{
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n_out) return;  // whole warps leave together
+    finalize_warp(acc, n_out, M, outs, Tv, compute_iv, res, i);
+}
+
+// Job-table form: one warp (block) per output, block b finalizes output
+// b - jobs[k].block0 of job k.
+__global__ void k_finalize_jobs(const FinJob* __restrict__ jobs, int n_jobs)
+{
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].block0 <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    const FinJob& J = jobs[lo];
+    finalize_warp(J.acc, J.n_out, J.M, J.outs, J.Tv, J.compute_iv, J.res, (int)((int64_t)blockIdx.x - J.block0));
+}
+
+void launch_finalize_jobs(const FinJob* jobs, int n_jobs, int64_t blocks, void* stream)
+{
+    k_finalize_jobs<<<(unsigned)blocks, 32, 0, (cudaStream_t)stream>>>(jobs, n_jobs);
+    count_launch();
 }
 
 void launch_finalize(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,

@@ -151,6 +151,34 @@ void launch_payoff_store(const Fp64Tables& t, const double* ivb, int64_t B, int6
                          void* stream, const double* ivp = nullptr);
 void launch_implied_vol(int n, const double* price, const double* K, const double* T, double* iv, void* stream);
 
+// ---- job-table forms of the payoff, merge and finalize kernels ----------
+// (the serving loop's shared launches: one launch serves many requests; each
+// job's arithmetic is the per-request kernels' own, block for block)
+// Block b of a launch belongs to the last job whose block0 <= b.
+struct PayoffJob {      // FP32 RT payoff sums, nchunks x ceil(n_out / 8) blocks
+    const OutDev* outs;
+    const float2* ivb;  // [group][B] (Ivdt, IsvdW)
+    double* part;       // [chunk][n_out][4]
+    int64_t B, block0;
+    int n_out, G, nchunks, pad;
+};
+struct AccJob {  // fixed-order merge of the chunk sums into acc (written, not added to), n_out blocks
+    const double* part;
+    double* acc;
+    int64_t block0;
+    int nchunks, n_out;
+};
+struct FinJob {  // price, stat, implied vol, n_out blocks of one warp
+    const double* acc;
+    const OutDev* outs;
+    const double* Tv;
+    double* res;
+    int64_t M, block0;
+    int n_out, compute_iv;
+};
+void launch_accumulate_jobs(const AccJob* jobs, int n_jobs, int64_t blocks, void* stream);
+void launch_finalize_jobs(const FinJob* jobs, int n_jobs, int64_t blocks, void* stream);
+
 // Kernel-launch counter shared by all launchers.
 void count_launch(int n = 1);
 

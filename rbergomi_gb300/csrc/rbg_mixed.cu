@@ -53,6 +53,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "rbg_device.cuh"
 #include "rbg_mixed.hpp"
@@ -1196,6 +1198,310 @@ done:
     }
 }
 
+// --------------------------------------------- job-table (shared) launches
+// The serving loop's shared launch: one path kernel over the tiles of many
+// requests ("jobs"), each with its own parameters, Philox seed, path range,
+// strip and compensator table (a.jobs[j], device memory), its tiles
+// [job_tile0[j], job_tile0[j + 1]) of the launch.  One TMEM pass (N <= 512),
+// the RT estimator, Philox normals, (Ivdt, IsvdW) per path out; payoffs in
+// the job-table payoff kernel.  Each CTA takes a contiguous range of tiles,
+// so it meets a new job rarely: then the MMA issuer reloads the strip once
+// every MMA issued on the old one has completed, and the epilogue warps the
+// compensator table after the barrier that ended the last tile.  The
+// launch's own arguments give the shared-memory layout (largest Np and group
+// count of its jobs), the error word and the TMEM allocation.
+// Per path it performs k_mixed_gemm's operations in the same order, so a
+// request's results are the same alone and in any mix.  It is a kernel of
+// its own, not a template flag of k_mixed_gemm: the per-tile job lookup
+// folded into that kernel made its ordinary launches 10% slower (measured).
+template <int SK>
+__global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm_jobs(const __grid_constant__ MixedArgs a)
+{
+    constexpr int NS = 2;
+    constexpr int kStageFB = stage_f_bytes(NS);
+    constexpr bool T32 = SK == 2;
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g, 0, NS, T32);
+    unsigned char* strip = base + L.strip;
+    float* acc_s = (float*)(base + L.acc);
+    float* beta_s = (float*)(base + L.beta);
+    uint64_t* bars = (uint64_t*)(base + L.bars);
+    const int S = a.stages;
+    uint64_t* full = bars;       // [S]
+    uint64_t* empty = bars + 3;  // [S]
+    uint64_t* accf = bars + 6;   // [S]
+    uint64_t* tmem_empty = bars + 9;
+    uint64_t* strip_bar = bars + 10;
+    uint64_t* final_bar = bars + 11;
+    uint32_t* tmem_holder = (uint32_t*)(bars + 12);
+    uint64_t* strip_free = bars + 13;  // every MMA issued on the old strip has completed
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // this CTA's tiles [t_first, t_last), starting in job jb
+    const int64_t T = a.job_tile0[a.n_jobs];
+    const int64_t t_first = T * blockIdx.x / gridDim.x, t_last = T * (blockIdx.x + 1) / gridDim.x;
+    int jb = 0;
+    while (jb + 1 < a.n_jobs && t_first >= a.job_tile0[jb + 1]) ++jb;
+    const MixedArgs& J0 = a.jobs[jb];
+    auto strip_bytes_of = [](int Np) { return (uint32_t)(T32 ? strip_smem_bytes_t32(Np) : strip_smem_bytes(Np)); };
+
+    if (threadIdx.x == kMmaWarp * 32) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(smem_u32(full + s), kProdWarps);
+            mbar_init(smem_u32(empty + s), 1 + kEpiWarps);
+            mbar_init(smem_u32(accf + s), 1);
+        }
+        mbar_init(smem_u32(tmem_empty), kEpiWarps);
+        mbar_init(smem_u32(strip_bar), 1);
+        mbar_init(smem_u32(final_bar), 1);
+        mbar_init(smem_u32(strip_free), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        const uint32_t nb = strip_bytes_of(J0.Np);
+        mbar_expect_tx(smem_u32(strip_bar), nb);
+        bulk_g2s(smem_u32(strip), J0.strip, nb, smem_u32(strip_bar));
+    }
+    if (warp == kMmaWarp) {
+        __syncwarp();
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                     "r"(a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    for (int i = threadIdx.x; i < J0.n_g * J0.Np; i += blockDim.x) beta_s[i] = J0.beta[i];
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    if (warp < kProdWarps) {
+        // ------------------------------------------------------- producers
+        const int p = threadIdx.x & (kTileM - 1);
+        const int h = threadIdx.x >> 7;
+        PhiloxKeys keys = philox_keys(J0.seed);
+        int s = 0, j = jb;
+        uint32_t ph = 0;
+        for (int64_t it = t_first; it < t_last; ++it) {
+            const int jp = j;
+            while (it >= a.job_tile0[j + 1]) ++j;
+            if (j != jp) keys = philox_keys(a.jobs[j].seed);
+            const MixedArgs& J = a.jobs[j];
+            const int64_t m = (it - a.job_tile0[j]) * kTileM + p;
+            const bool valid = m < J.B;
+            const uint64_t gpath = (uint64_t)(J.path0 + m);
+            for (int c = 0; c < J.nc; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+                if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1)) goto done;
+                unsigned char* st = base + L.a0 + s * kStageA;
+                float* w1s = (float*)(base + L.f0 + s * kStageFB);
+                produce_chunk<SK, false, false>(J, keys, gpath, valid, m, p, h, c, false, st, w1s);
+                fence_proxy_async();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(full + s));
+            }
+        }
+    } else if (warp < kMmaWarp) {
+        // -------------------------------------------------------- epilogue
+        const int ew = warp - kEpiWarp0;
+        const int wg = ew >> 2;
+        const int quad = warp & 3;
+        const int p = quad * 32 + lane;
+        const uint32_t tlane = tmem + ((uint32_t)(quad * 32) << 16);
+        float* my_acc = acc_s + (size_t)wg * a.n_g * NS * kTileM;
+        float* w10_s = acc_s + (size_t)2 * a.n_g * NS * kTileM;
+        int s = 0, j = jb;
+        uint32_t ph = 0;
+        for (int64_t it = t_first; it < t_last; ++it) {
+            const int jp = j;
+            while (it >= a.job_tile0[j + 1]) ++j;
+            const MixedArgs& J = a.jobs[j];
+            if (j != jp) {
+                // every epilogue warp finished the last tile at the barrier that ended it
+                for (int i = threadIdx.x - kEpiWarp0 * 32; i < J.n_g * J.Np; i += kEpiWarps * 32) beta_s[i] = J.beta[i];
+                asm volatile("bar.sync 1, %0;" ::"r"(kEpiWarps * 32) : "memory");
+            }
+            const int Np = J.Np, nc = J.nc;
+            const int64_t m = (it - a.job_tile0[j]) * kTileM + p;
+            const bool valid = m < J.B;
+            for (int g = 0; g < J.n_g; ++g)
+#pragma unroll
+                for (int t = 0; t < NS; ++t) my_acc[(NS * g + t) * kTileM + p] = 0.f;
+            for (int c = 0; c < nc; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+                if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7)) goto done;
+                const bool pass_end = c == nc - 1;
+                const bool has_next = c + 1 < nc;
+                const int sn = (s + 1 == S) ? 0 : s + 1;
+                if ((kEpiWGs == 1 || wg == 1) && has_next &&
+                    !mbar_wait_warp(smem_u32(full + sn), sn == 0 ? ph ^ 1u : ph, a.err, 8))
+                    goto done;
+                if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2)) goto done;
+                tc_fence_after();
+                const float* w1s = (const float*)(base + L.f0 + s * kStageFB);
+                const float* w1ps = w1s + kFW1p;
+#pragma unroll 1
+                for (int hh = wg; hh < 2; hh += kEpiWGs) {
+                    const int j0 = 16 * hh;
+                    float w1v[16], w1pv[16];
+#pragma unroll
+                    for (int jj = 0; jj < 16; jj += 4) {
+                        const int at = ftile_at(p, j0 + jj);
+                        const float4 u = *(const float4*)(w1s + at), v = *(const float4*)(w1ps + at);
+                        w1v[jj] = u.x; w1v[jj + 1] = u.y; w1v[jj + 2] = u.z; w1v[jj + 3] = u.w;
+                        w1pv[jj] = v.x; w1pv[jj + 1] = v.y; w1pv[jj + 2] = v.z; w1pv[jj + 3] = v.w;
+                    }
+                    const float* nexts = (const float*)(base + L.f0 + sn * kStageFB);
+                    const float w_after = (hh == 0) ? w1s[ftile_at(p, 16)] : (!has_next ? 0.f : nexts[ftile_at(p, 0)]);
+                    float x[16];
+                    tmem_ld16(tlane + (uint32_t)(kChunk * c + j0), x);
+                    if (pass_end && hh + kEpiWGs >= 2) {
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(smem_u32(tmem_empty));
+                    }
+                    float wn[16];
+#pragma unroll
+                    for (int jj = 0; jj < 16; ++jj) {
+                        const float w1 = w1v[jj];
+                        x[jj] = x[jj] + J.a1 * w1 + J.a2 * w1pv[jj];
+                        if (jj > 0) wn[jj - 1] = w1;
+                        if (jj == 0 && j0 == 0 && c == 0) w10_s[p] = w1;
+                    }
+                    wn[15] = w_after;
+                    for (int g = 0; g < J.n_g; ++g) {
+                        const float ah = J.alpha[g];
+                        const float* btp = beta_s + g * Np + kChunk * c + j0;
+                        float bt[16];
+#pragma unroll
+                        for (int jj = 0; jj < 16; jj += 4) {
+                            const float4 u = *(const float4*)(btp + jj);
+                            bt[jj] = u.x; bt[jj + 1] = u.y; bt[jj + 2] = u.z; bt[jj + 3] = u.w;
+                        }
+                        const int lim = J.nsteps[g] - 1 - kChunk * c - j0;
+                        float sv = 0.f, swv = 0.f;
+                        if (lim >= 16) {
+#pragma unroll
+                            for (int jj = 0; jj < 16; ++jj) {
+                                const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
+                                sv = fmaf(su, su, sv);
+                                swv = fmaf(su, wn[jj], swv);
+                            }
+                        } else {
+#pragma unroll
+                            for (int jj = 0; jj < 16; ++jj) {
+                                if (jj < lim) {
+                                    const float su = ex2_approx(fmaf(ah, x[jj], -bt[jj]));
+                                    sv = fmaf(su, su, sv);
+                                    swv = fmaf(su, wn[jj], swv);
+                                }
+                            }
+                        }
+                        my_acc[(NS * g) * kTileM + p] += sv;
+                        my_acc[(NS * g + 1) * kTileM + p] += swv;
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(empty + s));
+            }
+            asm volatile("bar.sync 1, %0;" ::"r"(kEpiWarps * 32) : "memory");
+            if (wg == 0 && valid) {
+                const float w1_0 = w10_s[p];
+                for (int g = 0; g < J.n_g; ++g) {
+                    float sv = acc_s[(NS * g) * kTileM + p], sw2 = acc_s[(NS * g + 1) * kTileM + p];
+                    if (kEpiWGs == 2) {
+                        sv += acc_s[((size_t)a.n_g * NS + NS * g) * kTileM + p];
+                        sw2 += acc_s[((size_t)a.n_g * NS + NS * g + 1) * kTileM + p];
+                    }
+                    J.ivb[(size_t)(J.g0 + g) * J.B + m] =
+                        make_float2(J.dt[g] * (J.xi + sv), J.sdt[g] * fmaf(J.sqrt_xi, w1_0, sw2));
+                }
+            }
+            asm volatile("bar.sync 1, %0;" ::"r"(kEpiWarps * 32) : "memory");
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------------ MMA issuer
+        const uint32_t strip_hi = smem_u32(strip);
+        uint32_t strip_lo = strip_hi + strip_bytes_of(J0.Np) / 2;
+        if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3)) {
+            int64_t pass = 0;
+            int s = 0, j = jb;
+            uint32_t ph = 0, strip_loads = 1, strip_frees = 0;
+            bool ok = true;
+            for (int64_t it = t_first; it < t_last && ok; ++it) {
+                const int jp = j;
+                while (it >= a.job_tile0[j + 1]) ++j;
+                const MixedArgs& J = a.jobs[j];
+                if (j != jp) {
+                    // the new job's strip, once every MMA issued on the old one has completed
+                    umma_commit(smem_u32(strip_free));
+                    if (!mbar_wait(smem_u32(strip_free), strip_frees & 1u, a.err, 9)) break;
+                    ++strip_frees;
+                    const uint32_t nb = strip_bytes_of(J.Np);
+                    mbar_expect_tx(smem_u32(strip_bar), nb);
+                    bulk_g2s(strip_hi, J.strip, nb, smem_u32(strip_bar));
+                    if (!mbar_wait(smem_u32(strip_bar), strip_loads & 1u, a.err, 3)) break;
+                    ++strip_loads;
+                    strip_lo = strip_hi + nb / 2;
+                }
+                const int hi = kChunk * J.nc;
+                for (int c = 0; c < J.nc; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+                    const bool first = c == 0;
+                    if (first) {
+                        if (pass > 0 &&
+                            !mbar_wait(smem_u32(tmem_empty), (uint32_t)((pass - 1) & 1), a.err, 4)) {
+                            ok = false;
+                            break;
+                        }
+                        ++pass;
+                        tc_fence_after();
+                    }
+                    if (!mbar_wait(smem_u32(full + s), ph, a.err, 5)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
+                    const uint32_t alo = ahi + kTileBytes;
+                    for (int col0 = kChunk * c; col0 < hi; col0 += 256) {
+                        const int n = (hi - col0 < 256) ? (hi - col0) : 256;
+                        const uint32_t jrow = (uint32_t)(col0 - kChunk * c);
+                        const uint32_t d = tmem + (uint32_t)col0;
+                        if constexpr (T32) {
+                            const uint32_t id = idesc_tf32(n);
+#pragma unroll
+                            for (int ks = 0; ks < kChunk / kStripKT; ++ks) {
+                                const uint64_t da = sdesc_sw128(ahi + 32 * ks);
+                                const uint32_t boff = (jrow + (uint32_t)(kStripKT * (3 - ks))) * 32u;
+                                umma_tf32(d, da, sdesc_sw32(strip_hi + boff), id, (first && ks == 0) ? 0u : 1u);
+                                umma_tf32(d, da, sdesc_sw32(strip_lo + boff), id, 1u);
+                            }
+                        } else {
+                            const uint32_t id = idesc_f16(n, SK);
+#pragma unroll
+                            for (int ks = 0; ks < 2; ++ks) {
+                                const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
+                                const uint64_t dbh = sdesc_sw64(strip_hi + jrow * 64 + 32 * ks);
+                                const uint64_t dbl = sdesc_sw64(strip_lo + jrow * 64 + 32 * ks);
+                                umma_f16(d, dah, dbh, id, (first && ks == 0) ? 0u : 1u);
+                                umma_f16(d, dah, dbl, id, 1u);
+                                umma_f16(d, dal, dbh, id, 1u);
+                            }
+                        }
+                    }
+                    umma_commit(smem_u32(empty + s));
+                    umma_commit(smem_u32(accf + s));
+                }
+            }
+        }
+        umma_commit(smem_u32(final_bar));
+        mbar_wait(smem_u32(final_bar), 0, a.err, 6);
+    }
+done:
+    tc_fence_before();
+    __syncthreads();
+    if (warp == kMmaWarp) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols)
+                     : "memory");
+    }
+}
+
 // ----------------------------------------------- FP32 payoffs, FP64 sums
 constexpr int kOPB32 = 8;
 
@@ -1207,14 +1513,15 @@ __device__ __forceinline__ float mc_payoff_f32(float Ivdt, float IsvdW, float Is
     return fmaxf(ex2_approx(1.4426950408889634f * lnS) - K, 0.0f);
 }
 
+// One block of the FP32 payoff sums: chunk c (paths [256 G c, 256 G (c + 1)))
+// and outputs [o0, o0 + 8).  Shared by the per-request and job-table kernels,
+// so a request's sums do not depend on which of them ran.
 template <bool MC>
-__global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restrict__ outs, int n_out,
-                                                         const float2* __restrict__ ivb, int64_t B, int G,
-                                                         double* __restrict__ part, const float* __restrict__ ivq)
+__device__ __forceinline__ void payoff_sums_block(const OutDev* __restrict__ outs, int n_out,
+                                                  const float2* __restrict__ ivb, int64_t B, int G,
+                                                  double* __restrict__ part, const float* __restrict__ ivq, int c,
+                                                  int o0, double (*red)[kOPB32][2])
 {
-    __shared__ double red[8][kOPB32][2];
-    const int c = blockIdx.x;
-    const int o0 = blockIdx.y * kOPB32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float rho[kOPB32], K[kOPB32], lnK[kOPB32];
     int vg[kOPB32];
@@ -1275,12 +1582,44 @@ __global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restric
     }
 }
 
+template <bool MC>
+__global__ void __launch_bounds__(256) k_payoff_sums_f32(const OutDev* __restrict__ outs, int n_out,
+                                                         const float2* __restrict__ ivb, int64_t B, int G,
+                                                         double* __restrict__ part, const float* __restrict__ ivq)
+{
+    __shared__ double red[8][kOPB32][2];
+    payoff_sums_block<MC>(outs, n_out, ivb, B, G, part, ivq, blockIdx.x, blockIdx.y * kOPB32, red);
+}
+
+// Job-table form: block b of the launch is block b - jobs[k].block0 of job k
+// (chunk-major as in the per-request grid: chunk = local % nchunks, output
+// block = local / nchunks).
+__global__ void __launch_bounds__(256) k_payoff_sums_f32_jobs(const PayoffJob* __restrict__ jobs, int n_jobs)
+{
+    __shared__ double red[8][kOPB32][2];
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {  // last job whose first block is <= blockIdx.x
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].block0 <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    const PayoffJob& J = jobs[lo];
+    const int local = (int)((int64_t)blockIdx.x - J.block0);
+    payoff_sums_block<false>(J.outs, J.n_out, J.ivb, J.B, J.G, J.part, nullptr, local % J.nchunks,
+                             (local / J.nchunks) * kOPB32, red);
+}
+
 void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int64_t B, int G, double* part,
                             int nchunks, cudaStream_t st, const float* ivq)
 {
     dim3 grid(nchunks, (n_out + kOPB32 - 1) / kOPB32);
     if (ivq) k_payoff_sums_f32<true><<<grid, 256, 0, st>>>(outs, n_out, (const float2*)ivb, B, G, part, ivq);
     else k_payoff_sums_f32<false><<<grid, 256, 0, st>>>(outs, n_out, (const float2*)ivb, B, G, part, ivq);
+    count_launch();
+}
+
+void launch_payoff_sums_f32_jobs(const PayoffJob* jobs, int n_jobs, int64_t blocks, cudaStream_t st)
+{
+    k_payoff_sums_f32_jobs<<<(unsigned)blocks, 256, 0, st>>>(jobs, n_jobs);
     count_launch();
 }
 
@@ -1436,6 +1775,37 @@ void build_strip(const double* gamma, int N, int Np, int sk, unsigned char* img)
 
 }  // namespace
 
+// Attributes of the current device the planner needs, queried once per
+// device ordinal (cudaGetDeviceProperties costs far more than the rest of a
+// request's planning, and the serving loop plans every request).
+struct DevInfo {
+    int major, sms, optin;
+};
+static bool device_info(DevInfo* out)
+{
+    static std::mutex mu;
+    static std::map<int, DevInfo> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it == cache.end()) {
+        DevInfo d{};
+        if (cudaDeviceGetAttribute(&d.major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&d.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        it = cache.emplace(dev, d).first;
+    }
+    *out = it->second;
+    return true;
+}
+
 void mixed_table_range(const MixedJob& job, int i, size_t* off, size_t* bytes)
 {
     const MixedLaunch& r = job.launches[i];
@@ -1457,15 +1827,12 @@ void mixed_twiddle_range(const MixedJob& job, size_t* off, size_t* bytes)
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
                   int64_t max_batch, bool mc)
 {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceProp prop;
-    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
-        cudaGetLastError();
-        err = "cudaGetDeviceProperties failed";
+    DevInfo dv;
+    if (!device_info(&dv)) {
+        err = "device attribute query failed";
         return RBG_ERR_CUDA;
     }
-    if (prop.major != 10) {
+    if (dv.major != 10) {
         err = "mixed form needs a Blackwell (sm_10x) GPU with tcgen05";
         return RBG_ERR_UNSUPPORTED;
     }
@@ -1493,7 +1860,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     job.n_vol = (int)plan.vols.size();
     job.n_vg = (int)plan.vgs.size();
     job.split = o.split;
-    job.sms = prop.multiProcessorCount;
+    job.sms = dv.sms;
     if (o.split != RBG_SPLIT_BF16X3 && o.split != RBG_SPLIT_F16X3 && o.split != RBG_SPLIT_TF32X2) {
         err = "unknown split";
         return RBG_ERR_ARG;
@@ -1501,7 +1868,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     // split kind of the kernels: 0 FP16x3, 1 BF16x3, 2 TF32 with one compensation term
     const int sk = split_kind(o.split);
     const bool tf32 = sk == 2;
-    const int optin = (int)prop.sharedMemPerBlockOptin;
+    const int optin = dv.optin;
     int tcols = 32;
     while (tcols < std::min(Np, kPassCols)) tcols <<= 1;
     // variance groups per GEMM launch: as many as fit two pipeline stages
@@ -1747,6 +2114,113 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         }
         count_launch();
     }
+    return RBG_OK;
+}
+
+bool mixed_job_batchable(const MixedJob& job)
+{
+    return job.backend == RBG_CONV_GEMM && job.launches.size() == 1 && job.launches[0].args.Np <= kPassCols &&
+           !job.mc && !job.fused && !job.sob;
+}
+
+size_t mixed_jobs_table_bytes(int n) { return sizeof(MixedArgs) * (size_t)n + sizeof(int64_t) * (size_t)(n + 1); }
+
+int mixed_jobs_prepare(const std::vector<MixedJobRef>& jobs, void* table, unsigned int* err, int sms,
+                       std::vector<unsigned char>& host_table, MixedArgs* launch_args, std::string& errmsg)
+{
+    const int n = (int)jobs.size();
+    if (n < 1) {
+        errmsg = "empty job table";
+        return -1;
+    }
+    const int split = jobs[0].job->split;
+    host_table.assign(mixed_jobs_table_bytes(n), 0);
+    MixedArgs* args = (MixedArgs*)host_table.data();
+    int64_t* tile0 = (int64_t*)(host_table.data() + sizeof(MixedArgs) * (size_t)n);
+    int Np_max = 0, ng_max = 1, tcols = 32;
+    tile0[0] = 0;
+    for (int k = 0; k < n; ++k) {
+        const MixedJobRef& r = jobs[k];
+        if (!mixed_job_batchable(*r.job) || r.job->split != split) {
+            errmsg = "job-table launch: every job needs one one-pass RT launch of the same split";
+            return -1;
+        }
+        const MixedLaunch& L = r.job->launches[0];
+        MixedArgs A = L.args;
+        const unsigned char* base = (const unsigned char*)r.ws;
+        const bool over = !r.job->table_dev.empty() && r.job->table_dev[0];
+        A.strip = over ? (const unsigned char*)r.job->table_dev[0] : base + L.off_strip;
+        A.beta = (const float*)(base + L.off_beta);
+        A.ivb = (float2*)r.ivb;
+        A.ivq = nullptr;
+        A.err = err;
+        A.otab = nullptr;
+        A.oidx = nullptr;
+        A.part = nullptr;
+        A.prof = nullptr;
+        A.spec = nullptr;
+        A.tw = nullptr;
+        A.sob = nullptr;
+        A.ext = nullptr;
+        A.dbg_w = nullptr;
+        A.dbg_x = nullptr;
+        A.n_o = 0;
+        A.seed = r.seed;
+        A.path0 = r.path0;
+        A.B = r.B;
+        A.jobs = nullptr;
+        A.job_tile0 = nullptr;
+        A.n_jobs = 0;
+        args[k] = A;
+        tile0[k + 1] = tile0[k] + (r.B + kTileM - 1) / kTileM;
+        Np_max = std::max(Np_max, A.Np);
+        ng_max = std::max(ng_max, A.n_g);
+        tcols = std::max(tcols, A.tmem_cols);
+    }
+    DevInfo dv;
+    if (!device_info(&dv)) {
+        errmsg = "device attribute query failed";
+        return -1;
+    }
+    const int optin = dv.optin;
+    const bool tf32 = split == RBG_SPLIT_TF32X2;
+    MixedArgs LA = args[0];
+    LA.Np = Np_max;
+    LA.nc = Np_max / kChunk;
+    LA.n_g = ng_max;
+    LA.tmem_cols = tcols;
+    LA.stages = smem_layout(Np_max, 3, ng_max, 0, 2, tf32).total <= optin ? 3 : 2;
+    if (smem_layout(Np_max, LA.stages, ng_max, 0, 2, tf32).total > optin) {
+        errmsg = "job-table launch: shared memory does not fit";
+        return -1;
+    }
+    LA.strip = nullptr;
+    LA.beta = nullptr;
+    LA.ivb = nullptr;
+    LA.B = 0;
+    LA.jobs = (const MixedArgs*)table;
+    LA.job_tile0 = (const int64_t*)((const unsigned char*)table + sizeof(MixedArgs) * (size_t)n);
+    LA.n_jobs = n;
+    *launch_args = LA;
+    return (int)std::min<int64_t>(tile0[n], sms);
+}
+
+int mixed_launch_jobs(const MixedArgs& A, int split, int grid, cudaStream_t st, std::string& errmsg)
+{
+    const int sk = split_kind(split);
+    void (*kern)(MixedArgs) = sk == 0 ? k_mixed_gemm_jobs<0> : (sk == 1 ? k_mixed_gemm_jobs<1> : k_mixed_gemm_jobs<2>);
+    const int smem = smem_layout(A.Np, A.stages, A.n_g, 0, 2, sk == 2).total;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) {
+        kern<<<grid, kThreads, smem, st>>>(A);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        errmsg = std::string("job-table kernel launch: ") + cudaGetErrorString(e);
+        return RBG_ERR_CUDA;
+    }
+    count_launch();
     return RBG_OK;
 }
 

@@ -47,6 +47,13 @@ struct MixedArgs {
     // moves them in the kernel's parameter space, which measured 4% slower on
     // the headline kernel (5.54 -> 5.78 ms at N = 512, 2^22 paths).
     int np;  // GEMM backend: TMEM passes per tile (1 .. 8)
+    // Job-table launches (the serving loop's shared launches): this launch's
+    // tiles belong to n_jobs requests; job j's arguments are jobs[j] (device
+    // memory, pointers filled) and its tiles are [job_tile0[j], job_tile0[j + 1])
+    // of the launch.  Unused (null / 0) in ordinary launches.
+    const MixedArgs* jobs;
+    const int64_t* job_tile0;
+    int n_jobs;
 };
 
 struct MixedLaunch {
@@ -105,5 +112,30 @@ void launch_payoff_store_f32(const OutDev* outs, int n_out, const void* ivb, con
                              double* payoff, cudaStream_t st);
 void launch_payoff_sums_f32(const OutDev* outs, int n_out, const void* ivb, int64_t B, int G, double* part,
                             int nchunks, cudaStream_t st, const float* ivq = nullptr);
+void launch_payoff_sums_f32_jobs(const PayoffJob* jobs, int n_jobs, int64_t blocks, cudaStream_t st);
+
+// ---- job-table launches of the path kernel (the serving loop's shared launches)
+// A request whose prepared job is one launch of one TMEM pass (N <= 512) of the
+// RT estimator on Philox normals, payoffs in the separate kernels.
+bool mixed_job_batchable(const MixedJob& job);
+// One job of a shared launch: its prepared job, its workspace image on the
+// device, its paths and its (Ivdt, IsvdW) buffer.
+struct MixedJobRef {
+    const MixedJob* job;
+    const void* ws;
+    uint64_t seed;
+    int64_t path0, B;
+    void* ivb;
+};
+// Device bytes of the job table of n jobs.
+size_t mixed_jobs_table_bytes(int n);
+// Fills the job table for `jobs` (all of one split) into host_table (grown to
+// mixed_jobs_table_bytes) for the device address `table`, and the launch's own
+// arguments into *launch_args; returns the CTA count.  The caller copies the
+// table to the device before the launch.
+int mixed_jobs_prepare(const std::vector<MixedJobRef>& jobs, void* table, unsigned int* err, int sms,
+                       std::vector<unsigned char>& host_table, MixedArgs* launch_args, std::string& errmsg);
+// Launches the path kernel over every job's tiles (grid: mixed_jobs_prepare's CTA count).
+int mixed_launch_jobs(const MixedArgs& launch_args, int split, int grid, cudaStream_t st, std::string& errmsg);
 
 }  // namespace rbg

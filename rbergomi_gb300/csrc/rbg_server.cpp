@@ -70,6 +70,10 @@ struct SBuf {
 // slot that had to grow it would call cudaFreeHost, which waits for the
 // whole device (every request in flight) on the scheduler thread.
 constexpr size_t kPinOutputs = 4096;
+// A shared launch prices at most this many outputs (all its requests' together)
+// and this many requests.
+constexpr int kBatchOutputs = (int)kPinOutputs;
+constexpr int kBatchJobsMax = 64;
 
 struct Req {
     uint64_t id = 0;
@@ -86,7 +90,22 @@ struct Req {
     std::string err;
     bool done = false;
     std::vector<int> cache_keys;  // cache entries pinned while in flight
+    bool batchable = false;       // priced in shared launches (one one-pass launch, RT)
     Clock::time_point t_submit, t_start, t_launched, t_done;
+};
+
+// A shared launch in flight: the requests it prices, where each one's
+// results sit in the pinned buffer, and its buffers (grow-only; results at a
+// fixed capacity so that its CUDA graph keeps one shape).
+struct BatchSlot {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    SBuf in, ivb, part, acc, res;
+    double* pin = nullptr;  // [0] error word, then 5 * kBatchOutputs results
+    std::vector<Req*> reqs;
+    std::vector<size_t> res_off;  // doubles, per request
+    std::vector<unsigned char> host_in, host_tab;
+    cudaGraphExec_t graph = nullptr;
 };
 
 struct Slot {
@@ -115,6 +134,7 @@ struct Server {
     rbg_server_config cfg{};
     int dev = 0;
     std::vector<Slot> slots;
+    std::vector<BatchSlot> bslots;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<Req*> pending;
@@ -135,11 +155,16 @@ struct Server {
     // statistics
     uint64_t completed = 0, failed = 0, cache_hits = 0, cache_misses = 0, graph_launches = 0;
     uint64_t graph_instantiations = 0, graph_updates = 0, max_launch_us = 0, pin_growths = 0;
+    uint64_t batches = 0, batched_requests = 0;
     double busy_since_ms = -1;
 
     void run();
     int launch(Slot& s, Req& r, std::string& err);
     void finish(Slot& s);
+    int launch_batch(BatchSlot& b, std::vector<Req*>& rs, std::string& err);
+    void finish_batch(BatchSlot& b, cudaError_t q);
+    int graph_run(cudaGraphExec_t& exec, cudaGraph_t g, cudaStream_t st, std::string& err);
+    void fail_request(Req* r, int status, const std::string& err);
     int acquire_tables(Req& r, cudaStream_t st, std::string& err);
     void release_tables(Req& r);
 };
@@ -377,6 +402,206 @@ void Server::finish(Slot& s)
     s.req = nullptr;
 }
 
+void Server::fail_request(Req* r, int status, const std::string& err)
+{
+    r->status = status;
+    r->err = err;
+    r->t_done = Clock::now();
+    r->done = true;
+    release_tables(*r);
+    in_use -= r->footprint;
+    ++failed;
+}
+
+// Updates `exec` in place from the captured graph, or instantiates it anew,
+// and launches it.
+int Server::graph_run(cudaGraphExec_t& exec, cudaGraph_t g, cudaStream_t st, std::string& err)
+{
+    bool ok = false;
+    if (exec) {
+        cudaGraphExecUpdateResultInfo info;
+        ok = cudaGraphExecUpdate(exec, g, &info) == cudaSuccess;
+        if (ok) {
+            ++graph_updates;
+        } else {
+            cudaGetLastError();
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (!ok) {
+        e = cudaGraphInstantiate(&exec, g, 0);
+        if (e == cudaSuccess) ++graph_instantiations;
+        else exec = nullptr;
+    }
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("graph launch: ") + cudaGetErrorString(e);
+        return RBG_ERR_CUDA;
+    }
+    ++graph_launches;
+    return RBG_OK;
+}
+
+// One shared launch for requests rs (all batchable, one split): their
+// workspace images, output tables and the job tables go up in one copy;
+// then the job-table path, payoff, merge and finalize kernels and the
+// result copy run on the batch slot's stream, as one CUDA graph.
+int Server::launch_batch(BatchSlot& b, std::vector<Req*>& rs, std::string& err)
+{
+    cudaStream_t st = b.st;
+    const int n = (int)rs.size();
+    for (Req* r : rs) {
+        const int rc = acquire_tables(*r, st, err);
+        if (rc) return rc;
+    }
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    std::vector<size_t> o_ws(n), o_outs(n), o_T(n), o_ivb(n), o_part(n), o_acc(n), o_res(n);
+    std::vector<int> G(n), nch(n);
+    size_t in_bytes = 256, ivb_bytes = 0, part_bytes = 0, acc_bytes = 0, res_d = 0;
+    for (int k = 0; k < n; ++k) {
+        const Req& r = *rs[k];
+        const int no = (int)r.plan.outs.size();
+        const int64_t B = r.M;  // one launch: the request's whole path count
+        o_ws[k] = in_bytes;
+        in_bytes = up(in_bytes + r.job.host_ws.size());
+        o_outs[k] = in_bytes;
+        in_bytes = up(in_bytes + sizeof(OutDev) * no);
+        o_T[k] = in_bytes;
+        in_bytes = up(in_bytes + sizeof(double) * no);
+        o_ivb[k] = ivb_bytes;
+        ivb_bytes = up(ivb_bytes + sizeof(float) * 2 * r.plan.vgs.size() * (size_t)B);
+        G[k] = payoff_paths_per_thread(r.job.batch, r.job.sms);
+        nch[k] = (int)((B + 256 * (int64_t)G[k] - 1) / (256 * (int64_t)G[k]));
+        o_part[k] = part_bytes;
+        part_bytes = up(part_bytes + sizeof(double) * 4 * no * (size_t)nch[k]);
+        o_acc[k] = acc_bytes;
+        acc_bytes = up(acc_bytes + sizeof(double) * 4 * no);
+        o_res[k] = res_d;
+        res_d += 5 * (size_t)no;
+    }
+    const size_t off_tab = in_bytes;
+    in_bytes = up(in_bytes + mixed_jobs_table_bytes(n));
+    const size_t off_pj = in_bytes;
+    in_bytes = up(in_bytes + sizeof(PayoffJob) * n);
+    const size_t off_aj = in_bytes;
+    in_bytes = up(in_bytes + sizeof(AccJob) * n);
+    const size_t off_fj = in_bytes;
+    in_bytes = up(in_bytes + sizeof(FinJob) * n);
+    cudaError_t e = b.in.ensure(in_bytes, st, pool);
+    if (e == cudaSuccess) e = b.ivb.ensure(ivb_bytes, st, pool);
+    if (e == cudaSuccess) e = b.part.ensure(part_bytes, st, pool);
+    if (e == cudaSuccess) e = b.acc.ensure(acc_bytes, st, pool);
+    if (e == cudaSuccess) e = b.res.ensure(sizeof(double) * 5 * kBatchOutputs, st, pool);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("batch buffers: ") + cudaGetErrorString(e);
+        return RBG_ERR_NOMEM;
+    }
+    unsigned char* din = (unsigned char*)b.in.p;
+    unsigned char* divb = (unsigned char*)b.ivb.p;
+    unsigned char* dpart = (unsigned char*)b.part.p;
+    unsigned char* dacc = (unsigned char*)b.acc.p;
+    double* dres = (double*)b.res.p;
+    b.host_in.assign(in_bytes, 0);  // error word at 0 cleared with the upload
+    std::vector<MixedJobRef> refs(n);
+    PayoffJob* pj = (PayoffJob*)(b.host_in.data() + off_pj);
+    AccJob* aj = (AccJob*)(b.host_in.data() + off_aj);
+    FinJob* fj = (FinJob*)(b.host_in.data() + off_fj);
+    int64_t pblocks = 0, ablocks = 0;
+    for (int k = 0; k < n; ++k) {
+        Req& r = *rs[k];
+        const int no = (int)r.plan.outs.size();
+        std::memcpy(b.host_in.data() + o_ws[k], r.job.host_ws.data(), r.job.host_ws.size());
+        std::memcpy(b.host_in.data() + o_outs[k], r.outs.data(), sizeof(OutDev) * no);
+        std::memcpy(b.host_in.data() + o_T[k], r.Tv.data(), sizeof(double) * no);
+        refs[k] = MixedJobRef{&r.job, din + o_ws[k], r.opt.seed, r.opt.path_offset, r.M, divb + o_ivb[k]};
+        const OutDev* outs = (const OutDev*)(din + o_outs[k]);
+        double* acc = (double*)(dacc + o_acc[k]);
+        pj[k] = PayoffJob{outs, (const float2*)(divb + o_ivb[k]), (double*)(dpart + o_part[k]), r.M, pblocks, no, G[k],
+                          nch[k], 0};
+        pblocks += (int64_t)nch[k] * ((no + 7) / 8);
+        aj[k] = AccJob{(const double*)(dpart + o_part[k]), acc, ablocks, nch[k], no};
+        fj[k] = FinJob{acc, outs, (const double*)(din + o_T[k]), dres + o_res[k], r.M, ablocks, no, r.opt.compute_iv};
+        ablocks += no;
+    }
+    MixedArgs LA;
+    const int grid = mixed_jobs_prepare(refs, din + off_tab, (unsigned int*)din, rs[0]->job.sms, b.host_tab, &LA, err);
+    if (grid < 1) return RBG_ERR_ARG;
+    std::memcpy(b.host_in.data() + off_tab, b.host_tab.data(), b.host_tab.size());
+    // pageable source: staged before the call returns, so host_in may be reused
+    e = cudaMemcpyAsync(din, b.host_in.data(), in_bytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("batch upload: ") + cudaGetErrorString(e);
+        return RBG_ERR_CUDA;
+    }
+    const bool graph = cfg.use_graphs != 0;
+    if (graph && (e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("graph capture: ") + cudaGetErrorString(e);
+        return RBG_ERR_CUDA;
+    }
+    int rc = mixed_launch_jobs(LA, rs[0]->job.split, grid, st, err);
+    if (rc == RBG_OK) {
+        launch_payoff_sums_f32_jobs((const PayoffJob*)(din + off_pj), n, pblocks, st);
+        launch_accumulate_jobs((const AccJob*)(din + off_aj), n, ablocks, st);
+        launch_finalize_jobs((const FinJob*)(din + off_fj), n, ablocks, st);
+        cudaMemcpyAsync(b.pin, din, 4, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(b.pin + 1, dres, sizeof(double) * 5 * kBatchOutputs, cudaMemcpyDeviceToHost, st);
+    }
+    if (graph) {
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(st, &g);
+        if (rc == RBG_OK && e == cudaSuccess) rc = graph_run(b.graph, g, st, err);
+        else if (rc == RBG_OK) {
+            cudaGetLastError();
+            err = std::string("graph capture: ") + cudaGetErrorString(e);
+            rc = RBG_ERR_CUDA;
+        }
+        if (g) cudaGraphDestroy(g);
+    }
+    if (rc != RBG_OK) return rc;
+    if ((e = cudaEventRecord(b.ev, st)) != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("batch launch: ") + cudaGetErrorString(e);
+        return RBG_ERR_CUDA;
+    }
+    b.reqs = rs;
+    b.res_off = o_res;
+    ++batches;
+    batched_requests += (uint64_t)n;
+    return RBG_OK;
+}
+
+void Server::finish_batch(BatchSlot& b, cudaError_t q)
+{
+    unsigned int word = 0;
+    std::memcpy(&word, b.pin, 4);
+    for (size_t k = 0; k < b.reqs.size(); ++k) {
+        Req* r = b.reqs[k];
+        if (q != cudaSuccess) {
+            fail_request(r, RBG_ERR_CUDA, std::string("device: ") + cudaGetErrorString(q));
+            continue;
+        }
+        if (word != 0) {
+            fail_request(r, RBG_ERR_TIMEOUT, "mixed kernel: a bounded pipeline wait expired (site " +
+                                                 std::to_string(word) + ")");
+            continue;
+        }
+        const size_t no = r->plan.outs.size();
+        r->res.assign(b.pin + 1 + b.res_off[k], b.pin + 1 + b.res_off[k] + 5 * no);
+        r->t_done = Clock::now();
+        r->done = true;
+        release_tables(*r);
+        in_use -= r->footprint;
+        ++completed;
+    }
+    b.reqs.clear();
+}
+
 void Server::run()
 {
     cudaSetDevice(dev);
@@ -403,15 +628,88 @@ void Server::run()
                 progressed = true;
             }
         }
+        for (BatchSlot& b : bslots) {
+            if (b.reqs.empty()) continue;
+            const cudaError_t q = cudaEventQuery(b.ev);
+            if (q == cudaErrorNotReady) continue;
+            if (q != cudaSuccess) cudaGetLastError();
+            finish_batch(b, q);
+            progressed = true;
+        }
         if (progressed) cv_done.notify_all();
-        if (stop && pending.empty()) {
-            bool busy = false;
-            for (Slot& s : slots) busy = busy || s.req;
-            if (!busy) break;
+        auto busy_now = [&] {
+            for (Slot& s : slots)
+                if (s.req) return true;
+            for (BatchSlot& b : bslots)
+                if (!b.reqs.empty()) return true;
+            return false;
+        };
+        if (stop && pending.empty() && !busy_now()) break;
+        // shared launches: every free batch slot takes the batchable requests
+        // pending now, in arrival order, up to its job / output / work limits --
+        // after the batching window, when one is set and fewer than a full
+        // batch are pending
+        Clock::time_point wake = Clock::time_point::max();
+        if (cfg.batch_wait_us > 0 && !stop) {
+            int nb = 0;
+            Clock::time_point oldest = Clock::time_point::max();
+            for (Req* r : pending)
+                if (r->batchable) {
+                    ++nb;
+                    oldest = std::min(oldest, r->t_submit);
+                }
+            const auto window = std::chrono::duration_cast<Clock::duration>(
+                std::chrono::duration<double, std::micro>(cfg.batch_wait_us));
+            if (nb > 0 && nb < cfg.max_batch_jobs && Clock::now() < oldest + window) wake = oldest + window;
+        }
+        for (BatchSlot& b : bslots) {
+            if (wake != Clock::time_point::max()) break;  // inside the batching window
+            if (!b.reqs.empty()) continue;
+            std::vector<Req*> batch;
+            int split = -1, outs = 0;
+            double work = 0;
+            size_t fp = 0;
+            for (auto it = pending.begin(); it != pending.end() && (int)batch.size() < cfg.max_batch_jobs;) {
+                Req* r = *it;
+                const int no = (int)r->plan.outs.size();
+                const bool take = r->batchable && (split < 0 || r->job.split == split) &&
+                                  outs + no <= kBatchOutputs &&
+                                  (batch.empty() || work + r->work <= cfg.batch_path_steps) &&
+                                  (in_use + fp + r->footprint <= cfg.hbm_budget || (in_use == 0 && batch.empty()));
+                if (!take) {
+                    ++it;
+                    continue;
+                }
+                split = r->job.split;
+                outs += no;
+                work += r->work;
+                fp += r->footprint;
+                batch.push_back(r);
+                it = pending.erase(it);
+            }
+            if (batch.empty()) break;
+            in_use += fp;
+            const Clock::time_point t0 = Clock::now();
+            for (Req* r : batch) r->t_start = t0;
+            std::string err;
+            const int rc = launch_batch(b, batch, err);
+            const Clock::time_point t1 = Clock::now();
+            max_launch_us = std::max<uint64_t>(
+                max_launch_us, (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count());
+            for (Req* r : batch) r->t_launched = t1;
+            if (rc != RBG_OK) {
+                for (Req* r : batch) fail_request(r, rc, err);
+                cv_done.notify_all();
+            }
+            progressed = true;
         }
         // admissions: first fit in arrival order
         for (auto it = pending.begin(); it != pending.end();) {
             Req* r = *it;
+            if (r->batchable && !bslots.empty()) {  // waits for a batch slot
+                ++it;
+                continue;
+            }
             const bool small = r->work <= cfg.small_request_path_steps;
             Slot* free_slot = nullptr;
             for (Slot& s : slots)
@@ -448,10 +746,12 @@ void Server::run()
             progressed = true;
         }
         if (!progressed) {
-            bool busy = false;
-            for (Slot& s : slots) busy = busy || s.req;
-            // poll the device quickly while work is in flight, sleep otherwise
-            cv_work.wait_for(lk, busy ? std::chrono::microseconds(50) : std::chrono::milliseconds(5));
+            // poll the device quickly while work is in flight, sleep otherwise (until
+            // the batching window closes, at the latest)
+            Clock::duration d = busy_now() ? Clock::duration(std::chrono::microseconds(50))
+                                           : Clock::duration(std::chrono::milliseconds(5));
+            if (wake != Clock::time_point::max()) d = std::min(d, std::max(Clock::duration(0), wake - Clock::now()));
+            cv_work.wait_for(lk, d);
         }
     }
 }
@@ -486,6 +786,10 @@ void rbg_server_default_config(rbg_server_config* c)
     c->table_cache_entries = 256;
     c->use_graphs = 1;
     c->device = -1;
+    c->batch_slots = 4;
+    c->max_batch_jobs = kBatchJobsMax;
+    c->batch_path_steps = (double)(1u << 30);
+    c->batch_wait_us = 0.0;
 }
 
 const char* rbg_server_last_error(void) { return g_srv_err.c_str(); }
@@ -498,6 +802,8 @@ int rbg_server_create(const rbg_server_config* cfg_in, rbg_server** out)
     if (cfg_in) cfg = *cfg_in;
     if (cfg.slots < 1 || cfg.slots > 64 || cfg.high_priority_slots < 0 || cfg.high_priority_slots > cfg.slots)
         return srv_fail(RBG_ERR_ARG, "slots must be 1..64 and high_priority_slots <= slots");
+    if (cfg.batch_slots < 0 || cfg.batch_slots > 16 || cfg.max_batch_jobs < 1 || cfg.max_batch_jobs > kBatchJobsMax)
+        return srv_fail(RBG_ERR_ARG, "batch_slots must be 0..16 and max_batch_jobs 1..64");
     std::unique_ptr<Server> s(new Server());
     s->cfg = cfg;
     int dev = cfg.device;
@@ -535,6 +841,15 @@ int rbg_server_create(const rbg_server_config* cfg_in, rbg_server** out)
         }
         sl.pin_n = bytes;
     }
+    s->bslots.resize(cfg.batch_slots);
+    for (BatchSlot& b : s->bslots) {
+        if (cudaStreamCreateWithPriority(&b.st, cudaStreamNonBlocking, hi) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaMallocHost((void**)&b.pin, sizeof(double) * (1 + 5 * (size_t)kBatchOutputs)) != cudaSuccess) {
+            cudaGetLastError();
+            return srv_fail(RBG_ERR_CUDA, "batch slot creation failed");
+        }
+    }
     Server* raw = s.get();
     s->thr = std::thread([raw] { raw->run(); });
     *out = new rbg_server{std::move(s)};
@@ -564,6 +879,8 @@ int rbg_server_submit(rbg_server* srv, const rbg_params* p, const rbg_options* o
         r->Tv[i] = r->plan.outs[i].T;
     }
     r->work = (double)p->M * p->N * (double)r->plan.vols.size();
+    r->batchable = srv->s->cfg.batch_slots > 0 && mixed_job_batchable(r->job) && r->M <= r->job.batch &&
+                   no <= kBatchOutputs;
     r->footprint = (size_t)p->M * (size_t)p->N * 4 + r->job.workspace_bytes;
     Server& s = *srv->s;
     {
@@ -645,6 +962,8 @@ int rbg_server_get_stats(rbg_server* srv, rbg_server_stats* st)
     st->graph_updates = s.graph_updates;
     st->max_launch_us = s.max_launch_us;
     st->pin_growths = s.pin_growths;
+    st->batches = s.batches;
+    st->batched_requests = s.batched_requests;
     return RBG_OK;
 }
 
@@ -668,6 +987,16 @@ int rbg_server_destroy(rbg_server* srv)
         if (sl.pin) cudaFreeHost(sl.pin);
         cudaEventDestroy(sl.ev);
         cudaStreamDestroy(sl.st);
+    }
+    for (BatchSlot& b : s.bslots) {
+        cudaStreamSynchronize(b.st);
+        if (b.graph) cudaGraphExecDestroy(b.graph);
+        for (SBuf* x : {&b.in, &b.ivb, &b.part, &b.acc, &b.res})
+            if (x->p) cudaFreeAsync(x->p, b.st);
+        cudaStreamSynchronize(b.st);
+        if (b.pin) cudaFreeHost(b.pin);
+        cudaEventDestroy(b.ev);
+        cudaStreamDestroy(b.st);
     }
     for (CacheEntry& e : s.cache) {
         if (e.dev) cudaFreeAsync(e.dev, s.copy_st);
