@@ -552,11 +552,13 @@ def run_sobol(args):
 
 
 # ------------------------------------------------------------ serving arm
-def serving_requests(n: int, rate: float, seed: int = 20261203):
+def serving_requests(n: int, rate: float, seed: int = 20261203, small: bool = False):
     """Calibration-style traffic: Poisson arrivals at `rate`/s; H ~ U[.03,.45],
     eta ~ U[.5,3], rho ~ U[-.99,-.3], xi ~ U[.01,.1], T ~ U[.05,3], 1-64 strikes
     on [0.5, 1.5], N and M log-uniform on [64, 1024] and [2^14, 2^22], Philox
-    seed = request index."""
+    seed = request index.  small: N on [64, 512] and M on [2^14, 2^17] (the
+    requests shared launches price), for a saturating stream."""
+    n_hi, m_hi = (512, 2 ** 17) if small else (1024, 2 ** 22)
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / rate, n))
     reqs = []
@@ -566,8 +568,8 @@ def serving_requests(n: int, rate: float, seed: int = 20261203):
             H=[float(rng.uniform(0.03, 0.45))], eta=[float(rng.uniform(0.5, 3.0))], rho=[float(rng.uniform(-0.99, -0.3))],
             xi=float(rng.uniform(0.01, 0.1)), T=[float(rng.uniform(0.05, 3.0))] * nk,
             K=list(np.linspace(0.5, 1.5, nk)) if nk > 1 else [1.0],
-            N=int(np.exp(rng.uniform(np.log(64), np.log(1024)))),
-            M=int(np.exp(rng.uniform(np.log(2 ** 14), np.log(2 ** 22)))), seed=i, t=float(t[i])))
+            N=int(np.exp(rng.uniform(np.log(64), np.log(n_hi)))),
+            M=int(np.exp(rng.uniform(np.log(2 ** 14), np.log(m_hi)))), seed=i, t=float(t[i])))
     return reqs
 
 
@@ -579,7 +581,7 @@ def serve_stream(args, local: int) -> dict:
 
     import rbergomi_gb300 as R
 
-    reqs = serving_requests(args.requests, args.rate)
+    reqs = serving_requests(args.requests, args.rate, small=args.small_only)
     # warm the kernels and the allocator on a few off-schedule requests
     with R.Server() as srv:
         for r in reqs[:8]:
@@ -587,7 +589,8 @@ def serve_stream(args, local: int) -> dict:
     lat = np.zeros((len(reqs), 3))
     n0 = R.launch_count()
     with ClockSampler(local) as clk:
-        with R.Server(use_graphs=0 if args.no_graphs else 1, batch_wait_us=args.batch_wait_us) as srv:
+        with R.Server(use_graphs=0 if args.no_graphs else 1, batch_wait_us=args.batch_wait_us,
+                      batch_slots=args.batch_slots) as srv:
             tickets = [None] * len(reqs)
             ready = threading.Semaphore(0)
 
@@ -638,7 +641,7 @@ def serve_stream(args, local: int) -> dict:
                 "note": "one request at a time, no queueing: latency is service time only"}
     return {
         "workload": "serving-poisson", "requests": len(reqs), "rate_per_s": args.rate, "graphs": not args.no_graphs,
-        "batch_wait_us": args.batch_wait_us,
+        "batch_wait_us": args.batch_wait_us, "batch_slots": args.batch_slots, "small_only": args.small_only,
         "p50_ms": float(np.percentile(total, 50)), "p99_ms": float(np.percentile(total, 99)),
         "max_ms": float(np.max(total)), "mean_ms": float(np.mean(total)),
         "queue_p99_ms": float(np.percentile(lat[:, 0], 99)), "service_p99_ms": float(np.percentile(lat[:, 1], 99)),
@@ -696,6 +699,9 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serving: Poisson arrival rate per second")
     ap.add_argument("--fp64-sample", type=int, default=20, help="serving: FP64 one-at-a-time sample size")
     ap.add_argument("--no-graphs", action="store_true", help="serving: launch without CUDA graphs")
+    ap.add_argument("--batch-slots", type=int, default=8, help="serving: shared launches in flight (0: none)")
+    ap.add_argument("--small-only", action="store_true",
+                    help="serving: only requests shared launches price (N <= 512, M <= 2^17)")
     ap.add_argument("--batch-wait-us", type=float, default=0.0,
                     help="serving: batching window of the shared launches (0: launch what is pending at once)")
     ap.add_argument("--skip-cpu", action="store_true")

@@ -786,7 +786,7 @@ void rbg_server_default_config(rbg_server_config* c)
     c->table_cache_entries = 256;
     c->use_graphs = 1;
     c->device = -1;
-    c->batch_slots = 4;
+    c->batch_slots = 8;
     c->max_batch_jobs = kBatchJobsMax;
     c->batch_path_steps = (double)(1u << 30);
     c->batch_wait_us = 0.0;
