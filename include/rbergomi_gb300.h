@@ -342,10 +342,12 @@ int rbg_debug_mixed_profile(const rbg_params* p, const rbg_options* o, uint64_t*
  * requests (M*N*n_H <= small_request_path_steps) use high-priority streams;
  * large ones are cut into launches of at most max_batch_paths paths so they
  * yield the GPU between launches.  Volterra tables are cached on the device
- * per (backend, H, N, split).  With use_graphs, each request's device work is
- * launched as a CUDA graph, one executable per launch shape, updated in
- * place.  All requests run the mixed form; results do not depend on what
- * else is in flight (counter-based normals, per-request sums). */
+ * per (backend, H, N, split).  With use_graphs, the device work of each
+ * shared launch, and of each request of one launch, runs as a CUDA graph,
+ * one executable per batch slot or launch shape, updated in place.  All
+ * requests run the mixed form; results do not depend on what else is in
+ * flight, nor on whether they ran alone or in a shared launch
+ * (counter-based normals, per-request sums, the same per-path arithmetic). */
 typedef struct rbg_server rbg_server;
 
 typedef struct rbg_server_config {
@@ -376,6 +378,9 @@ typedef struct rbg_server_stats {
     uint64_t max_launch_us;                       /* longest admission-to-launched time on the scheduler */
     uint64_t pin_growths;                         /* pinned result buffers regrown (a device-wide wait each) */
     uint64_t batches, batched_requests;           /* shared launches, and the requests they priced */
+    /* longest scheduler-thread time of one launch in each phase (us): device
+     * buffers, Volterra tables, uploads, graph capture + instantiate/update + launch */
+    uint64_t max_alloc_us, max_tables_us, max_upload_us, max_graph_us;
 } rbg_server_stats;
 
 void rbg_server_default_config(rbg_server_config* cfg);

@@ -539,7 +539,8 @@ class RbgServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("completed", "failed", "pending", "in_flight", "hbm_in_use",
                                           "table_cache_hits", "table_cache_misses", "graph_launches",
                                           "graph_instantiations", "graph_updates", "max_launch_us", "pin_growths",
-                                          "batches", "batched_requests")]
+                                          "batches", "batched_requests", "max_alloc_us", "max_tables_us",
+                                          "max_upload_us", "max_graph_us")]
 
 
 def _server_lib():

@@ -759,6 +759,16 @@ void launch_finalize_jobs(const FinJob* jobs, int n_jobs, int64_t blocks, void* 
     count_launch();
 }
 
+void reduce_preload()
+{
+    cudaFuncAttributes fa;
+    cudaFuncGetAttributes(&fa, k_accumulate);
+    cudaFuncGetAttributes(&fa, k_accumulate_jobs);
+    cudaFuncGetAttributes(&fa, k_finalize);
+    cudaFuncGetAttributes(&fa, k_finalize_jobs);
+    cudaGetLastError();
+}
+
 void launch_finalize(const double* acc, int n_out, int64_t M, const OutDev* outs, const double* Tvals,
                      int compute_iv, double* res, void* stream)
 {

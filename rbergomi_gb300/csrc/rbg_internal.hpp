@@ -178,6 +178,8 @@ struct FinJob {  // price, stat, implied vol, n_out blocks of one warp
 };
 void launch_accumulate_jobs(const AccJob* jobs, int n_jobs, int64_t blocks, void* stream);
 void launch_finalize_jobs(const FinJob* jobs, int n_jobs, int64_t blocks, void* stream);
+// Loads the merge and finalize kernels (modules load lazily, on first use).
+void reduce_preload();
 
 // Kernel-launch counter shared by all launchers.
 void count_launch(int n = 1);

@@ -2224,6 +2224,23 @@ int mixed_launch_jobs(const MixedArgs& A, int split, int grid, cudaStream_t st, 
     return RBG_OK;
 }
 
+// Loads the path and payoff kernels a serving loop may launch (CUDA loads a
+// kernel's module lazily, on first use: a load in the middle of a request
+// stream stalls that request's launch).
+void mixed_preload()
+{
+    cudaFuncAttributes fa;
+    void (*kerns[])(MixedArgs) = {
+        k_mixed_gemm<0, 0, false>, k_mixed_gemm<0, 1, false>, k_mixed_gemm<0, 2, false>,
+        k_mixed_gemm<1, 0, false>, k_mixed_gemm<1, 1, false>, k_mixed_gemm<1, 2, false>,
+        k_mixed_gemm<2, 0, false>, k_mixed_gemm<2, 1, false>, k_mixed_gemm<2, 2, false>,
+        k_mixed_gemm_jobs<0>, k_mixed_gemm_jobs<1>, k_mixed_gemm_jobs<2>};
+    for (auto k : kerns) cudaFuncGetAttributes(&fa, k);
+    cudaFuncGetAttributes(&fa, k_payoff_sums_f32<false>);
+    cudaFuncGetAttributes(&fa, k_payoff_sums_f32_jobs);
+    cudaGetLastError();
+}
+
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err)
 {
     unsigned int word = 0;

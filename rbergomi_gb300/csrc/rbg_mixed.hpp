@@ -97,6 +97,8 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
                  const double* ext = nullptr);
 int mixed_part_rows(const MixedJob& job, int64_t B);
 int mixed_check(const MixedJob& job, void* ws, cudaStream_t st, std::string& err);
+// Loads the path and payoff kernels a serving loop may launch (modules load lazily).
+void mixed_preload();
 // one warp waits on an mbarrier nothing arrives on, with the pipeline's bounded
 // wait and a 20 ms limit; *err receives `site` on expiry
 int launch_wait_probe(unsigned int* err, unsigned int site, cudaStream_t st);

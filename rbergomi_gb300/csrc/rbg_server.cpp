@@ -156,6 +156,8 @@ struct Server {
     uint64_t completed = 0, failed = 0, cache_hits = 0, cache_misses = 0, graph_launches = 0;
     uint64_t graph_instantiations = 0, graph_updates = 0, max_launch_us = 0, pin_growths = 0;
     uint64_t batches = 0, batched_requests = 0;
+    // longest scheduler-thread time per launch phase (us): buffers, tables, uploads, graph
+    uint64_t max_alloc_us = 0, max_tables_us = 0, max_upload_us = 0, max_graph_us = 0;
     double busy_since_ms = -1;
 
     void run();
@@ -167,6 +169,17 @@ struct Server {
     void fail_request(Req* r, int status, const std::string& err);
     int acquire_tables(Req& r, cudaStream_t st, std::string& err);
     void release_tables(Req& r);
+};
+
+// Times the phases of one launch on the scheduler thread into the server's maxima.
+struct Laps {
+    Clock::time_point t = Clock::now();
+    void lap(uint64_t& mx)
+    {
+        const Clock::time_point n = Clock::now();
+        mx = std::max<uint64_t>(mx, (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(n - t).count());
+        t = n;
+    }
 };
 
 static uint64_t hbits(double x)
@@ -253,6 +266,7 @@ int Server::launch(Slot& s, Req& r, std::string& err)
     const int64_t B = job.batch;
     const int G = payoff_paths_per_thread(B, job.sms);
     const int64_t rows = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+    Laps laps;
     cudaError_t e = s.ws.ensure(job.workspace_bytes, st, pool);
     if (e == cudaSuccess && !job.fused)
         e = s.ivb.ensure(sizeof(float) * 2 * r.plan.vgs.size() * (size_t)B, st, pool);
@@ -275,8 +289,10 @@ int Server::launch(Slot& s, Req& r, std::string& err)
         err = std::string("slot buffers: ") + cudaGetErrorString(e);
         return RBG_ERR_NOMEM;
     }
+    laps.lap(max_alloc_us);
     int rc = acquire_tables(r, st, err);
     if (rc) return rc;
+    laps.lap(max_tables_us);
     OutDev* d_outs = (OutDev*)s.outs.p;
     double* d_T = (double*)((unsigned char*)s.outs.p + ((sizeof(OutDev) * no + 255) / 256) * 256);
     // inputs (pageable host memory; the request keeps them alive until it completes)
@@ -289,8 +305,11 @@ int Server::launch(Slot& s, Req& r, std::string& err)
         return RBG_ERR_CUDA;
     }
 
-    // device work of the request: captured as a CUDA graph when configured
-    const bool graph = cfg.use_graphs != 0;
+    laps.lap(max_upload_us);
+    // device work of the request: captured as a CUDA graph when configured, for
+    // requests of one launch (replaying a many-launch request saves nothing
+    // measurable, and instantiating its graph took milliseconds)
+    const bool graph = cfg.use_graphs != 0 && r.M <= B;
     if (graph) {
         e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) {
@@ -369,6 +388,7 @@ int Server::launch(Slot& s, Req& r, std::string& err)
             return RBG_ERR_CUDA;
         }
     }
+    laps.lap(max_graph_us);
     if (rc != RBG_OK) {
         err = kerr;
         return rc;
@@ -453,10 +473,12 @@ int Server::launch_batch(BatchSlot& b, std::vector<Req*>& rs, std::string& err)
 {
     cudaStream_t st = b.st;
     const int n = (int)rs.size();
+    Laps laps;
     for (Req* r : rs) {
         const int rc = acquire_tables(*r, st, err);
         if (rc) return rc;
     }
+    laps.lap(max_tables_us);
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     std::vector<size_t> o_ws(n), o_outs(n), o_T(n), o_ivb(n), o_part(n), o_acc(n), o_res(n);
     std::vector<int> G(n), nch(n);
@@ -500,6 +522,7 @@ int Server::launch_batch(BatchSlot& b, std::vector<Req*>& rs, std::string& err)
         err = std::string("batch buffers: ") + cudaGetErrorString(e);
         return RBG_ERR_NOMEM;
     }
+    laps.lap(max_alloc_us);
     unsigned char* din = (unsigned char*)b.in.p;
     unsigned char* divb = (unsigned char*)b.ivb.p;
     unsigned char* dpart = (unsigned char*)b.part.p;
@@ -538,6 +561,7 @@ int Server::launch_batch(BatchSlot& b, std::vector<Req*>& rs, std::string& err)
         err = std::string("batch upload: ") + cudaGetErrorString(e);
         return RBG_ERR_CUDA;
     }
+    laps.lap(max_upload_us);
     const bool graph = cfg.use_graphs != 0;
     if (graph && (e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
         cudaGetLastError();
@@ -563,6 +587,7 @@ int Server::launch_batch(BatchSlot& b, std::vector<Req*>& rs, std::string& err)
         }
         if (g) cudaGraphDestroy(g);
     }
+    laps.lap(max_graph_us);
     if (rc != RBG_OK) return rc;
     if ((e = cudaEventRecord(b.ev, st)) != cudaSuccess) {
         cudaGetLastError();
@@ -850,6 +875,9 @@ int rbg_server_create(const rbg_server_config* cfg_in, rbg_server** out)
             return srv_fail(RBG_ERR_CUDA, "batch slot creation failed");
         }
     }
+    // every kernel the loop may launch, loaded now rather than mid-stream
+    mixed_preload();
+    reduce_preload();
     Server* raw = s.get();
     s->thr = std::thread([raw] { raw->run(); });
     *out = new rbg_server{std::move(s)};
@@ -964,6 +992,10 @@ int rbg_server_get_stats(rbg_server* srv, rbg_server_stats* st)
     st->pin_growths = s.pin_growths;
     st->batches = s.batches;
     st->batched_requests = s.batched_requests;
+    st->max_alloc_us = s.max_alloc_us;
+    st->max_tables_us = s.max_tables_us;
+    st->max_upload_us = s.max_upload_us;
+    st->max_graph_us = s.max_graph_us;
     return RBG_OK;
 }
 
