@@ -76,7 +76,7 @@ struct MixedJob {
     std::vector<unsigned char> host_ws;  // image uploaded by mixed_upload
 };
 
-// mc: the plain Monte Carlo estimator (GEMM backend, N <= 1024).
+// mc: the plain Monte Carlo estimator (a third normal stream; both backends, every pass mode).
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
                   int64_t max_batch = 0, bool mc = false);
 // Byte range of launch i's strip (GEMM) or spectrum (FFT) inside host_ws, and
