@@ -37,7 +37,15 @@
 
 namespace rbg {
 
-__host__ __device__ constexpr int fft_threads(int logL) { return 256; }
+// Threads per CTA: one radix-16 butterfly each (L / 16), between one warp and
+// 256 threads; L = 8192 runs two butterflies per thread.
+__host__ __device__ constexpr int fft_threads(int logL)
+{
+    return logL >= 12 ? 256 : (logL >= 10 ? (1 << logL) / 16 : 32);
+}
+// CTAs per SM the launch bounds promise: at most 128 registers a thread below
+// L = 8192 (which runs one CTA per SM at up to 255).
+__host__ __device__ constexpr int fft_min_blocks(int logL) { return logL >= 13 ? 1 : 65536 / (fft_threads(logL) * 128); }
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -222,9 +230,14 @@ __device__ __forceinline__ void fft_r16(float2* buf, const float2* tw, const Fft
 
 // Forward transform of the pair's normals times the spectrum, or inverse
 // transform of the buffer.  L >= 16.  For odd log2 L the radix-2 first pass
-// of the forward transform is the SRC_WS_DUP read.
+// of the forward transform is the SRC_WS_DUP read.  The input descriptor is
+// passed by value and the Philox round keys come from parameter space: with
+// both, the kernel needs no local memory at L = 4096 and 8192 (it spilled
+// 84 B at L = 4096 before).  Compiling the transforms as functions of their
+// own also removes the spill but measured 13 % slower at L = 4096: the
+// scheduler can no longer overlap a pass's twiddle loads with other work.
 template <int LOGL, bool INV, int T>
-__device__ __forceinline__ void fft_inplace(float2* buf, const float2* tw, const FftIn& in, const float2* spec)
+__device__ __forceinline__ void fft_inplace(float2* buf, const float2* tw, const FftIn in, const float2* spec)
 {
     constexpr int REM = LOGL % 4;
     if constexpr (INV) {
@@ -257,7 +270,7 @@ __host__ __device__ inline FftSmem fft_smem(int L, int Np, int n_g, int ns = 2)
     const int warps = fft_threads(logL) / 32;
     FftSmem S;
     S.buf = 0;
-    S.w = (L + L / 16) * 8;                        // padded transform buffer
+    S.w = ((L + L / 16) * 8 + 15) & ~15;           // padded transform buffer; the normals start 16-byte aligned
     S.red = S.w + 2 * ns * (Np + 4) * 4;           // [2 paths][W1 | W1perp (| Wperp)][Np + 4]
     S.total = S.red + warps * n_g * 2 * ns * 4 + 64;
     return S;
@@ -265,7 +278,7 @@ __host__ __device__ inline FftSmem fft_smem(int L, int Np, int n_g, int ns = 2)
 
 // MC: plain Monte Carlo, a third normal stream (Wperp) and IsvdWp per path.
 template <int LOGL, bool MC>
-__global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed_fft(const __grid_constant__ MixedArgs a)
+__global__ void __launch_bounds__(fft_threads(LOGL), fft_min_blocks(LOGL)) k_mixed_fft(const __grid_constant__ MixedArgs a)
 {
     constexpr int T = fft_threads(LOGL), L = 1 << LOGL, WARPS = T / 32, NS = MC ? 3 : 2;
     extern __shared__ __align__(16) unsigned char smf[];
@@ -276,7 +289,7 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
     float* red = (float*)(smf + S.red);
     const int W = Np + 4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const PhiloxKeys keys = philox_keys(a.seed);
+    const PhiloxKeys& keys = *reinterpret_cast<const PhiloxKeys*>(a.pk);  // parameter space, no registers
     const int64_t npairs = (a.B + 1) / 2;
     const int ngrp = (N + 3) >> 2;
 
@@ -302,9 +315,12 @@ __global__ void __launch_bounds__(fft_threads(LOGL), LOGL >= 13 ? 1 : 2) k_mixed
                 box_muller_f32(x.x, x.y, z[0], z[1]);
                 box_muller_f32(x.z, x.w, z[2], z[3]);
             }
-            float* o = ws + (NS * pth + s) * W + 4 * g;
+            // one 16-byte store (W and the row bases are multiples of 4 floats): four
+            // scalar stores 16 bytes apart would each be 4-way bank conflicted
 #pragma unroll
-            for (int e = 0; e < 4; ++e) o[e] = (4 * g + e < N) ? z[e] : 0.f;
+            for (int e = 0; e < 4; ++e)
+                if (4 * g + e >= N) z[e] = 0.f;
+            *(float4*)(ws + (NS * pth + s) * W + 4 * g) = make_float4(z[0], z[1], z[2], z[3]);
             g += T;
             while (g >= ngrp) {
                 g -= ngrp;

@@ -2084,7 +2084,7 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         A.dbg_x = dbg_x;
         A.sob = job.sob;
         A.ext = ext;
-        A.seed = seed;
+        mixed_set_seed(A, seed);
         A.path0 = path0;
         A.B = B;
         const int smem =
@@ -2165,7 +2165,7 @@ int mixed_jobs_prepare(const std::vector<MixedJobRef>& jobs, void* table, unsign
         A.dbg_w = nullptr;
         A.dbg_x = nullptr;
         A.n_o = 0;
-        A.seed = r.seed;
+        mixed_set_seed(A, r.seed);
         A.path0 = r.path0;
         A.B = r.B;
         A.jobs = nullptr;

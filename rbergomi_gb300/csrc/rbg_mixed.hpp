@@ -54,7 +54,26 @@ struct MixedArgs {
     const MixedArgs* jobs;
     const int64_t* job_tile0;
     int n_jobs;
+    // Philox4x32-10 round keys of `seed` in the PhiloxKeys layout (pk[r] = lo +
+    // r 0x9E3779B9, pk[10 + r] = hi + r 0xBB67AE85), set with it by
+    // mixed_set_seed.  The FFT kernel reads them from parameter space, where
+    // each round's key is an operand of its XOR instead of one of 20 registers
+    // held across the whole kernel.
+    uint32_t pk[20];
 };
+
+// Sets a.seed and its Philox round keys a.pk.
+inline void mixed_set_seed(MixedArgs& a, uint64_t seed)
+{
+    a.seed = seed;
+    uint32_t x = (uint32_t)seed, y = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        a.pk[r] = x;
+        a.pk[10 + r] = y;
+        x += 0x9E3779B9u;
+        y += 0xBB67AE85u;
+    }
+}
 
 struct MixedLaunch {
     MixedArgs args;  // device pointers filled at launch time
