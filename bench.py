@@ -498,8 +498,8 @@ def run_sobol(args):
     H=0.1, eta=1.9, rho=-0.9, xi=0.235^2, T=1, 21 strikes on [0.6, 1.4], N=256
     (512 Sobol' dimensions), M = 2^20 points.  Direction integers: the
     reference generator's own (rBergomi/sobol.cpp), recovered from its points
-    in tests/golden/sobol.npz.  The same call with the Brownian bridge and the
-    Philox FP64 pricer on the same workload are timed beside it."""
+    in tests/golden/sobol.npz.  The same call with the Brownian bridge (both
+    forms) and the Philox pricers on the same workload are timed beside it."""
     import torch
 
     import rbergomi_gb300 as R
@@ -536,6 +536,8 @@ def run_sobol(args):
     ms_p, (pp, sp, _) = timed(lambda: R.price_rt(*a, seed=11, precision=R.FP64, stream=stream.cuda_stream))
     ms_m, (pm, _, _) = timed(lambda: R.price_rt_sobol(*a, V, precision=R.MIXED, stream=stream.cuda_stream))
     ms_pm, _ = timed(lambda: R.price_rt(*a, seed=11, precision=R.MIXED, stream=stream.cuda_stream))
+    ms_mb, (pmb, _, _) = timed(lambda: R.price_rt_sobol(*a, V, bridge=True, precision=R.MIXED,
+                                                        stream=stream.cuda_stream))
     print(json.dumps({
         "metric": METRIC, "value": M * N / (ms / 1e3), "unit": "path-steps/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -545,6 +547,8 @@ def run_sobol(args):
         "bridge_value": M * N / (ms_b / 1e3), "philox_fp64_value": M * N / (ms_p / 1e3),
         "mixed_value": M * N / (ms_m / 1e3), "max_rel_diff_mixed_vs_fp64_qmc": float(np.max(np.abs(pm - pq) / pq)),
         "philox_mixed_value": M * N / (ms_pm / 1e3),
+        "mixed_bridge_value": M * N / (ms_mb / 1e3),
+        "max_rel_diff_mixed_vs_fp64_bridge": float(np.max(np.abs(pmb - pb) / pb)),
         "max_abs_diff_qmc_vs_philox": float(np.max(np.abs(pq - pp))), "philox_stat_max": float(np.max(sp)),
         "max_abs_diff_bridge_vs_plain_qmc": float(np.max(np.abs(pb - pq))),
         "clocks": clk.summary(), "gpu_launches": launches,

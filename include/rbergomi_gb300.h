@@ -257,8 +257,12 @@ int rbg_generate_normals_streams(uint64_t seed, int64_t path_offset, int64_t M, 
 /* RT prices over Sobol' normals; the seed is unused, o->path_offset shifts
  * the point range.  stat is the reference's Monte Carlo formula applied to
  * the QMC sample.  o->precision == RBG_FP64: the FP64 form (normcdfinv),
- * bridge allowed.  RBG_MIXED: the tensor-core form on the same points (FP32
- * quantile, GEMM backend: N <= 1024), no bridge, point indices below 2^32. */
+ * bridge allowed.  RBG_MIXED: the tensor-core form on the same points, any
+ * backend and N the mixed form takes.  Without the bridge its normals are the
+ * FP32 quantile of each coordinate's top 32 bits: drawn by the GEMM kernel's
+ * producer for N <= 1024 and point indices below 2^32, otherwise materialized
+ * per batch on the device.  With the bridge those FP32 normals go through
+ * the bridge in FP32 (materialized). */
 int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t* directions, int dims, int bridge,
                        double* price, double* stat, double* iv);
 /* Failure-detection check (no counterpart in the reference): one warp waits,
@@ -271,7 +275,7 @@ int rbg_debug_wait_timeout(unsigned int* site);
 /* The Sobol' normals those prices use: M*2*N doubles in the quadrature
  * layout, host pointer.  precision RBG_FP64: normcdfinv of the 62-bit point;
  * RBG_MIXED: the mixed form's FP32 normals (top 32 bits of the point, FP32
- * quantile), widened exactly to double (no bridge). */
+ * quantile; with the bridge, the bridge in FP32), widened exactly to double. */
 int rbg_sobol_normals(const uint64_t* directions, int dims, int N, int64_t M, int64_t path_offset, int bridge,
                       int precision, double* Z);
 

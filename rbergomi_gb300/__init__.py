@@ -378,7 +378,7 @@ def sobol_normals(directions, N, M, path_offset=0, bridge=False, precision=FP64)
     XOR of directions[d, k] over the set bits k of s ^ (s >> 1), times 2^-62).
     bridge: Brownian-bridge map of each stream (rBergomi/aux.h
     hierarchical2increments; N a power of two).  precision=MIXED: the mixed
-    form's FP32 normals, widened to double."""
+    form's FP32 normals (with the bridge in FP32), widened to double."""
     V = _sobol_table(directions)
     Z = np.empty((M, 2, N))
     _check(lib().rbg_sobol_normals(V.ctypes.data_as(C.POINTER(C.c_uint64)), V.shape[0], int(N), int(M),
@@ -387,8 +387,10 @@ def sobol_normals(directions, N, M, path_offset=0, bridge=False, precision=FP64)
 
 
 def price_rt_sobol(xi, H, eta, rho, T, K, N, M, directions, bridge=False, **opts):
-    """RT prices over Sobol' normals, FP64 form (the reference's
-    ComputeIVRTMT_sobol, rBergomi/rBergomiMT.cpp:610-715): (price, stat, iv)."""
+    """RT prices over Sobol' normals (the reference's ComputeIVRTMT_sobol,
+    rBergomi/rBergomiMT.cpp:610-715): (price, stat, iv).  FP64 form by
+    default; precision=MIXED runs the same points through the tensor-core
+    form, with or without the Brownian bridge, on either backend."""
     V = _sobol_table(directions)
     p = _Params(xi, H, eta, rho, T, K, N, M)
     opts.setdefault("precision", FP64)

@@ -378,23 +378,40 @@ static int price_fp64(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M,
     return RBG_OK;
 }
 
+// Sobol' normals materialized per batch on the device and read by the mixed
+// path kernel as caller normals (quadrature layout): the mixed form's QMC
+// where its GEMM producer cannot draw the points itself -- the Brownian
+// bridge (each bridged step needs the whole point), the FFT backend, and
+// more than 1024 steps (multi-pass tiles redraw earlier chunks).
+struct SobolZ {
+    const unsigned long long* vt;  // FP64 direction table [62][2N] on the device
+    const SobolBridge* br;         // null: no bridge; FP32 quantile (the GEMM producer's normals), FP32 bridge
+    int64_t path_offset;
+};
+
 // Mixed form: tcgen05 fused path kernel writes FP32 (Ivdt, IsvdW) per
 // (variance group, path); the FP64 payoff/sum kernels finish.
 // sob: Sobol' normals (device table [32][2N], bits 30..61 of the direction
-// integers; GEMM backend, RT) instead of the Philox stream.
+// integers; GEMM backend, RT) instead of the Philox stream; sz: Sobol'
+// normals materialized per batch instead.
 static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M, cudaStream_t st,
-                       double* host_res, bool mc = false, const unsigned int* sob = nullptr)
+                       double* host_res, bool mc = false, const unsigned int* sob = nullptr,
+                       const SobolZ* sz = nullptr)
 {
     TableSet ts;
     int rc = upload_tables(c, plan, st, ts);
     if (rc) return rc;
     const int no = (int)plan.outs.size();
     MixedJob job;
-    if ((rc = mixed_prepare(plan, o, M, job, g_err, 0, mc))) return rc;
+    // materialized normals: 2 N doubles per path, at most 2 GiB per batch
+    const int64_t zcap = sz ? std::max<int64_t>(256, ((int64_t)1 << 31) / (16 * (int64_t)plan.N)) : 0;
+    if ((rc = mixed_prepare(plan, o, M, job, g_err, zcap, mc))) return rc;
     job.sob = sob;
     if (sob && (job.backend != RBG_CONV_GEMM || plan.N > 1024))
         return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend and N <= 1024");
     const int64_t B = job.batch;
+    if (sz && (rc = ensure(c.z, sizeof(double) * 2 * plan.N * (size_t)B, "normals"))) return rc;
+    const double* zext = sz ? c.z.as<double>() : nullptr;
     if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
     const int G = payoff_paths_per_thread(B, job.sms);
     const int64_t max_chunks = job.fused ? mixed_part_rows(job, B) : (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
@@ -417,6 +434,12 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
     RBG_CUDA(cudaMemsetAsync(c.acc.p, 0, sizeof(double) * 4 * no, st));
     for (int64_t m0 = 0; m0 < M; m0 += B) {
         const int64_t b = std::min(B, M - m0);
+        if (sz) {
+            ProfScope ps(kStageNormals, st);
+            if (launch_sobol_normals(sz->vt, plan.N, (uint64_t)(sz->path_offset + m0 + 1), b, sz->br, c.z.as<double>(),
+                                     st, 1))
+                return fail(RBG_ERR_UNSUPPORTED, "Brownian bridge shared memory not available for this N");
+        }
         if (job.fused) {
             // payoffs summed inside the path kernel: one partial row per CTA
             const int rows = mixed_part_rows(job, b);
@@ -424,7 +447,7 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
             {
                 ProfScope ps(kStageMixed, st, (int)job.launches.size());
                 if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, nullptr, st, g_err, nullptr,
-                                       nullptr, c.part.as<double>())))
+                                       nullptr, c.part.as<double>(), nullptr, nullptr, zext)))
                     return rc;
             }
             ProfScope ps(kStageReduce, st);
@@ -433,7 +456,7 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
             {
                 ProfScope ps(kStageMixed, st, (int)job.launches.size());
                 if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, c.ivb.p, st, g_err, nullptr,
-                                       nullptr, nullptr, nullptr, ivq)))
+                                       nullptr, nullptr, nullptr, ivq, zext)))
                     return rc;
             }
             const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
@@ -448,10 +471,14 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
         }
         RBG_CUDA(cudaGetLastError());
     }
-    if ((rc = mixed_check(job, c.mixed_ws.p, st, g_err))) return rc;
-    g_d2h += 4;
     launch_finalize(c.acc.as<double>(), no, M, ts.t.outs, ts.Tvals, o.compute_iv, c.res.as<double>(), st);
     RBG_CUDA(cudaGetLastError());
+    // one wait for the whole call: the kernel error word is read after the
+    // finalize kernel is queued (finalizing the sums of a launch that gave up
+    // is harmless; its results are discarded), so no host round trip sits
+    // between the path kernels and the finalize
+    if ((rc = mixed_check(job, c.mixed_ws.p, st, g_err))) return rc;
+    g_d2h += 4;
     RBG_CUDA(cudaMemcpyAsync(host_res, c.res.p, sizeof(double) * 5 * no, cudaMemcpyDeviceToHost, st));
     RBG_CUDA(cudaStreamSynchronize(st));
     g_d2h += sizeof(double) * 5 * no;
@@ -939,10 +966,6 @@ int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t
 {
     if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
     if (o->precision != RBG_FP64 && o->precision != RBG_MIXED) return fail(RBG_ERR_ARG, "unknown precision");
-    if (o->precision == RBG_MIXED && bridge)
-        return fail(RBG_ERR_UNSUPPORTED, "the Brownian bridge runs in the FP64 form only");
-    if (o->precision == RBG_MIXED && (o->conv == RBG_CONV_FFT || p->N > 1024))
-        return fail(RBG_ERR_UNSUPPORTED, "Sobol' normals in the mixed form need the GEMM backend and N <= 1024");
     g_h2d = g_d2h = 0;
     Plan plan;
     std::string err;
@@ -953,9 +976,18 @@ int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
     std::vector<double> res(5 * plan.outs.size(), 0.0);
-    if (o->precision == RBG_MIXED) {
+    // the mixed form's GEMM producer draws the points itself (N <= 1024, point
+    // indices below 2^32, no bridge); otherwise the normals are materialized
+    const bool producer = !bridge && o->conv != RBG_CONV_FFT && plan.N <= 1024 &&
+                          (uint64_t)o->path_offset + (uint64_t)p->M + 128 < ((uint64_t)1 << 32);
+    if (o->precision == RBG_MIXED && producer) {
         if ((rc = sobol32_setup(*c, directions, dims, plan.N, o->path_offset, p->M, st))) return rc;
         if ((rc = price_mixed(*c, plan, *o, p->M, st, res.data(), false, c->sobol32.as<unsigned int>()))) return rc;
+    } else if (o->precision == RBG_MIXED) {
+        SobolBridge br{};
+        if ((rc = sobol_setup(*c, directions, dims, plan.N, bridge, o->path_offset, p->M, st, br))) return rc;
+        const SobolZ sz{c->sobol.as<unsigned long long>(), bridge ? &br : nullptr, o->path_offset};
+        if ((rc = price_mixed(*c, plan, *o, p->M, st, res.data(), false, nullptr, &sz))) return rc;
     } else {
         SobolBridge br{};
         if ((rc = sobol_setup(*c, directions, dims, plan.N, bridge, o->path_offset, p->M, st, br))) return rc;

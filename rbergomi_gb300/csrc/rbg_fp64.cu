@@ -644,15 +644,31 @@ __device__ double bs_gen(double K, double T, double s, int put)
     return put ? (-phi_cdf(-d1) + phi_cdf(-d2) * K) : (phi_cdf(d1) - phi_cdf(d2) * K);
 }
 
+// The out-of-the-money Black-Scholes price in FP32 (S0 = 1, r = 0): the
+// bracketing rounds of implied_vol_warp.  lnK1 = ln(1 / K), sqT = sqrt(T).
+__device__ __forceinline__ float bs_gen_f32(float lnK1, float sqT, float K, float s, int put)
+{
+    const float ssq = s * sqT;
+    const float d1 = fmaf(0.5f, ssq, lnK1 * rcp_approx(ssq));
+    const float d2 = d1 - ssq;
+    return put ? fmaf(K, phi_f32(-d2), -phi_f32(-d1)) : fmaf(-K, phi_f32(d2), phi_f32(d1));
+}
+
 // Implied vol by a warp: inverts on the out-of-the-money side (put-call
 // parity for K < 1, as rBergLib/BlackScholes.cpp:38-41 does).  The 32 lanes
-// price 32 volatilities at once: first a geometric grid 1e-3 * 2^(l/2) to
-// bracket the root, then 33-section rounds of the bracket (the price is
-// increasing in sigma, ~33x narrower per round) down to 1e-6 relative, then
-// Newton on the log price inside the bracket to 1e-15.  The search is a chain
-// of serial FP64 evaluations on GB300's slow FP64 pipe, so fewer rounds is
-// what makes it fast.  All lanes return the same value; NaN when no
-// volatility fits.
+// price 32 volatilities at once:
+//   1. a geometric grid 1e-3 * 2^(l/2) in FP64 brackets the root (or shows
+//      there is none) within a factor sqrt(2);
+//   2. three 33-section rounds in FP32 narrow the bracket ~36,000-fold (FP32
+//      resolves it no further);
+//   3. one FP64 step checks the narrowed bracket (lanes 0 and 1 price its
+//      ends, widened by 1e-6) while lane 2 prices its middle, the first Newton
+//      point; if the check fails -- FP32 cannot resolve the price, e.g. far in
+//      a wing -- FP64 33-section rounds narrow the grid bracket to 1e-6 instead;
+//   4. Newton on the log price inside the bracket to 1e-15.
+// The search is a chain of serial FP64 evaluations on GB300's slow FP64 pipe,
+// so fewer of them is what makes it fast: the FP32 rounds replace four.  All
+// lanes return the same value; NaN when no volatility fits.
 __device__ double implied_vol_warp(double price, double K, double T)
 {
     const unsigned FULL = 0xffffffffu;
@@ -668,16 +684,44 @@ __device__ double implied_vol_warp(double price, double K, double T)
     int f = __ffs(b) - 1;
     double lo = (f > 0) ? 1e-3 * exp2(0.5 * (f - 1)) : 0.0;
     double hi = 1e-3 * exp2(0.5 * f);
-    // 33-section rounds (one evaluation per lane) until the bracket is within
-    // 1e-6 relative, where Newton converges quadratically
-    for (int it = 0; it < 14 && hi - lo > 1e-6 * hi; ++it) {
-        const double s = lo + (hi - lo) * (double)(lane + 1) / 33.0;
-        b = __ballot_sync(FULL, bs_gen(K, T, s, put) >= target);
-        f = b ? __ffs(b) - 1 : 32;
-        const double nlo = __shfl_sync(FULL, s, f > 0 ? f - 1 : 0);
-        const double nhi = __shfl_sync(FULL, s, f < 32 ? f : 31);
-        if (f > 0) lo = nlo;
-        if (f < 32) hi = nhi;
+    // FP32 33-section rounds
+    const float lnK1 = (float)log(1.0 / K), sqT32 = (float)sqrt(T), K32 = (float)K, t32 = (float)target;
+    float lo32 = (float)lo, hi32 = (float)hi;
+#pragma unroll 1
+    for (int it = 0; it < 3; ++it) {
+        const float s = fmaf(hi32 - lo32, (float)(lane + 1) * (1.0f / 33.0f), lo32);
+        const unsigned bb = __ballot_sync(FULL, bs_gen_f32(lnK1, sqT32, K32, s, put) >= t32);
+        const int ff = bb ? __ffs(bb) - 1 : 32;
+        const float nlo = __shfl_sync(FULL, s, ff > 0 ? ff - 1 : 0);
+        const float nhi = __shfl_sync(FULL, s, ff < 32 ? ff : 31);
+        if (ff > 0) lo32 = nlo;
+        if (ff < 32) hi32 = nhi;
+    }
+    // the FP64 check of the narrowed bracket, with the first Newton point
+    const double lo2 = fmax(lo, (double)lo32 * (1.0 - 1e-6)), hi2 = fmin(hi, (double)hi32 * (1.0 + 1e-6));
+    const double sv = lane == 0 ? lo2 : (lane == 1 ? hi2 : 0.5 * (lo2 + hi2));
+    const double pv = (sv > 0.0) ? bs_gen(K, T, sv, put) : 0.0;  // zero volatility: the OTM price is 0
+    const double plo = __shfl_sync(FULL, pv, 0), phi_ = __shfl_sync(FULL, pv, 1), pmid = __shfl_sync(FULL, pv, 2);
+    const bool narrowed = lo2 < hi2 && plo < target && phi_ >= target;
+    double s, p0 = 0.0;
+    if (narrowed) {
+        lo = lo2;
+        hi = hi2;
+        s = 0.5 * (lo2 + hi2);
+        p0 = pmid;
+    } else {
+        // FP64 33-section rounds (one evaluation per lane) until the bracket
+        // is within 1e-6 relative, where Newton converges quadratically
+        for (int it = 0; it < 14 && hi - lo > 1e-6 * hi; ++it) {
+            const double sl = lo + (hi - lo) * (double)(lane + 1) / 33.0;
+            b = __ballot_sync(FULL, bs_gen(K, T, sl, put) >= target);
+            f = b ? __ffs(b) - 1 : 32;
+            const double nlo = __shfl_sync(FULL, sl, f > 0 ? f - 1 : 0);
+            const double nhi = __shfl_sync(FULL, sl, f < 32 ? f : 31);
+            if (f > 0) lo = nlo;
+            if (f < 32) hi = nhi;
+        }
+        s = 0.5 * (lo + hi);
     }
     // safeguarded Newton on the log price (every lane computes the same
     // iterate).  A Newton step below 1e-14 relative ends the search: the
@@ -685,9 +729,8 @@ __device__ double implied_vol_warp(double price, double K, double T)
     // step that leaves the bracket, or a vanishing price, falls back to
     // bisection; 40 halvings take a 1e-6 bracket below 1e-15 on their own.
     const double lt = log(target), sqT = sqrt(T);
-    double s = 0.5 * (lo + hi);
     for (int it = 0; it < 40; ++it) {
-        const double p = bs_gen(K, T, s, put);
+        const double p = (it == 0 && narrowed) ? p0 : bs_gen(K, T, s, put);
         if (p == target) break;
         if (p > target) hi = s;
         else lo = s;

@@ -119,8 +119,8 @@ struct SobolBridge {
     int m;
 };
 // Z [B][2][N] for points s0 .. s0 + B - 1; Vt = [kSobolBits][2N] on the
-// device; br = nullptr: no bridge; f32: the mixed form's FP32 normals (no
-// bridge), widened to double.  Returns nonzero when the bridge's shared
+// device; br = nullptr: no bridge; f32: the mixed form's FP32 normals (FP32
+// quantile, and the bridge in FP32), widened to double.  Returns nonzero when the bridge's shared
 // memory cannot be granted.
 int launch_sobol_normals(const unsigned long long* Vt, int N, uint64_t s0, int64_t B, const SobolBridge* br,
                          double* Z, void* stream, int f32 = 0);

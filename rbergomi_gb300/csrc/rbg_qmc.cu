@@ -1,4 +1,4 @@
-// rbg_qmc.cu -- Sobol' quasi-Monte Carlo normals for the FP64 form.
+// rbg_qmc.cu -- Sobol' quasi-Monte Carlo normals (FP64 form; FP32 for the mixed form).
 //
 // Restates
 //   rBergomi/rBergomiMT.cpp:669-670 (ComputePriceRTMT_sobol): path m takes
@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 
 #include "rbg_device.cuh"
 #include "rbg_internal.hpp"
@@ -75,33 +76,56 @@ __global__ void k_sobol_normals(const unsigned long long* __restrict__ Vt, int N
 
 // The same, then each stream through the hierarchical map; one block per
 // path, the path's 2N normals staged in shared memory.  The sum runs in the
-// reference's order, dW[i] = c0 Z[0] + sum_n (c_n w) Z[index], with every
-// product and sum rounded separately (no contraction into FMA).
+// reference's order, dW[i] = c0 Z[0] + sum_n (c_n w) Z[index].  FP64 (the FP64
+// form): every product and sum rounded separately (no contraction into FMA).
+// F32 (the mixed form): the FP32 quantile of each coordinate's top 32 bits and
+// the same sum in FP32, widened exactly to double -- GB300's FP64 pipe made the
+// FP64 map the whole cost of the mixed form's bridged pricing.
+template <bool F32>
 __global__ void k_sobol_bridge(const unsigned long long* __restrict__ Vt, int N, unsigned long long s0, int64_t B,
                                const __grid_constant__ SobolBridge br, double* __restrict__ Z)
 {
-    extern __shared__ double zs[];  // [2][N]
+    using T = typename std::conditional<F32, float, double>::type;
+    extern __shared__ double zs_raw[];  // [2][N] of T
+    T* zs = reinterpret_cast<T*>(zs_raw);
     for (int64_t b = blockIdx.x; b < B; b += gridDim.x) {
         for (int j = threadIdx.x; j < N; j += blockDim.x) {
-            double x0, x1;
-            sobol_pair(Vt, N, s0 + (unsigned long long)b, j, x0, x1);
-            zs[j] = normcdfinv(x0);
-            zs[N + j] = normcdfinv(x1);
+            unsigned long long q0, q1;
+            sobol_pair_q(Vt, N, s0 + (unsigned long long)b, j, q0, q1);
+            if (F32) {
+                zs[j] = (T)sobol_normal_f32((unsigned int)(q0 >> 30));
+                zs[N + j] = (T)sobol_normal_f32((unsigned int)(q1 >> 30));
+            } else {
+                zs[j] = (T)normcdfinv(__ull2double_rn(q0) * 0x1p-62);
+                zs[N + j] = (T)normcdfinv(__ull2double_rn(q1) * 0x1p-62);
+            }
         }
         __syncthreads();
         double* z = Z + (size_t)b * 2 * N;
         for (int i = threadIdx.x; i < N; i += blockDim.x) {
 #pragma unroll
             for (int st = 0; st < 2; ++st) {
-                const double* y = zs + st * N;
-                double w = __dmul_rn(br.c[0], y[0]);
-                for (int n = 1; n <= br.m; ++n) {
-                    const int i2nm = i >> (br.m - n);  // floor(i 2^(n - m))
-                    const int iota = (i2nm + 1) & 1;
-                    const int index = (1 << (n - 1)) + ((i2nm + iota + 1) >> 1) - 1;
-                    w = __dadd_rn(w, __dmul_rn(iota ? br.c[n] : -br.c[n], y[index]));
+                const T* y = zs + st * N;
+                T w;
+                if (F32) {
+                    w = (T)br.c[0] * y[0];
+                    for (int n = 1; n <= br.m; ++n) {
+                        const int i2nm = i >> (br.m - n);  // floor(i 2^(n - m))
+                        const int iota = (i2nm + 1) & 1;
+                        const int index = (1 << (n - 1)) + ((i2nm + iota + 1) >> 1) - 1;
+                        const T cn = (T)br.c[n];
+                        w = fmaf(iota ? cn : -cn, y[index], w);
+                    }
+                } else {
+                    w = __dmul_rn(br.c[0], y[0]);
+                    for (int n = 1; n <= br.m; ++n) {
+                        const int i2nm = i >> (br.m - n);
+                        const int iota = (i2nm + 1) & 1;
+                        const int index = (1 << (n - 1)) + ((i2nm + iota + 1) >> 1) - 1;
+                        w = __dadd_rn(w, __dmul_rn(iota ? br.c[n] : -br.c[n], y[index]));
+                    }
                 }
-                z[st * N + i] = w;
+                z[st * N + i] = (double)w;
             }
         }
         __syncthreads();
@@ -124,14 +148,14 @@ int launch_sobol_normals(const unsigned long long* Vt, int N, uint64_t s0, int64
         else
             k_sobol_normals<false><<<(unsigned)blocks, 256, 0, st>>>(Vt, N, (unsigned long long)s0, B, Z);
     } else {
-        const size_t smem = sizeof(double) * 2 * (size_t)N;
+        const size_t smem = (f32 ? sizeof(float) : sizeof(double)) * 2 * (size_t)N;
+        auto kern = f32 ? k_sobol_bridge<true> : k_sobol_bridge<false>;
         if (smem > 48 * 1024 &&
-            cudaFuncSetAttribute(k_sobol_bridge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-                cudaSuccess)
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return -1;
         const int threads = N >= 256 ? 256 : ((N + 31) / 32) * 32;
         const int64_t blocks = B < (int64_t)sms * 8 ? B : (int64_t)sms * 8;
-        k_sobol_bridge<<<(unsigned)blocks, threads, smem, st>>>(Vt, N, (unsigned long long)s0, B, *br, Z);
+        kern<<<(unsigned)blocks, threads, smem, st>>>(Vt, N, (unsigned long long)s0, B, *br, Z);
     }
     count_launch();
     return 0;

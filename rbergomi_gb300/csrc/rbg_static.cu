@@ -180,9 +180,10 @@ int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price
                                nchunks, st);
         launch_accumulate((const double*)(s + off_part), nchunks, n_out, (double*)(s + off_acc), st);
     }
-    if ((rc = mixed_check(job, s + off_ws, st, err))) return fail_queued(rc, err);
     launch_finalize((const double*)(s + off_acc), n_out, p->M, (const OutDev*)(s + off_outs),
                     (const double*)(s + off_T), o->compute_iv, (double*)(s + off_res), st);
+    // the error word after the finalize is queued: one wait for the whole call
+    if ((rc = mixed_check(job, s + off_ws, st, err))) return fail_queued(rc, err);
     std::vector<double> res(5 * (size_t)n_out);
     e = cudaGetLastError();
     if (e == cudaSuccess)

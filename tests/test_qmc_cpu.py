@@ -98,15 +98,19 @@ def test_live_reference_generator(oracle, V):
         np.testing.assert_array_equal(oracle.hier(z), oracle.qmc_ref_hier(z))
 
 
-def test_sobol_entry_rejects_unsupported_forms():
+def test_sobol_entry_takes_every_mixed_form():
+    """The mixed form takes the bridge and the FFT backend on Sobol' points
+    (the normals are materialized); no host-side refusal precedes the device
+    work, which this container cannot run.  A malformed table is refused
+    before any call."""
     import rbergomi_gb300 as R
 
     V = np.zeros((8, 62), np.uint64)
     a = (0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 4, 16, V)
-    with pytest.raises(R.RbgError, match="FP64 form only"):
-        R.price_rt_sobol(*a, bridge=True, precision=R.MIXED)
-    with pytest.raises(R.RbgError, match="GEMM backend"):
-        R.price_rt_sobol(*a, precision=R.MIXED, conv=R.CONV_FFT)
+    for kw in (dict(bridge=True, precision=R.MIXED), dict(precision=R.MIXED, conv=R.CONV_FFT)):
+        with pytest.raises(R.RbgError) as e:
+            R.price_rt_sobol(*a, **kw)
+        assert "FP64 form only" not in str(e.value) and "GEMM backend" not in str(e.value)
     with pytest.raises(ValueError):
         R.price_rt_sobol(0.04, [0.1], [1.5], [-0.7], [1.0], [1.0], 4, 16, np.zeros((8, 63), np.uint64))
 

@@ -3,7 +3,9 @@
 Direction integers: the reference's own (rBergomi/sobol.cpp), recovered from
 its points in tests/golden/sobol.npz (valid for point indices below 2^24).
 Normals: CUDA's FP64 normcdfinv against the oracle's quantile, a few ulps.
-Prices: the FP64 pipeline on identical normals, 1e-12 relative."""
+Prices: the FP64 pipeline on identical normals, 1e-12 relative; the mixed
+form (producer-drawn or materialized points, with or without the bridge, on
+either backend) within its 1e-4 relative / 0.2 standard-error bounds."""
 import os
 
 import numpy as np
@@ -112,6 +114,62 @@ def test_mixed_form_path_offset(R, V):
         q2, _, _ = R.price_rt_sobol(*a, precision=R.FP64, path_offset=off)
         assert np.all(rel_err(p2, q2) < 1e-4)
         assert np.all(np.abs(p2 - q2) < 0.2 * s2)
+
+
+@pytest.mark.parametrize("N,M", [(64, 4096), (256, 8192)])
+def test_mixed_bridge_matches_fp64_bridge(R, V, N, M):
+    """The Brownian bridge in the mixed form: the FP64 form's bridged
+    normals, materialized on the device and read in FP32 by the tensor-core
+    path kernel, price within the mixed form's bounds of the FP64 bridge."""
+    g = GRID
+    a = (g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, M, V)
+    p64, s64, _ = R.price_rt_sobol(*a, bridge=True, precision=R.FP64)
+    p32, s32, _ = R.price_rt_sobol(*a, bridge=True, precision=R.MIXED)
+    assert np.all(rel_err(p32, p64) < 1e-4)
+    assert np.all(np.abs(p32 - p64) < 0.2 * s64)
+    # the bridge changes the estimate: not the unbridged points' prices
+    q32, _, _ = R.price_rt_sobol(*a, precision=R.MIXED)
+    assert np.all(p32 != q32)
+
+
+@pytest.mark.parametrize("N", [100, 512])
+def test_mixed_sobol_on_the_fft_backend(R, V, N):
+    """The FFT backend on Sobol' points: the same FP32 normals the GEMM
+    producer draws, materialized; both backends within the mixed bounds of
+    the FP64 form and of each other."""
+    g = GRID
+    a = (g["xi"], g["H"], g["eta"], g["rho"], g["T"], g["K"], N, 6000, V)
+    p64, s64, _ = R.price_rt_sobol(*a, precision=R.FP64)
+    pg, _, _ = R.price_rt_sobol(*a, precision=R.MIXED)
+    pf, sf, _ = R.price_rt_sobol(*a, precision=R.MIXED, conv=R.CONV_FFT)
+    for p in (pg, pf):
+        assert np.all(rel_err(p, p64) < 1e-4)
+        assert np.all(np.abs(p - p64) < 0.2 * s64)
+    assert np.all(rel_err(pf, pg) < 1e-4)
+
+
+def synthetic_directions(dims, seed=5):
+    """Any 62-bit integers define a digital point set by the same Gray-code
+    rule (not a low-discrepancy one): enough to check that both forms price
+    the same points beyond the reference table's 1111 dimensions and 2^24
+    points."""
+    rng = np.random.default_rng(seed)
+    hi = rng.integers(0, 1 << 31, size=(dims, 62), dtype=np.uint64)
+    lo = rng.integers(0, 1 << 31, size=(dims, 62), dtype=np.uint64)
+    return (hi << np.uint64(31)) | lo
+
+
+@pytest.mark.parametrize("N,M,off", [(1536, 3000, 0), (64, 4096, (1 << 32) + 5)])
+def test_mixed_sobol_materialized_matches_fp64(R, N, M, off):
+    """Past the GEMM producer's range -- more than 1024 steps (multi-pass
+    tiles), point indices beyond 2^32 -- the mixed form materializes the
+    points' FP32 normals and prices them within its bounds of the FP64 form."""
+    Vs = synthetic_directions(2 * N)
+    a = (0.04, [0.1, 0.3], [1.5, 2.0], [-0.7, -0.9], [1.0, 2.0], [1.0, 0.9], N, M, Vs)
+    p64, s64, _ = R.price_rt_sobol(*a, precision=R.FP64, path_offset=off)
+    p32, _, _ = R.price_rt_sobol(*a, precision=R.MIXED, path_offset=off)
+    assert np.all(rel_err(p32, p64) < 1e-4)
+    assert np.all(np.abs(p32 - p64) < 0.2 * s64)
 
 
 def test_rejects_bad_requests(R, V):
