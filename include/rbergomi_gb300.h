@@ -174,8 +174,13 @@ int rbg_price_rt_unordered(const rbg_unordered* u, const rbg_options* o, double*
  *   var(Y), X the RT payoff, Y = BS(S, K, 1, sqrt(rho^2 (Q - Ivdt)));
  *   main: M paths, each the mean of X + alpha Y at W and at -W (Q_max where
  *   Q <= Ivdt), then price -= alpha E[Y] in closed form.
- * FP64.  Pilot normals come from Philox paths 2^62 + path_offset + m, main
- * normals from paths path_offset + m. */
+ * Pilot normals come from Philox paths 2^62 + path_offset + m, main normals
+ * from paths path_offset + m.  o->precision RBG_FP64: every stage in FP64.
+ * RBG_MIXED: the pilot in FP64 on FP32 normals, the main paths through the
+ * tensor-core path kernel (twice: W, and -W by the negated variance
+ * exponent) and FP32 payoffs with FP64 sums; the FP64 form with
+ * o->normals = RBG_NORMALS_F32 draws the same normals.  The caller-normals
+ * entry below is FP64 only. */
 typedef struct rbg_cv_params {
     const double* xi;
     const double* H;

@@ -574,13 +574,101 @@ static int price_cv(Ctx& c, const Plan& plan, const rbg_cv_params& p, const rbg_
     return RBG_OK;
 }
 
+// Control-variate estimator in the mixed form: the pilot in FP64 on the
+// mixed form's FP32 normals (the same alpha and Q as the FP64 form with
+// RBG_NORMALS_F32), the main paths through the tensor-core path kernel twice
+// per batch -- as is, then with the variance exponent's coefficient negated,
+// which prices the antithetic paths -W exactly -- with xi = 0 in the kernel's
+// final sums, since each tuple carries its own xi (added back per group by the
+// FP32 control-variate payoff kernel).
+static int price_cv_mixed(Ctx& c, const Plan& plan, const rbg_cv_params& p, const rbg_options& o, cudaStream_t st,
+                          double* host_res)
+{
+    TableSet ts;
+    int logL = 0;
+    int rc = fp64_conv_log2(RBG_CONV_AUTO, plan.N, &logL);
+    if (rc) return rc;
+    if ((rc = upload_tables(c, plan, st, ts, logL))) return rc;
+    const int no = (int)plan.outs.size(), N = plan.N, ng = (int)plan.vgs.size();
+    const int64_t Mc = p.M_control, M = p.M;
+    if (Mc > fp64_batch(plan, Mc, 2)) return fail(RBG_ERR_ARG, "M_control too large for one pilot batch");
+    MixedJob job;
+    if ((rc = mixed_prepare(plan, o, M, job, g_err, 0, false))) return rc;
+    if (job.fused) return fail(RBG_ERR_UNSUPPORTED, "the control-variate estimator needs the unfused path kernel");
+    const int64_t B = job.batch;
+    const int G = payoff_paths_per_thread(B, job.sms);
+    const int64_t max_chunks = (B + 256 * (int64_t)G - 1) / (256 * (int64_t)G);
+    if ((rc = ensure(c.z, sizeof(double) * 2 * N * (size_t)Mc, "pilot normals"))) return rc;
+    if ((rc = ensure(c.ivp, sizeof(double) * 2 * ng * (size_t)Mc, "pilot sums"))) return rc;
+    if ((rc = ensure(c.ivb, sizeof(float) * 4 * ng * (size_t)B, "variance sums"))) return rc;
+    const size_t cv_bytes = sizeof(double) * (size_t)no * (2 * (size_t)Mc + 2) + sizeof(unsigned long long) * no;
+    if ((rc = ensure(c.cv, cv_bytes, "control-variate scratch"))) return rc;
+    if ((rc = ensure(c.mixed_ws, job.workspace_bytes, "mixed workspace"))) return rc;
+    if ((rc = ensure(c.part, sizeof(double) * 4 * no * (size_t)max_chunks, "partials"))) return rc;
+    if ((rc = ensure(c.acc, sizeof(double) * 4 * no, "accumulators"))) return rc;
+    if ((rc = ensure(c.res, sizeof(double) * 5 * no, "results"))) return rc;
+    double* alpha = c.cv.as<double>();
+    double* Q = alpha + no;
+    unsigned long long* count = (unsigned long long*)(Q + no);
+    double* xy = (double*)(count + no);
+    // pilot: one FP64 batch of Mc paths on FP32 normals
+    launch_normals(o.seed, kCvPilotPath0 + o.path_offset, Mc, N, 1, c.z.as<double>(), st);
+    launch_path_fp64(ts.t, c.z.as<double>(), Mc, c.ivp.as<double>(), st);
+    launch_cv_pilot(ts.t, c.ivp.as<double>(), Mc, xy, alpha, Q, st);
+    RBG_CUDA(cudaMemsetAsync(count, 0, sizeof(unsigned long long) * no, st));
+    RBG_CUDA(cudaMemsetAsync(c.acc.p, 0, sizeof(double) * 4 * no, st));
+    // main paths: the job as is and its antithetic twin, both with xi = 0 in the final sums
+    for (MixedLaunch& L : job.launches) L.args.xi = L.args.sqrt_xi = 0.f;
+    MixedJob anti = job;
+    for (MixedLaunch& L : anti.launches)
+        for (int g = 0; g < L.args.n_g; ++g) L.args.alpha[g] = -L.args.alpha[g];
+    if (c.mixed_img != job.host_ws) {
+        c.mixed_img.clear();
+        if ((rc = mixed_upload(job, c.mixed_ws.p, st, g_err))) return rc;
+        c.mixed_img = job.host_ws;
+    } else {
+        RBG_CUDA(cudaMemsetAsync((unsigned char*)c.mixed_ws.p + job.off_err, 0, 4, st));
+    }
+    float2* ivb = c.ivb.as<float2>();
+    float2* ivn = ivb + (size_t)ng * B;
+    for (int64_t m0 = 0; m0 < M; m0 += B) {
+        const int64_t b = std::min(B, M - m0);
+        {
+            ProfScope ps(kStageMixed, st, 2 * (int)job.launches.size());
+            if ((rc = mixed_launch(job, c.mixed_ws.p, o.seed, o.path_offset + m0, b, ivb, st, g_err))) return rc;
+            if ((rc = mixed_launch(anti, c.mixed_ws.p, o.seed, o.path_offset + m0, b, ivn, st, g_err))) return rc;
+        }
+        const int nchunks = (int)((b + 256 * (int64_t)G - 1) / (256 * (int64_t)G));
+        {
+            ProfScope ps(kStagePayoff, st);
+            launch_payoff_sums_cv_f32(ts.t.outs, ts.t.vgs, no, ivb, ivn, b, G, o.seed, o.path_offset + m0, alpha, Q,
+                                      p.Q_max, c.part.as<double>(), count, nchunks, st);
+        }
+        {
+            ProfScope ps(kStageReduce, st);
+            launch_accumulate(c.part.as<double>(), nchunks, no, c.acc.as<double>(), st);
+        }
+        RBG_CUDA(cudaGetLastError());
+    }
+    launch_finalize_cv(c.acc.as<double>(), no, M, ts.t.outs, ts.Tvals, alpha, Q, count, p.Q_max, o.compute_iv,
+                       c.res.as<double>(), st);
+    RBG_CUDA(cudaGetLastError());
+    if ((rc = mixed_check(job, c.mixed_ws.p, st, g_err))) return rc;
+    RBG_CUDA(cudaMemcpyAsync(host_res, c.res.p, sizeof(double) * 5 * no, cudaMemcpyDeviceToHost, st));
+    RBG_CUDA(cudaStreamSynchronize(st));
+    prof_collect();
+    return RBG_OK;
+}
+
 static int price_cv_any(const rbg_cv_params* p, const rbg_options* o, const double* Zc, const double* Z,
                         std::vector<double>& res)
 {
     if (!p || !o) return fail(RBG_ERR_ARG, "null params/options");
     if (!p->xi) return fail(RBG_ERR_ARG, "null xi array");
     if (p->M_control < 2) return fail(RBG_ERR_ARG, "M_control must be >= 2");
-    if (o->precision != RBG_FP64) return fail(RBG_ERR_UNSUPPORTED, "the control-variate estimator runs in FP64");
+    if (o->precision != RBG_FP64 && o->precision != RBG_MIXED) return fail(RBG_ERR_ARG, "unknown precision");
+    if (o->precision == RBG_MIXED && (Zc || Z))
+        return fail(RBG_ERR_UNSUPPORTED, "the control-variate estimator on caller normals runs in FP64");
     g_h2d = g_d2h = 0;
     rbg_unordered u{p->xi[0], p->H, p->eta, p->rho, p->T, p->K, p->size, p->N, p->M};
     Plan plan;
@@ -593,6 +681,7 @@ static int price_cv_any(const rbg_cv_params* p, const rbg_options* o, const doub
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
     res.assign(5 * plan.outs.size(), 0.0);
+    if (o->precision == RBG_MIXED) return price_cv_mixed(*c, plan, *p, *o, st, res.data());
     return price_cv(*c, plan, *p, *o, Zc, Z, st, res.data());
 }
 

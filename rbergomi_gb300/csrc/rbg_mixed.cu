@@ -1656,6 +1656,129 @@ void launch_payoff_store_f32(const OutDev* outs, int n_out, const void* ivb, con
     count_launch();
 }
 
+// ------------------------------------------- control variate, FP32 payoffs
+// The Romano-Touzi estimator with the McCrickerd-Pakkanen control variate on
+// antithetic paths (ML_console_ST/RBergomi.cpp:218-306), priced from the
+// mixed path kernel's FP32 sums: f = X + alpha Y with X = BS(spot, K,
+// sqrt((1 - rho^2) Ivdt)) and Y = BS(spot, K, sqrt(rho^2 (Q - Ivdt))) -- Q_max
+// in place of Q where Q <= Ivdt, counted -- averaged over W and -W.
+__device__ __forceinline__ float cv_half_f32(float Ivdt, float IsvdW, float rho, float K, float lnK, float alpha,
+                                             float Q, float Qmax, unsigned& exc)
+{
+    const RtSpot r = rt_spot_f32(Ivdt, IsvdW, rho);
+    const float x = rt_payoff_f32(r, K, lnK);
+    const bool inside = Q > Ivdt;
+    if (!inside) ++exc;
+    RtSpot ry = r;
+    const float v2 = rho * rho * ((inside ? Q : Qmax) - Ivdt);
+    ry.deg = !(v2 > 0.0f);
+    ry.rv = rsqrt_approx(v2);
+    ry.vol = v2 * ry.rv;
+    return fmaf(alpha, rt_payoff_f32(ry, K, lnK), x);
+}
+
+// One block per (chunk c of 256 G paths, 8 outputs), as k_payoff_sums_f32.
+// The path kernel ran twice with xi = 0 in its final sums: ivb with the
+// variance exponent's coefficient as is, ivn with it negated, which is the
+// antithetic path -W exactly (X is linear in the normals, so X(-W) = -X(W)).
+// Per group g and path: Ivdt = raw.x + dt xi_g; IsvdW = raw.y + sdt sqrt(xi_g)
+// W1_0 for W and -(raw.y + sdt sqrt(xi_g) W1_0) for -W, W1_0 redrawn from the
+// path's Philox stream (the path kernel's first W1).
+__global__ void __launch_bounds__(256) k_payoff_sums_cv_f32(const OutDev* __restrict__ outs,
+                                                            const VGDev* __restrict__ vgs, int n_out,
+                                                            const float2* __restrict__ ivb,
+                                                            const float2* __restrict__ ivn, int64_t B, int G,
+                                                            uint64_t seed, int64_t path0,
+                                                            const double* __restrict__ alpha,
+                                                            const double* __restrict__ Q, float Qmax,
+                                                            double* __restrict__ part,
+                                                            unsigned long long* __restrict__ count)
+{
+    __shared__ double red[8][kOPB32][2];
+    const int c = blockIdx.x, o0 = blockIdx.y * kOPB32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float rho[kOPB32], K[kOPB32], lnK[kOPB32], al[kOPB32], qq[kOPB32];
+    int vg[kOPB32];
+    unsigned exc[kOPB32];
+#pragma unroll
+    for (int q = 0; q < kOPB32; ++q) {
+        const int i = o0 + q;
+        const OutDev od = (i < n_out) ? outs[i] : OutDev{0.0, 1.0, -1, 0};
+        rho[q] = (float)od.rho; K[q] = (float)od.K; lnK[q] = logf((float)od.K); vg[q] = od.vg;
+        al[q] = (i < n_out) ? (float)alpha[i] : 0.f;
+        qq[q] = (i < n_out) ? (float)Q[i] : 0.f;
+        exc[q] = 0;
+    }
+    const PhiloxKeys keys = philox_keys(seed);
+    float s1[kOPB32], s2[kOPB32];
+#pragma unroll
+    for (int q = 0; q < kOPB32; ++q) { s1[q] = 0.f; s2[q] = 0.f; }
+    for (int sub = 0; sub < G; ++sub) {
+        const int64_t m = ((int64_t)c * G + sub) * 256 + threadIdx.x;
+        if (m >= B) break;
+        const uint4 x0 = philox_group(keys, (uint64_t)(path0 + m), 0u, 0u);
+        float w10, w11;
+        box_muller_f32(x0.x, x0.y, w10, w11);
+        int cur = -1;
+        float ipx = 0.f, ipy = 0.f, inx = 0.f, iny = 0.f;
+#pragma unroll
+        for (int q = 0; q < kOPB32; ++q) {
+            if (vg[q] < 0) continue;
+            if (vg[q] != cur) {
+                cur = vg[q];
+                const VGDev gd = vgs[cur];
+                const float dtxi = (float)(gd.dt * gd.xi), c0 = (float)(gd.sdt * sqrt(gd.xi)) * w10;
+                const float2 rp = ivb[(size_t)cur * B + m], rn = ivn[(size_t)cur * B + m];
+                ipx = rp.x + dtxi;
+                ipy = rp.y + c0;
+                inx = rn.x + dtxi;
+                iny = -(rn.y + c0);
+            }
+            const float x = 0.5f * (cv_half_f32(ipx, ipy, rho[q], K[q], lnK[q], al[q], qq[q], Qmax, exc[q]) +
+                                    cv_half_f32(inx, iny, rho[q], K[q], lnK[q], al[q], qq[q], Qmax, exc[q]));
+            s1[q] += x;
+            s2[q] = fmaf(x, x, s2[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kOPB32; ++q) {
+        float a = s1[q], b = s2[q];
+        unsigned e = exc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+            e += __shfl_xor_sync(0xffffffffu, e, o);
+        }
+        if (lane == 0) {
+            red[w][q][0] = (double)a;
+            red[w][q][1] = (double)b;
+            if (e && o0 + q < n_out) atomicAdd(count + o0 + q, (unsigned long long)e);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < kOPB32 && o0 + (int)threadIdx.x < n_out) {
+        const int q = threadIdx.x;
+        double S = 0, CS = 0, S2 = 0, CS2 = 0;
+        for (int k = 0; k < 8; ++k) {
+            neumaier_add(S, CS, red[k][q][0]);
+            neumaier_add(S2, CS2, red[k][q][1]);
+        }
+        double* pp = part + ((size_t)c * n_out + o0 + q) * 4;
+        pp[0] = S; pp[1] = CS; pp[2] = S2; pp[3] = CS2;
+    }
+}
+
+void launch_payoff_sums_cv_f32(const OutDev* outs, const VGDev* vgs, int n_out, const void* ivb, const void* ivn,
+                               int64_t B, int G, uint64_t seed, int64_t path0, const double* alpha, const double* Q,
+                               double Qmax, double* part, unsigned long long* count, int nchunks, cudaStream_t st)
+{
+    const dim3 grid((unsigned)nchunks, (unsigned)((n_out + kOPB32 - 1) / kOPB32));
+    k_payoff_sums_cv_f32<<<grid, 256, 0, st>>>(outs, vgs, n_out, (const float2*)ivb, (const float2*)ivn, B, G, seed,
+                                                path0, alpha, Q, (float)Qmax, part, count);
+    count_launch();
+}
+
 // Failure-detection check: one warp waits, through the pricing kernels'
 // bounded-wait helper, on an mbarrier that nothing arrives on, with a 20 ms
 // limit; the expiry records `site` in the error word, as a pipeline wait
@@ -1969,7 +2092,6 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     }
     std::vector<unsigned char>& ws = job.host_ws;
     ws.assign(off, 0);
-    const double lnxi = std::log(plan.xi);
     for (const MixedLaunch& r : job.launches) {
         const MixedArgs& A = r.args;
         const int vol = plan.vgs[A.g0].vol;
@@ -1994,11 +2116,14 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             }
         }
         float* beta = (float*)(ws.data() + r.off_beta);
-        for (int g = 0; g < A.n_g; ++g)
+        for (int g = 0; g < A.n_g; ++g) {
+            // the group's forward variance: the plan's, or the tuple's own in the control-variate form
+            const double lnxi = std::log(plan.vgs[A.g0 + g].xi);
             for (int j = 0; j < Np; ++j) {
                 const double cj = (j < N) ? plan.comp[(size_t)(A.g0 + g) * N + j] : 0.0;
                 beta[(size_t)g * Np + j] = (float)(0.5 * (cj - lnxi) * log2e);
             }
+        }
     }
     job.workspace_bytes = off;
     // batch: float2 per (variance group, path) within 1 GiB

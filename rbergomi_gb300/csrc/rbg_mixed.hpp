@@ -159,4 +159,12 @@ int mixed_jobs_prepare(const std::vector<MixedJobRef>& jobs, void* table, unsign
 // Launches the path kernel over every job's tiles (grid: mixed_jobs_prepare's CTA count).
 int mixed_launch_jobs(const MixedArgs& launch_args, int split, int grid, cudaStream_t st, std::string& errmsg);
 
+// Control-variate payoff sums from two path-kernel runs with xi = 0 in their
+// final sums, the second with the variance exponent's coefficient negated
+// (the antithetic paths): per chunk (S, C, S2, C2) of 0.5 (f(W) + f(-W)), the
+// Q_max exceptions counted per output.  alpha, Q: the pilot's, per output.
+void launch_payoff_sums_cv_f32(const OutDev* outs, const VGDev* vgs, int n_out, const void* ivb, const void* ivn,
+                               int64_t B, int G, uint64_t seed, int64_t path0, const double* alpha, const double* Q,
+                               double Qmax, double* part, unsigned long long* count, int nchunks, cudaStream_t st);
+
 }  // namespace rbg
