@@ -424,10 +424,12 @@ const char* rbg_server_last_error(void);
  * message from rbg_static_last_error() otherwise); M is unbounded (paths are
  * processed in batches that fit, cut at the same payoff-chunk boundaries as
  * rbg_price_rt's, so prices agree to FP64 roundoff).  A NULL o->stream runs
- * on the calling thread's per-thread default stream.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress) and
- * should come before any stream capture; the address is kept for the life
- * of the process, so cudaDeviceReset between calls is not supported.  All
+ * on the calling thread's per-thread default stream.  Every call
+ * synchronises its stream before returning (it reads the results back), so
+ * it cannot be recorded under stream capture.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); the address is
+ * kept for the life of the process, so cudaDeviceReset between calls is not
+ * supported.  All
  * calls share the array and see the previous call's contents; each call
  * clears what must start at zero.  Calls that overlap on the GPU race on the
  * array: serialise them.  A call that fails after queuing work waits for

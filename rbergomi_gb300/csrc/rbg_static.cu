@@ -11,10 +11,10 @@
 // loads this library holds until the process exits.
 //
 // The device address of that array is looked up once per device, with the
-// device current, on the first call on that device (cudaGetSymbolAddress);
-// that first call should therefore come before any stream capture.  The
-// address stays cached for the life of the process, so a cudaDeviceReset
-// between calls is not supported.  All calls share the array and it keeps
+// device current, on the first call on that device (cudaGetSymbolAddress).
+// The address stays cached for the life of the process, so a cudaDeviceReset
+// between calls is not supported.  Every call synchronises its stream to
+// return the prices, so none can run under stream capture.  All calls share the array and it keeps
 // the last call's contents; what must start at zero (the kernel error word
 // and the running sums) is cleared by every call.  Calls whose work overlaps
 // on the GPU race on the array, so callers serialise them (one stream, or
