@@ -207,3 +207,28 @@ def test_mixed_extreme_strikes(R):
     rel = np.abs(mp - fp) / fp
     assert np.all(rel[fp > 1e-5] < 1e-4)
     assert np.all(np.abs(mp - fp) < 0.2 * fs)
+
+
+def test_repeated_calls_reuse_the_plan(R):
+    """A mixed call with the inputs of the last one (another seed or path
+    offset) skips planning and uploads; its results equal a call that plans
+    afresh, including after other calls changed what the device holds."""
+    a = (CFG2["xi"], CFG2["H"], CFG2["eta"], CFG2["rho"], CFG2["T"], CFG2["K"], 512, 20000)
+    b = (GRID["xi"], GRID["H"], GRID["eta"], GRID["rho"], GRID["T"], GRID["K"], 300, 9000)
+    first = R.price_rt(*a, seed=5, precision=R.MIXED)
+    again = R.price_rt(*a, seed=5, precision=R.MIXED)                 # same inputs: the cached plan
+    other_seed = R.price_rt(*a, seed=6, precision=R.MIXED)            # cached plan, another stream
+    R.price_rt(*b, seed=5, precision=R.MIXED)                         # another plan and images
+    after_other = R.price_rt(*a, seed=5, precision=R.MIXED)
+    R.price_rt(*a, seed=5, precision=R.FP64)                          # the FP64 form's tables
+    after_fp64 = R.price_rt(*a, seed=5, precision=R.MIXED)
+    shard = R.price_rt(*a, seed=5, precision=R.MIXED, path_offset=20000)
+    for r in (again, after_other, after_fp64):
+        for x, y in zip(first, r):
+            np.testing.assert_array_equal(x, y)
+    assert np.all(other_seed[0] != first[0]) and np.all(shard[0] != first[0])
+    # another seed through a freshly planned call gives the cached call's bits
+    R.price_rt(*b, seed=5, precision=R.MIXED)
+    fresh = R.price_rt(*a, seed=6, precision=R.MIXED)
+    for x, y in zip(other_seed, fresh):
+        np.testing.assert_array_equal(x, y)
