@@ -54,6 +54,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <set>
 #include <mutex>
 
 #include "rbg_device.cuh"
@@ -1877,43 +1878,49 @@ float to_tf32(float f)
 // 32-byte SW32 row).
 void build_strip(const double* gamma, int N, int Np, int sk, unsigned char* img)
 {
-    if (sk == 2) {
-        const size_t half = (size_t)strip_bytes_t32(Np) / 2;
-        std::memset(img, 0, 2 * half);
-        for (int r = 0; r < Np + kLeadT; ++r)
-            for (int k = 0; k < kStripKT; ++k) {
-                const int d = r - kLeadT - k;
-                const double gv = (d >= 0 && d < N) ? gamma[d] : 0.0;
-                const float hi = to_tf32((float)gv);
-                const float lo = to_tf32((float)(gv - (double)hi));
-                const size_t off = (size_t)r * 32 + ((((k >> 2) ^ ((r >> 2) & 1))) << 4) + (k & 3) * 4;
-                std::memcpy(img + off, &hi, 4);
-                std::memcpy(img + half + off, &lo, 4);
-            }
-        return;
-    }
-    const int bf16 = sk;
-    const size_t half = (size_t)strip_bytes(Np) / 2;
-    std::memset(img, 0, 2 * half);
-    const bool wide = strip_k(Np) == kChunk;
-    const int rows = wide ? Np : Np + kStripK, kw = wide ? kChunk : kStripK, lead = wide ? 0 : kStripK;
-    for (int r = 0; r < rows; ++r)
-        for (int k = 0; k < kw; ++k) {
-            const int d = r - lead - k;
-            const double gv = (d >= 0 && d < N) ? gamma[d] : 0.0;
-            uint16_t hi, lo;
-            if (bf16) {
-                hi = to_bf16((float)gv);
-                lo = to_bf16((float)(gv - (double)from_bf16(hi)));
-            } else {
-                hi = to_f16((float)gv);
-                lo = to_f16((float)(gv - (double)from_f16(hi)));
-            }
-            const int sw = wide ? ((r >> 1) & 3) : ((r >> 2) & 1);
-            const size_t off = (size_t)r * kw * 2 + ((((k >> 3) ^ sw)) << 4) + (k & 7) * 2;
-            std::memcpy(img + off, &hi, 2);
-            std::memcpy(img + half + off, &lo, 2);
+    // Row r of every strip form holds Gamma[r - lead - k] for k = 0 .. kw - 1,
+    // in 16-byte chunks of consecutive k permuted by the row's swizzle.  Along
+    // a chunk the Gamma index falls by one per element, so each chunk is a
+    // 16-byte run of the hi / lo values in reversed order: the N distinct
+    // values are split once and every chunk is one copy (the element-wise
+    // build took ~100 us at N = 512, as much as the rest of a call's planning).
+    const int esz = (sk == 2) ? 4 : 2;                        // bytes per element
+    const bool wide = sk != 2 && strip_k(Np) == kChunk;
+    const int kw = (sk == 2) ? kStripKT : (wide ? kChunk : kStripK);
+    const int lead = (sk == 2) ? kLeadT : (wide ? 0 : kStripK);
+    const int rows = wide ? Np : Np + lead;
+    const int per = 16 / esz;                                 // elements per chunk
+    const size_t half = (size_t)rows * kw * esz;
+    // reversed, zero-padded: rev[pad + i] holds Gamma[N - 1 - i] (i in [0, N))
+    const int pad = kw + lead + 32;
+    std::vector<unsigned char> rh((size_t)(N + 2 * pad) * esz, 0), rl((size_t)(N + 2 * pad) * esz, 0);
+    for (int d = 0; d < N; ++d) {
+        const size_t at = (size_t)(pad + N - 1 - d) * esz;
+        if (sk == 2) {
+            const float hi = to_tf32((float)gamma[d]);
+            const float lo = to_tf32((float)(gamma[d] - (double)hi));
+            std::memcpy(&rh[at], &hi, 4);
+            std::memcpy(&rl[at], &lo, 4);
+        } else {
+            const uint16_t hi = sk ? to_bf16((float)gamma[d]) : to_f16((float)gamma[d]);
+            const uint16_t lo = sk ? to_bf16((float)(gamma[d] - (double)from_bf16(hi)))
+                                   : to_f16((float)(gamma[d] - (double)from_f16(hi)));
+            std::memcpy(&rh[at], &hi, 2);
+            std::memcpy(&rl[at], &lo, 2);
         }
+    }
+    std::memset(img, 0, 2 * half);
+    for (int r = 0; r < rows; ++r) {
+        // the swizzle of row r: SW64 (wide) XORs the chunk with (r / 2) mod 4, SW32 with (r / 4) mod 2
+        const int sw = wide ? ((r >> 1) & 3) : ((r >> 2) & 1);
+        for (int c = 0; c < kw / per; ++c) {
+            // chunk c covers k = per c .. per c + per - 1: Gamma indices r - lead - per c down by one
+            const int i0 = N - 1 - (r - lead - per * c);  // rev index of its first element
+            const size_t src = (size_t)(pad + i0) * esz, dst = (size_t)r * kw * esz + (size_t)((c ^ sw) * 16);
+            std::memcpy(img + dst, &rh[src], 16);
+            std::memcpy(img + half + dst, &rl[src], 16);
+        }
+    }
 }
 
 }  // namespace
@@ -1965,6 +1972,26 @@ void mixed_twiddle_range(const MixedJob& job, size_t* off, size_t* bytes)
 {
     *off = job.off_tw;
     *bytes = (job.backend == RBG_CONV_FFT && !job.launches.empty()) ? (size_t)job.launches[0].args.L * 8 : 0;
+}
+
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum, once per (device, kernel): every launch then takes any size the
+// planner accepted, with no attribute call on the launch path.
+static cudaError_t allow_max_smem(void (*kern)(MixedArgs))
+{
+    static std::mutex mu;
+    static std::set<std::pair<int, void (*)(MixedArgs)>> done;
+    DevInfo dv;
+    int dev = 0;
+    if (!device_info(&dv) || cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return cudaErrorInvalidDevice;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({dev, kern})) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dv.optin);
+    if (e == cudaSuccess) done.insert({dev, kern});
+    return e;
 }
 
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
@@ -2248,7 +2275,7 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
                 kern = job.mc ? gemm_kernel<true, 2>(sk, pm) : gemm_kernel<false, 2>(sk, pm);
             else
                 kern = job.mc ? gemm_kernel<true, 0>(sk, pm) : gemm_kernel<false, 0>(sk, pm);
-            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            e = allow_max_smem(kern);
             if (e == cudaSuccess) kern<<<grid, kThreads, smem, st>>>(A);
         }
         if (e == cudaSuccess) e = cudaGetLastError();
@@ -2355,7 +2382,7 @@ int mixed_launch_jobs(const MixedArgs& A, int split, int grid, cudaStream_t st, 
     const int sk = split_kind(split);
     void (*kern)(MixedArgs) = sk == 0 ? k_mixed_gemm_jobs<0> : (sk == 1 ? k_mixed_gemm_jobs<1> : k_mixed_gemm_jobs<2>);
     const int smem = smem_layout(A.Np, A.stages, A.n_g, 0, 2, sk == 2).total;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = allow_max_smem(kern);
     if (e == cudaSuccess) {
         kern<<<grid, kThreads, smem, st>>>(A);
         e = cudaGetLastError();
