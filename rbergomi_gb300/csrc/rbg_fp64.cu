@@ -657,18 +657,22 @@ __device__ __forceinline__ float bs_gen_f32(float lnK1, float sqT, float K, floa
 // Implied vol by a warp: inverts on the out-of-the-money side (put-call
 // parity for K < 1, as rBergLib/BlackScholes.cpp:38-41 does).  The 32 lanes
 // price 32 volatilities at once:
-//   1. a geometric grid 1e-3 * 2^(l/2) in FP64 brackets the root (or shows
-//      there is none) within a factor sqrt(2);
+//   1. a geometric grid 1e-3 * 2^(l/2) brackets the root within a factor
+//      sqrt(2), in FP32; where the FP32 grid brackets nothing, the same grid in
+//      FP64 decides (no bracket there: no volatility fits, NaN);
 //   2. three 33-section rounds in FP32 narrow the bracket ~36,000-fold (FP32
 //      resolves it no further);
 //   3. one FP64 step checks the narrowed bracket (lanes 0 and 1 price its
-//      ends, widened by 1e-6) while lane 2 prices its middle, the first Newton
-//      point; if the check fails -- FP32 cannot resolve the price, e.g. far in
-//      a wing -- FP64 33-section rounds narrow the grid bracket to 1e-6 instead;
-//   4. Newton on the log price inside the bracket to 1e-15.
+//      ends, widened by 1e-6) while lane 2 prices its middle; if the check
+//      fails -- FP32 cannot resolve the price, e.g. far in a wing -- the FP64
+//      grid and FP64 33-section rounds (to 1e-6) take over;
+//   4. from the checked bracket's middle one Halley step on the log price
+//      (cubic: from a 1e-5 bracket the error left is 1e-15 near the money,
+//      below ~1e-12 in the wings), then safeguarded Newton on the
+//      log price where a step is still larger than that.
 // The search is a chain of serial FP64 evaluations on GB300's slow FP64 pipe,
-// so fewer of them is what makes it fast: the FP32 rounds replace four.  All
-// lanes return the same value; NaN when no volatility fits.
+// so fewer of them is what makes it fast: two on the common path.  All lanes
+// return the same value; NaN when no volatility fits.
 __device__ double implied_vol_warp(double price, double K, double T)
 {
     const unsigned FULL = 0xffffffffu;
@@ -678,40 +682,50 @@ __device__ double implied_vol_warp(double price, double K, double T)
     const double upper = put ? K : 1.0;
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
     if (!(target > 0.0) || !(target < upper) || !(T > 0.0)) return nan;
-    double sig = 1e-3 * exp2(0.5 * lane);
-    unsigned b = __ballot_sync(FULL, bs_gen(K, T, sig, put) >= target);
-    if (b == 0u) return nan;
-    int f = __ffs(b) - 1;
-    double lo = (f > 0) ? 1e-3 * exp2(0.5 * (f - 1)) : 0.0;
-    double hi = 1e-3 * exp2(0.5 * f);
-    // FP32 33-section rounds
     const float lnK1 = (float)log(1.0 / K), sqT32 = (float)sqrt(T), K32 = (float)K, t32 = (float)target;
-    float lo32 = (float)lo, hi32 = (float)hi;
+    double lo = 0.0, hi = 0.0;
+    bool narrowed = false;
+    double s = 0.0, p0 = 0.0;
+    {
+        // FP32 grid and rounds, then the FP64 check
+        const unsigned b32 = __ballot_sync(FULL, bs_gen_f32(lnK1, sqT32, K32, 1e-3f * exp2f(0.5f * lane), put) >= t32);
+        if (b32 != 0u) {
+            const int f = __ffs(b32) - 1;
+            const double glo = (f > 0) ? 1e-3 * exp2(0.5 * (f - 1)) : 0.0, ghi = 1e-3 * exp2(0.5 * f);
+            float lo32 = (float)glo, hi32 = (float)ghi;
 #pragma unroll 1
-    for (int it = 0; it < 3; ++it) {
-        const float s = fmaf(hi32 - lo32, (float)(lane + 1) * (1.0f / 33.0f), lo32);
-        const unsigned bb = __ballot_sync(FULL, bs_gen_f32(lnK1, sqT32, K32, s, put) >= t32);
-        const int ff = bb ? __ffs(bb) - 1 : 32;
-        const float nlo = __shfl_sync(FULL, s, ff > 0 ? ff - 1 : 0);
-        const float nhi = __shfl_sync(FULL, s, ff < 32 ? ff : 31);
-        if (ff > 0) lo32 = nlo;
-        if (ff < 32) hi32 = nhi;
+            for (int it = 0; it < 3; ++it) {
+                const float sl = fmaf(hi32 - lo32, (float)(lane + 1) * (1.0f / 33.0f), lo32);
+                const unsigned bb = __ballot_sync(FULL, bs_gen_f32(lnK1, sqT32, K32, sl, put) >= t32);
+                const int ff = bb ? __ffs(bb) - 1 : 32;
+                const float nlo = __shfl_sync(FULL, sl, ff > 0 ? ff - 1 : 0);
+                const float nhi = __shfl_sync(FULL, sl, ff < 32 ? ff : 31);
+                if (ff > 0) lo32 = nlo;
+                if (ff < 32) hi32 = nhi;
+            }
+            const double lo2 = fmax(glo, (double)lo32 * (1.0 - 1e-6)), hi2 = fmin(ghi, (double)hi32 * (1.0 + 1e-6));
+            const double sv = lane == 0 ? lo2 : (lane == 1 ? hi2 : 0.5 * (lo2 + hi2));
+            const double pv = (sv > 0.0) ? bs_gen(K, T, sv, put) : 0.0;  // zero volatility: the OTM price is 0
+            const double plo = __shfl_sync(FULL, pv, 0), phi_ = __shfl_sync(FULL, pv, 1);
+            const double pmid = __shfl_sync(FULL, pv, 2);
+            if (lo2 < hi2 && plo < target && phi_ >= target) {
+                narrowed = true;
+                lo = lo2;
+                hi = hi2;
+                s = 0.5 * (lo2 + hi2);
+                p0 = pmid;
+            }
+        }
     }
-    // the FP64 check of the narrowed bracket, with the first Newton point
-    const double lo2 = fmax(lo, (double)lo32 * (1.0 - 1e-6)), hi2 = fmin(hi, (double)hi32 * (1.0 + 1e-6));
-    const double sv = lane == 0 ? lo2 : (lane == 1 ? hi2 : 0.5 * (lo2 + hi2));
-    const double pv = (sv > 0.0) ? bs_gen(K, T, sv, put) : 0.0;  // zero volatility: the OTM price is 0
-    const double plo = __shfl_sync(FULL, pv, 0), phi_ = __shfl_sync(FULL, pv, 1), pmid = __shfl_sync(FULL, pv, 2);
-    const bool narrowed = lo2 < hi2 && plo < target && phi_ >= target;
-    double s, p0 = 0.0;
-    if (narrowed) {
-        lo = lo2;
-        hi = hi2;
-        s = 0.5 * (lo2 + hi2);
-        p0 = pmid;
-    } else {
-        // FP64 33-section rounds (one evaluation per lane) until the bracket
-        // is within 1e-6 relative, where Newton converges quadratically
+    if (!narrowed) {
+        // FP64 grid, then FP64 33-section rounds (one evaluation per lane)
+        // until the bracket is within 1e-6 relative
+        const double sig = 1e-3 * exp2(0.5 * lane);
+        unsigned b = __ballot_sync(FULL, bs_gen(K, T, sig, put) >= target);
+        if (b == 0u) return nan;
+        int f = __ffs(b) - 1;
+        lo = (f > 0) ? 1e-3 * exp2(0.5 * (f - 1)) : 0.0;
+        hi = 1e-3 * exp2(0.5 * f);
         for (int it = 0; it < 14 && hi - lo > 1e-6 * hi; ++it) {
             const double sl = lo + (hi - lo) * (double)(lane + 1) / 33.0;
             b = __ballot_sync(FULL, bs_gen(K, T, sl, put) >= target);
@@ -723,14 +737,30 @@ __device__ double implied_vol_warp(double price, double K, double T)
         }
         s = 0.5 * (lo + hi);
     }
+    const double lt = log(target), sqT = sqrt(T);
+    if (narrowed && p0 > 0.0) {
+        // Halley on g(s) = log p(s) - log target: g' = vega / p and
+        // g'' = (vomma p - vega^2) / p^2 with vomma = vega d1 d2 / s
+        const double d1 = (log(1.0 / K) + 0.5 * s * s * T) / (s * sqT);
+        const double d2 = d1 - s * sqT;
+        const double vega = exp(-0.5 * d1 * d1) * 0.39894228040143267794 * sqT;
+        const double g = log(p0) - lt, g1 = vega / p0, g2 = (vega * d1 * d2 / s) / p0 - g1 * g1;
+        const double nt = s - 2.0 * g * g1 / (2.0 * g1 * g1 - g * g2);
+        if (nt > lo && nt < hi) {
+            if (fabs(nt - s) <= 1e-5 * s) return nt;  // cubic: the error left is below ~1e-12 relative
+            s = nt;
+        }
+        if (p0 > target) hi = 0.5 * (lo + hi);
+        else lo = 0.5 * (lo + hi);
+        if (!(s > lo && s < hi)) s = 0.5 * (lo + hi);
+    }
     // safeguarded Newton on the log price (every lane computes the same
     // iterate).  A Newton step below 1e-14 relative ends the search: the
     // convergence is quadratic, so the iterate it gives is at roundoff.  A
     // step that leaves the bracket, or a vanishing price, falls back to
     // bisection; 40 halvings take a 1e-6 bracket below 1e-15 on their own.
-    const double lt = log(target), sqT = sqrt(T);
     for (int it = 0; it < 40; ++it) {
-        const double p = (it == 0 && narrowed) ? p0 : bs_gen(K, T, s, put);
+        const double p = bs_gen(K, T, s, put);
         if (p == target) break;
         if (p > target) hi = s;
         else lo = s;

@@ -74,3 +74,39 @@ def test_mixed_corners_vs_fp64_identical_normals(R, conv):
     assert np.all(err[big] <= 1e-4 * fp[big])
     assert np.all(err <= 0.2 * fs + 1e-12)
     assert np.all(np.abs(ms[big] / fs[big] - 1) < 1e-3)
+
+
+def test_implied_vol_sweep_vs_oracle(R, oracle):
+    """The GPU implied-vol search (FP32 bracketing, FP64 check, Halley and
+    Newton steps on the log price, FP64 fallback) against the oracle's FP64
+    root on 4,000 call prices from K in [0.3, 3], T in [0.01, 5] and vols in
+    [0.01, 3], out-of-the-money values down to 1e-12 -- where FP32 cannot
+    resolve the price the search falls back to FP64 -- plus prices with no
+    volatility (NaN in both)."""
+    from scipy.stats import norm
+
+    rng = np.random.default_rng(4)
+    n = 4000
+    K = np.exp(rng.uniform(np.log(0.3), np.log(3.0), n))
+    T = np.exp(rng.uniform(np.log(0.01), np.log(5.0), n))
+    sig = np.exp(rng.uniform(np.log(0.01), np.log(3.0), n))
+    d1 = (np.log(1.0 / K) + 0.5 * sig * sig * T) / (sig * np.sqrt(T))
+    d2 = d1 - sig * np.sqrt(T)
+    otm = np.where(K < 1.0, K * norm.cdf(-d2) - norm.cdf(-d1), norm.cdf(d1) - K * norm.cdf(d2))
+    keep = otm > 1e-12
+    K, T, sig, otm = K[keep], T[keep], sig[keep], otm[keep]
+    price = np.where(K < 1.0, otm + 1.0 - K, otm)  # call prices
+    # and a few with no volatility: below intrinsic, at or above the spot
+    price = np.concatenate([price, [0.3, 1.0, 1.5, 0.05]])
+    K = np.concatenate([K, [0.5, 1.0, 0.9, 1.2]])
+    T = np.concatenate([T, [1.0, 1.0, 1.0, 0.0]])
+    iv = R.implied_vol(price, K, T)
+    ivo = np.array([oracle.iv_call(p, k, t) for p, k, t in zip(price, K, T)])
+    ok = ~np.isnan(ivo)
+    np.testing.assert_array_equal(np.isnan(iv), ~ok)
+    assert ok.sum() >= len(sig) - 5
+    assert np.all(rel_err(iv[ok], ivo[ok]) < 1e-10)
+    # the generating vols, where the call price carries the OTM value to many digits
+    m = len(sig)
+    good = ok[:m] & (otm > 1e-6)
+    assert np.all(rel_err(iv[:m][good], sig[good]) < 1e-6)
