@@ -173,22 +173,41 @@ struct Ctx {
     ~Ctx() {}
 };
 
+// One context per (device, caller stream): its own buffers, device tables,
+// plan cache and lock, so calls on different streams run concurrently and
+// only calls on one stream (which that stream orders anyway) wait for each
+// other.  A NULL stream maps to a context with the library's own
+// non-blocking stream.  Contexts live until the process exits.
 static std::mutex g_ctx_mu;
-static std::map<int, std::unique_ptr<Ctx>> g_ctx;
+static std::map<std::pair<int, void*>, std::unique_ptr<Ctx>> g_ctx;
 
-static int get_ctx(Ctx** out)
+static int get_ctx(Ctx** out, void* stream = nullptr)
 {
     int dev = 0;
     RBG_CUDA(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lk(g_ctx_mu);
-    auto& slot = g_ctx[dev];
+    auto& slot = g_ctx[{dev, stream}];
     if (!slot) {
         std::unique_ptr<Ctx> c(new Ctx());
         c->dev = dev;
-        RBG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        if (stream)
+            c->stream = (cudaStream_t)stream;
+        else
+            RBG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
         slot = std::move(c);
     }
     *out = slot.get();
+    return RBG_OK;
+}
+
+// Every context of the current device (rbg_synchronize, rbg_release).
+static int device_ctxs(std::vector<Ctx*>& out)
+{
+    int dev = 0;
+    RBG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    for (auto& kv : g_ctx)
+        if (kv.first.first == dev) out.push_back(kv.second.get());
     return RBG_OK;
 }
 
@@ -525,7 +544,7 @@ static int price_mixed(Ctx& c, const Plan& plan, const rbg_options& o, int64_t M
 static int price_plan(const Plan& plan, int64_t M, const rbg_options* o, std::vector<double>& res, bool mc = false)
 {
     Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    int rc = get_ctx(&c, o->stream);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
@@ -564,7 +583,7 @@ static std::vector<unsigned char> mixed_key(const rbg_params& p, const rbg_optio
 static int price_mixed_cached(const rbg_params& p, const rbg_options& o, std::vector<double>& res, bool mc)
 {
     Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    int rc = get_ctx(&c, o.stream);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o.stream ? (cudaStream_t)o.stream : c->stream;
@@ -769,7 +788,7 @@ static int price_cv_any(const rbg_cv_params* p, const rbg_options* o, const doub
     if (p->size > 0 && !build_plan_unordered(u, plan, err, p->xi, 1)) return fail(RBG_ERR_ARG, err);
     if (p->size <= 0) return fail(RBG_ERR_ARG, "size must be positive");
     Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    int rc = get_ctx(&c, o->stream);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
@@ -786,7 +805,7 @@ static int payoffs_quadrature(const rbg_params* p, const double* Z, double* payo
     if (!build_plan(*p, plan, err, mc)) return fail(RBG_ERR_ARG, err);
     if (!Z || !payoff) return fail(RBG_ERR_ARG, "null Z/payoff");
     Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    int rc = get_ctx(&c, user_stream);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = user_stream ? user_stream : c->stream;
@@ -840,7 +859,7 @@ static int payoffs_quadrature_mixed(const rbg_params* p, const rbg_options& o, c
     if (!build_plan(*p, plan, err, mc)) return fail(RBG_ERR_ARG, err);
     if (!Z || !payoff) return fail(RBG_ERR_ARG, "null Z/payoff");
     Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    int rc = get_ctx(&c, o.stream);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o.stream ? (cudaStream_t)o.stream : c->stream;
@@ -1154,7 +1173,7 @@ int rbg_price_rt_sobol(const rbg_params* p, const rbg_options* o, const uint64_t
     std::string err;
     if (!build_plan(*p, plan, err, false)) return fail(RBG_ERR_ARG, err);
     Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    int rc = get_ctx(&c, o->stream);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
@@ -1231,22 +1250,31 @@ int rbg_synchronize(void)
     Ctx* c = nullptr;
     int rc = get_ctx(&c);
     if (rc) return rc;
-    RBG_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<Ctx*> all;
+    if ((rc = device_ctxs(all))) return rc;
+    for (Ctx* x : all) RBG_CUDA(cudaStreamSynchronize(x->stream));
     return RBG_OK;
 }
 
 int rbg_release(void)
 {
-    Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    Ctx* c0 = nullptr;
+    int rc = get_ctx(&c0);
     if (rc) return rc;
-    std::lock_guard<std::mutex> lk(c->mu);
-    RBG_CUDA(cudaStreamSynchronize(c->stream));
-    for (DevBuf* b : {&c->z, &c->ivb, &c->ivp, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws, &c->cv})
-        b->release();
-    c->tabs_img.clear();
-    c->mixed_img.clear();
-    ++c->img_gen;
+    std::vector<Ctx*> all;
+    if ((rc = device_ctxs(all))) return rc;
+    for (Ctx* c : all) {
+        std::lock_guard<std::mutex> lk(c->mu);
+        RBG_CUDA(cudaStreamSynchronize(c->stream));
+        for (DevBuf* b : {&c->z, &c->ivb, &c->ivp, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws,
+                          &c->cv, &c->sobol, &c->sobol32})
+            b->release();
+        c->tabs_img.clear();
+        c->mixed_img.clear();
+        c->sobol_img.clear();
+        c->sobol32_img.clear();
+        ++c->img_gen;
+    }
     return RBG_OK;
 }
 
@@ -1258,7 +1286,7 @@ int rbg_debug_mixed_paths(const rbg_params* p, const rbg_options* o, float* norm
     if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
     if (p->M > (1 << 20)) return fail(RBG_ERR_ARG, "diagnostic runs are limited to 2^20 paths");
     Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    int rc = get_ctx(&c, o->stream);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;
@@ -1348,7 +1376,7 @@ int rbg_debug_mixed_profile(const rbg_params* p, const rbg_options* o, uint64_t*
     std::string err;
     if (!build_plan(*p, plan, err)) return fail(RBG_ERR_ARG, err);
     Ctx* c = nullptr;
-    int rc = get_ctx(&c);
+    int rc = get_ctx(&c, o->stream);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
     cudaStream_t st = o->stream ? (cudaStream_t)o->stream : c->stream;

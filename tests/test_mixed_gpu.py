@@ -232,3 +232,34 @@ def test_repeated_calls_reuse_the_plan(R):
     fresh = R.price_rt(*a, seed=6, precision=R.MIXED)
     for x, y in zip(other_seed, fresh):
         np.testing.assert_array_equal(x, y)
+
+
+def test_calls_on_two_streams_from_two_threads(R):
+    """Host threads pricing on different CUDA streams hold separate library
+    contexts (buffers, tables, plan cache, lock) and run side by side; each
+    result equals the same call made alone."""
+    import threading
+
+    import torch
+
+    a = (CFG2["xi"], CFG2["H"], CFG2["eta"], CFG2["rho"], CFG2["T"], CFG2["K"], 512, 30000)
+    b = (GRID["xi"], GRID["H"], GRID["eta"], GRID["rho"], GRID["T"], GRID["K"], 300, 20000)
+    want_a = R.price_rt(*a, seed=3, precision=R.MIXED)
+    want_b = R.price_rt(*b, seed=4, precision=R.MIXED)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    got = {}
+
+    def run(key, args, seed, stream):
+        torch.cuda.set_device(0)
+        got[key] = [R.price_rt(*args, seed=seed, precision=R.MIXED, stream=stream.cuda_stream) for _ in range(3)]
+
+    th = [threading.Thread(target=run, args=("a", a, 3, s1)), threading.Thread(target=run, args=("b", b, 4, s2))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for key, want in (("a", want_a), ("b", want_b)):
+        assert len(got[key]) == 3
+        for r in got[key]:
+            for x, y in zip(r, want):
+                np.testing.assert_array_equal(x, y)
