@@ -593,8 +593,13 @@ def serve_stream(args, local: int) -> dict:
     lat = np.zeros((len(reqs), 3))
     n0 = R.launch_count()
     with ClockSampler(local) as clk:
+        extra = {}
+        if args.slots:
+            extra["slots"] = args.slots
+        if args.high_slots is not None:
+            extra["high_priority_slots"] = args.high_slots
         with R.Server(use_graphs=0 if args.no_graphs else 1, batch_wait_us=args.batch_wait_us,
-                      batch_slots=args.batch_slots) as srv:
+                      batch_slots=args.batch_slots, **extra) as srv:
             tickets = [None] * len(reqs)
             ready = threading.Semaphore(0)
 
@@ -646,6 +651,7 @@ def serve_stream(args, local: int) -> dict:
     return {
         "workload": "serving-poisson", "requests": len(reqs), "rate_per_s": args.rate, "graphs": not args.no_graphs,
         "batch_wait_us": args.batch_wait_us, "batch_slots": args.batch_slots, "small_only": args.small_only,
+        "slots": args.slots or None, "high_priority_slots": args.high_slots,
         "p50_ms": float(np.percentile(total, 50)), "p99_ms": float(np.percentile(total, 99)),
         "max_ms": float(np.max(total)), "mean_ms": float(np.mean(total)),
         "queue_p99_ms": float(np.percentile(lat[:, 0], 99)), "service_p99_ms": float(np.percentile(lat[:, 1], 99)),
@@ -704,6 +710,8 @@ def main():
     ap.add_argument("--fp64-sample", type=int, default=20, help="serving: FP64 one-at-a-time sample size")
     ap.add_argument("--no-graphs", action="store_true", help="serving: launch without CUDA graphs")
     ap.add_argument("--batch-slots", type=int, default=8, help="serving: shared launches in flight (0: none)")
+    ap.add_argument("--slots", type=int, default=0, help="serving: request slots (0: the server's default)")
+    ap.add_argument("--high-slots", type=int, default=None, help="serving: high-priority request slots")
     ap.add_argument("--small-only", action="store_true",
                     help="serving: only requests shared launches price (N <= 512, M <= 2^17)")
     ap.add_argument("--batch-wait-us", type=float, default=0.0,

@@ -56,18 +56,22 @@ def test_cv_reduces_the_standard_error(R):
     assert s1[0] < 0.5 * srt[0]
 
 
-@pytest.mark.parametrize("N,M,Mc", [(100, 1 << 14, 2000), (512, 1 << 14, 2000), (1536, 8192, 1500), (64, 1 << 14, 40)])
-def test_mixed_cv_matches_fp64_cv_on_the_same_normals(R, N, M, Mc):
+@pytest.mark.parametrize("N,M,Mc,conv", [(100, 1 << 14, 2000, "auto"), (512, 1 << 14, 2000, "auto"),
+                                         (1536, 8192, 1500, "auto"), (64, 1 << 14, 40, "auto"),
+                                         (700, 8192, 1500, "fft")])
+def test_mixed_cv_matches_fp64_cv_on_the_same_normals(R, N, M, Mc, conv):
     """The mixed form of the control-variate estimator -- FP64 pilot, main
     paths through the tensor-core kernel as is and with the exponent negated
     (the antithetic paths), FP32 payoffs -- against the FP64 form on the same
     FP32 normals (RBG_NORMALS_F32): the same pilot alpha and Q, prices within
     1e-4 relative and 0.2 of their standard error.  One tuple xi each; one and
-    three TMEM passes; M_control = 40 sends paths through the Q_max branch."""
+    three TMEM passes and the FFT backend; M_control = 40 sends paths through
+    the Q_max branch."""
     xi, H, eta, rho = [0.04, 0.06, 0.05, 0.03], [0.07, 0.2, 0.35, 0.1], [1.9, 1.2, 2.4, 1.5], [-0.9, -0.5, -0.7, -0.8]
     T, K = [1.0, 0.5, 2.0, 0.25], [1.05, 0.95, 1.2, 1.0]
     p64, s64, iv64 = R.price_rt_cv(xi, H, eta, rho, T, K, N, M, M_control=Mc, seed=21, normals=R.NORMALS_F32)
-    p32, s32, iv32 = R.price_rt_cv(xi, H, eta, rho, T, K, N, M, M_control=Mc, seed=21, precision=R.MIXED)
+    p32, s32, iv32 = R.price_rt_cv(xi, H, eta, rho, T, K, N, M, M_control=Mc, seed=21, precision=R.MIXED,
+                                   conv=R.CONV_FFT if conv == "fft" else R.CONV_AUTO)
     assert np.all(rel_err(p32, p64) < 1e-4)
     assert np.all(np.abs(p32 - p64) < 0.2 * s64)
     assert np.all(rel_err(s32, s64) < 1e-2)
