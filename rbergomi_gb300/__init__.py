@@ -242,6 +242,35 @@ def price_rt(xi, H, eta, rho, T, K, N, M, **opts):
     return price, stat, iv
 
 
+class RtPricer:
+    """price_rt with its arguments marshalled once, for repeated calls on
+    one grid (a calibration or risk loop, a benchmark): each call passes the
+    same C structures and output arrays and changes only the seed, the path
+    offset or the stream.  With the library's plan cache (a call repeating
+    the previous call's inputs reuses its plan and device tables), a repeated
+    call costs the C call and the kernels.  The returned arrays are reused by
+    the next call: copy them to keep them."""
+
+    def __init__(self, xi, H, eta, rho, T, K, N, M, **opts):
+        self._p = _Params(xi, H, eta, rho, T, K, N, M)
+        self._o = options(**opts)
+        out = self._p.out
+        self.price, self.stat, self.iv = np.empty(out), np.empty(out), np.empty(out)
+        self._ptrs = (self.price.ctypes.data_as(_dp), self.stat.ctypes.data_as(_dp), self.iv.ctypes.data_as(_dp))
+        self._fn = lib().rbg_price_rt
+
+    def __call__(self, seed=None, path_offset=None, stream=None):
+        o = self._o
+        if seed is not None:
+            o.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        if path_offset is not None:
+            o.path_offset = int(path_offset)
+        if stream is not None:
+            o.stream = stream
+        _check(self._fn(C.byref(self._p.s), C.byref(o), *self._ptrs))
+        return self.price, self.stat, self.iv
+
+
 def price_rt_unordered(xi, H, eta, rho, T, K, N, M, **opts):
     """Unordered parameter list (the reference's ComputeIVRTMTunstructured,
     rBergomi/rBergomiMT.cpp:837-938): output i prices (H[i], eta[i], rho[i],

@@ -263,3 +263,15 @@ def test_calls_on_two_streams_from_two_threads(R):
         for r in got[key]:
             for x, y in zip(r, want):
                 np.testing.assert_array_equal(x, y)
+
+
+def test_prepared_pricer_equals_price_rt(R):
+    """RtPricer (arguments marshalled once) gives price_rt's results call by
+    call, seed and path offset changed between calls."""
+    a = (CFG2["xi"], CFG2["H"], CFG2["eta"], CFG2["rho"], CFG2["T"], CFG2["K"], 512, 20000)
+    pr = R.RtPricer(*a, precision=R.MIXED)
+    for seed, off in ((5, 0), (6, 0), (6, 20000), (5, 0)):
+        got = [x.copy() for x in pr(seed=seed, path_offset=off)]
+        want = R.price_rt(*a, seed=seed, path_offset=off, precision=R.MIXED)
+        for x, y in zip(got, want):
+            np.testing.assert_array_equal(x, y)
