@@ -1980,7 +1980,7 @@ void mixed_twiddle_range(const MixedJob& job, size_t* off, size_t* bytes)
 static cudaError_t allow_max_smem(void (*kern)(MixedArgs))
 {
     static std::mutex mu;
-    static std::set<std::pair<int, void (*)(MixedArgs)>> done;
+    static std::set<std::pair<int, uintptr_t>> done;  // (device, kernel address)
     DevInfo dv;
     int dev = 0;
     if (!device_info(&dv) || cudaGetDevice(&dev) != cudaSuccess) {
@@ -1988,9 +1988,10 @@ static cudaError_t allow_max_smem(void (*kern)(MixedArgs))
         return cudaErrorInvalidDevice;
     }
     std::lock_guard<std::mutex> lk(mu);
-    if (done.count({dev, kern})) return cudaSuccess;
+    const std::pair<int, uintptr_t> key{dev, reinterpret_cast<uintptr_t>(kern)};
+    if (done.count(key)) return cudaSuccess;
     const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dv.optin);
-    if (e == cudaSuccess) done.insert({dev, kern});
+    if (e == cudaSuccess) done.insert(key);
     return e;
 }
 
