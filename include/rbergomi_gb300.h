@@ -294,12 +294,12 @@ const char* rbg_last_error(void);
 /* Number of kernels this library has launched in this process. */
 uint64_t rbg_launch_count(void);
 
-/* Waits for every stream the library has priced on for the current device
- * (its own and each caller stream it has a context for). */
+/* Waits for the library's own stream on the current device (work a caller
+ * queued on its own streams is the caller's to wait for). */
 int rbg_synchronize(void);
 
-/* Releases the cached device buffers and tables of every context (one per
- * caller stream) of the current device. */
+/* Waits for the current device, then releases the cached device buffers and
+ * tables of every context (one per caller stream) on it. */
 int rbg_release(void);
 
 /* Host-only introspection of the ParamTot plan (no GPU needed): the number

@@ -1250,9 +1250,7 @@ int rbg_synchronize(void)
     Ctx* c = nullptr;
     int rc = get_ctx(&c);
     if (rc) return rc;
-    std::vector<Ctx*> all;
-    if ((rc = device_ctxs(all))) return rc;
-    for (Ctx* x : all) RBG_CUDA(cudaStreamSynchronize(x->stream));
+    RBG_CUDA(cudaStreamSynchronize(c->stream));
     return RBG_OK;
 }
 
@@ -1263,9 +1261,11 @@ int rbg_release(void)
     if (rc) return rc;
     std::vector<Ctx*> all;
     if ((rc = device_ctxs(all))) return rc;
+    // caller streams may be gone by now: wait for the device, not for each stream
+    std::vector<std::unique_lock<std::mutex>> locks;
+    for (Ctx* c : all) locks.emplace_back(c->mu);
+    RBG_CUDA(cudaDeviceSynchronize());
     for (Ctx* c : all) {
-        std::lock_guard<std::mutex> lk(c->mu);
-        RBG_CUDA(cudaStreamSynchronize(c->stream));
         for (DevBuf* b : {&c->z, &c->ivb, &c->ivp, &c->part, &c->acc, &c->tabs, &c->res, &c->pay, &c->mixed_ws,
                           &c->cv, &c->sobol, &c->sobol32})
             b->release();
