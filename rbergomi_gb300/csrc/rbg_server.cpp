@@ -74,6 +74,12 @@ constexpr size_t kPinOutputs = 4096;
 // and this many requests.
 constexpr int kBatchOutputs = (int)kPinOutputs;
 constexpr int kBatchJobsMax = 64;
+// Completion polling interval while work is in flight: on average half of it
+// is added to every request's latency.
+#ifndef RBG_SERVER_POLL_US
+#define RBG_SERVER_POLL_US 10
+#endif
+constexpr int kPollUs = RBG_SERVER_POLL_US;
 
 struct Req {
     uint64_t id = 0;
@@ -773,7 +779,7 @@ void Server::run()
         if (!progressed) {
             // poll the device quickly while work is in flight, sleep otherwise (until
             // the batching window closes, at the latest)
-            Clock::duration d = busy_now() ? Clock::duration(std::chrono::microseconds(50))
+            Clock::duration d = busy_now() ? Clock::duration(std::chrono::microseconds(kPollUs))
                                            : Clock::duration(std::chrono::milliseconds(5));
             if (wake != Clock::time_point::max()) d = std::min(d, std::max(Clock::duration(0), wake - Clock::now()));
             cv_work.wait_for(lk, d);
