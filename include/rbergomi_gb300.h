@@ -425,7 +425,12 @@ const char* rbg_server_last_error(void);
  * outputs, and the job's tables must fit the array (RBG_ERR_ARG with a
  * message from rbg_static_last_error() otherwise); M is unbounded (paths are
  * processed in batches that fit, cut at the same payoff-chunk boundaries as
- * rbg_price_rt's, so prices agree to FP64 roundoff).  A NULL o->stream runs
+ * rbg_price_rt's, so prices agree to FP64 roundoff).  One exception: for
+ * 512 < N <= 1024 with the 16-bit splits, rbg_price_rt's path kernel keeps
+ * A tiles in a per-CTA device cache (tens of MB) that the array cannot hold,
+ * so this entry runs the two-pass kernel that draws them again: the same
+ * products in another FP32 accumulation order, prices equal to within about
+ * 1e-6 relative.  A NULL o->stream runs
  * on the calling thread's per-thread default stream.  Every call
  * synchronises its stream before returning (it reads the results back), so
  * it cannot be recorded under stream capture.  The first call on a device

@@ -544,8 +544,9 @@ def debug_mixed_paths(xi, H, eta, rho, T, K, N, M, **opts):
 
 PROFILE_SITES = {1: "producer wait (free stage)", 2: "epilogue wait (MMA results)", 3: "MMA wait (strip load)",
                  4: "MMA wait (TMEM free)", 5: "MMA wait (A tile)", 7: "epilogue wait (producer tile)",
-                 8: "epilogue wait (next producer tile)", 16: "producer busy", 17: "epilogue busy", 18: "MMA busy",
-                 20: "epilogue fused payoffs"}
+                 8: "epilogue wait (next producer tile)", 9: "MMA wait (cached-tile slot free)",
+                 10: "MMA wait (cached tile)", 11: "MMA wait (A tile stored)", 12: "MMA wait (stores complete)",
+                 16: "producer busy", 17: "epilogue busy", 18: "MMA busy", 20: "epilogue fused payoffs"}
 
 
 def debug_mixed_profile(xi, H, eta, rho, T, K, N, M, **opts):

@@ -32,6 +32,11 @@
 // (W1 only, no epilogue work), then from its own chunks.  For two passes the
 // producers' chunk sequence per tile is
 //   [0, n0) real | [0, n0) redrawn | [n0, nc) real.
+// For the 16-bit splits and the RT estimator on Philox normals, 512 < Np <=
+// 1024 runs pass mode 3 instead (PassPlan): 256-column passes alternating
+// between two TMEM buffers, each chunk drawn once, the far-field of the next
+// pass accumulated in the other buffer from the chunks' A tiles that the MMA
+// thread keeps in a per-CTA global cache.
 // Up to Np = 1024 the whole narrow strip stays in shared memory.  Above that
 // (up to 4096, eight passes) only its first 528 rows do -- all that a chunk
 // drawn for real reads -- and each redrawn chunk brings the 528-row window it
@@ -74,6 +79,9 @@ constexpr int kMaxG = kMixedMaxGroups;
 #ifndef RBG_FUSE_PAYOFFS
 #define RBG_FUSE_PAYOFFS 0
 #endif
+#ifndef RBG_PASS3
+#define RBG_PASS3 1  // pass mode 3 for the two-pass range where it applies (0: the redrawing two-pass kernel)
+#endif
 constexpr int kProdWarps = RBG_PROD_WARPS;          // 4 * 128 / kProdWarps... threads per path: kProdWarps / 4
 constexpr int kEpiWarps = RBG_EPI_WARPS;            // 4 (one warpgroup) or 8 (two, 16 columns each per chunk)
 constexpr int kEpiWGs = kEpiWarps / 4;
@@ -85,6 +93,10 @@ constexpr int kPassCols = 512;                      // TMEM: 128 lanes x 512 FP3
 constexpr int kMaxNp = 2 * kPassCols;               // two passes with the whole narrow strip resident
 constexpr int kMaxNpMulti = 8 * kPassCols;          // up to eight passes with streamed strip windows
 constexpr int kStripK = 16;                         // narrow strip width: one K = 16 MMA step
+// Pass mode 3 (below): 256-column passes in two TMEM buffers, and slots for
+// the cached A tiles the far-field MMAs read.
+constexpr int kHalfCols = kPassCols / 2;
+constexpr int kCSlots = 3;
 constexpr int kHPerPath = kProdWarps * 32 / kTileM; // producer threads per path
 constexpr uint64_t kWaitNs = 2000000000ull;         // 2 s per wait
 
@@ -136,7 +148,7 @@ __host__ __device__ inline int strip_bytes(int Np)
 }
 
 struct SmemLayout {
-    int strip, a0, f0, fstride, stages, acc, beta, otab, osum, bars, total;
+    int strip, a0, f0, fstride, stages, cs, acc, beta, otab, osum, bars, total;
 };
 
 __host__ __device__ inline int strip_bytes_t32(int Np) { return 2 * (Np + kLeadT) * kStripKT * 4; }
@@ -158,7 +170,10 @@ __host__ __device__ inline int strip_smem_bytes_t32(int Np)
 // window (hi and lo halves), so it is at least 2 kWindowBytes (a multiple of
 // the 256-byte SW32 swizzle atom).
 // tf32: the TF32 strip geometry (split kind 2).
-__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, int n_o, int ns = 2, bool tf32 = false)
+// cslots: pass mode 3's slots for cached A tiles (1024-aligned, after the FP32
+// tiles; 0 in the other pass modes, whose layout it leaves unchanged).
+__host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, int n_o, int ns = 2, bool tf32 = false,
+                                                  int cslots = 0)
 {
     SmemLayout L;
     L.strip = 0;
@@ -168,12 +183,15 @@ __host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, i
     L.fstride = stage_f_bytes(ns);
     const int win2 = tf32 ? 2 * kWindowBytesT : 2 * kWindowBytes;
     if (pass_mode(Np) == 2 && L.fstride < win2) L.fstride = win2;
-    L.acc = L.f0 + stages * L.fstride;
-    L.beta = L.acc + 2 * n_g * ns * kTileM * 4 + (ns - 1) * kTileM * 4;  // per warpgroup, then W1_0 (Wperp_0)
+    L.cs = L.f0 + stages * L.fstride;
+    if (cslots > 0) L.cs = (L.cs + 1023) / 1024 * 1024;
+    L.acc = L.cs + cslots * kStageA;
+    // per warpgroup, then W1_0 (Wperp_0), then (pass mode 3) the deferred sqrt(v) per group
+    L.beta = L.acc + 2 * n_g * ns * kTileM * 4 + (ns - 1) * kTileM * 4 + (cslots > 0 ? n_g * kTileM * 4 : 0);
     L.otab = L.beta + n_g * Np * 4;
     L.osum = (L.otab + n_o * 16 + 15) / 16 * 16;
     L.bars = L.osum + kEpiWarps * n_o * 16;
-    L.total = L.bars + 128 + 1024;  // barriers + alignment slack for the dynamic base
+    L.total = L.bars + (cslots > 0 ? 256 : 128) + 1024;  // barriers + alignment slack for the dynamic base
     return L;
 }
 
@@ -217,6 +235,20 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                  : "memory");
 }
 
+// Bulk copy shared memory of this CTA -> global (16-byte aligned addresses, a
+// multiple of 16 bytes) as one bulk async-group of the issuing thread.
+__device__ __forceinline__ void bulk_s2g(void* dst, uint32_t src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// The issuing thread's bulk stores: every source read (read0), every store
+// complete (done0), or all but the most recent one complete (done1).
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_done0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_done1() { asm volatile("cp.async.bulk.wait_group 1;" ::: "memory"); }
+
 // One wait attempt; the hardware may suspend the thread for up to 20 us
 // (the suspend-time hint) until the phase completes, so waiting warps do not
 // spin on the issue slots the working roles need.
@@ -257,6 +289,15 @@ __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned i
     }
     if (prof && (threadIdx.x & 31) == 0) atomicAdd(prof + site, (unsigned long long)(clock64() - c0));
     return ok;
+}
+
+// Waits up to 10 ms for a phase whatever the error word says: a CTA winding
+// down after an error lets its own bulk copies in flight land before it exits.
+__device__ __noinline__ void mbar_drain(uint32_t bar, uint32_t parity)
+{
+    const uint64_t t0 = globaltimer();
+    while (!mbar_try(bar, parity) && globaltimer() - t0 < 10000000ull) {
+    }
 }
 
 // the same wait, made warp-uniform so .sync.aligned tcgen05 ops stay converged;
@@ -344,6 +385,27 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                  : "memory");
+}
+
+// The three split products of one chunk's 16-bit A tile (hi at ahi, lo
+// 8 KB above) against the narrow strip (hi / lo halves at bhi / blo) into n
+// TMEM columns from d, the first of which reads strip row jrow (K half ks
+// from row jrow + 16 - 16 ks).  overwrite: the first product replaces D.
+template <int SK>
+__device__ __forceinline__ void mma_chunk_narrow(uint32_t d, uint32_t ahi, uint32_t bhi, uint32_t blo, uint32_t jrow,
+                                                 int n, bool overwrite)
+{
+    const uint32_t id = idesc_f16(n, SK);
+    const uint32_t alo = ahi + kTileBytes;
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+        const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
+        const uint32_t boff = (jrow + (uint32_t)(kStripK * (1 - ks))) * (kStripK * 2);
+        const uint64_t dbh = sdesc_sw32(bhi + boff), dbl = sdesc_sw32(blo + boff);
+        umma_f16(d, dah, dbh, id, (overwrite && ks == 0) ? 0u : 1u);
+        umma_f16(d, dah, dbl, id, 1u);
+        umma_f16(d, dal, dbh, id, 1u);
+    }
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
@@ -747,13 +809,24 @@ __device__ __forceinline__ void produce_chunk_ext(const MixedArgs& a, int64_t ti
 // whole contribution to the pass's columns; the rest are drawn for real and
 // their columns become final one chunk at a time, as in one pass.  Every role
 // walks this same (pass, chunk) sequence, one pipeline stage per chunk.
+//
+// Pass mode 3 cuts the columns into passes of 256 (pass 0: n0 chunks, the
+// rest 8 each) held alternately in two TMEM buffers, and draws every chunk
+// once.  While pass q's own chunks accumulate into its buffer and its columns
+// are read, the other buffer takes the next pass's whole far-field: each of
+// pass q's chunks over all 256 next-pass columns, and every earlier chunk
+// (0 .. begin(q) - 1) from a per-CTA global cache of A tiles that the MMA
+// thread stored when the chunk was first used.  So the far-field MMAs overlap
+// the producers' work instead of waiting for redrawn tiles, and a pass's
+// columns are complete when its first own chunk lands.
 template <int PM>
 struct PassPlan {
+    static constexpr int kPer = (PM == 3 ? kHalfCols : kPassCols) / kChunk;  // chunks of a pass after the first
     int np, n0, nc;
     __device__ __forceinline__ PassPlan(const MixedArgs& a)
         : np(PM == 0 ? 1 : (PM == 1 ? 2 : a.np)), n0(PM == 0 ? 0 : a.n0), nc(a.nc) {}
-    __device__ __forceinline__ int begin(int p) const { return p == 0 ? 0 : n0 + kPassCols / kChunk * (p - 1); }
-    __device__ __forceinline__ int end(int p) const { return p + 1 >= np ? nc : n0 + kPassCols / kChunk * p; }
+    __device__ __forceinline__ int begin(int p) const { return p == 0 ? 0 : n0 + kPer * (p - 1); }
+    __device__ __forceinline__ int end(int p) const { return p + 1 >= np ? nc : n0 + kPer * p; }
 };
 
 // PM: pass mode (pass_mode(Np)): 0 one TMEM pass; 1 two passes, the narrow
@@ -770,11 +843,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     constexpr int kStageFB = stage_f_bytes(NS);
     constexpr bool T32 = SK == 2;
     constexpr int WB = T32 ? kWindowBytesT : kWindowBytes;  // one half of a strip window
-    static_assert(PM >= 0 && PM <= 2 && SK >= 0 && SK <= 2, "pass mode / split kind");
+    static_assert(PM >= 0 && PM <= 3 && SK >= 0 && SK <= 2, "pass mode / split kind");
+    static_assert(PM != 3 || (SK != 2 && !MC && SRC == 0), "pass mode 3: 16-bit splits, RT, Philox");
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g, a.n_o, NS, T32);
+    const SmemLayout L = smem_layout(a.Np, a.stages, a.n_g, a.n_o, NS, T32, PM == 3 ? kCSlots : 0);
     unsigned char* strip = base + L.strip;
     float* acc_s = (float*)(base + L.acc);
     float* beta_s = (float*)(base + L.beta);
@@ -790,6 +864,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     uint64_t* strip_bar = bars + 10;
     uint64_t* final_bar = bars + 11;
     uint32_t* tmem_holder = (uint32_t*)(bars + 12);
+    // pass mode 3 only: the second TMEM buffer's release, the cached-tile slots' fill and release
+    uint64_t* tmem_empty1 = bars + 13;
+    uint64_t* cfull = bars + 14;   // [kCSlots]
+    uint64_t* cempty = bars + 17;  // [kCSlots]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int Np = a.Np, nc = a.nc;
@@ -802,10 +880,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     if (threadIdx.x == kMmaWarp * 32) {
         for (int s = 0; s < S; ++s) {
             mbar_init(smem_u32(full + s), kProdWarps);
-            mbar_init(smem_u32(empty + s), 1 + kEpiWarps);
+            // pass mode 3: the MMA thread also arrives once the stage's A tile is in the cache
+            mbar_init(smem_u32(empty + s), 1 + kEpiWarps + (PM == 3 ? 1 : 0));
             mbar_init(smem_u32(accf + s), 1);
         }
         mbar_init(smem_u32(tmem_empty), kEpiWarps);
+        if (PM == 3) {
+            mbar_init(smem_u32(tmem_empty1), kEpiWarps);
+            for (int s = 0; s < kCSlots; ++s) {
+                mbar_init(smem_u32(cfull + s), 1);
+                mbar_init(smem_u32(cempty + s), 1);
+            }
+        }
         mbar_init(smem_u32(strip_bar), 1);
         mbar_init(smem_u32(final_bar), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -848,11 +934,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
             const uint64_t gpath = (uint64_t)(a.path0 + m);
             for (int q = 0; q < pp.np; ++q) {
                 const int cb = pp.begin(q), ce = pp.end(q);
-                for (int c = 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+                // pass mode 3 draws each chunk once: no redrawn chunks, no boundary rows
+                for (int c = PM == 3 ? cb : 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
                     // redrawn chunks of a later pass feed only the MMA (W1 A tile)
-                    const bool redraw = PM > 0 && c < cb;
+                    const bool redraw = (PM == 1 || PM == 2) && c < cb;
                     // last real chunk of a pass before the last: boundary row for its successor
-                    const bool bnd = PM > 0 && !redraw && c == ce - 1 && q + 1 < pp.np;
+                    const bool bnd = (PM == 1 || PM == 2) && !redraw && c == ce - 1 && q + 1 < pp.np;
                     if (!mbar_wait_warp(smem_u32(empty + s), ph ^ 1u, a.err, 1, a.prof)) goto done;
                     unsigned char* st = base + L.a0 + s * kStageA;
                     float* w1s = (float*)(base + L.f0 + s * FB);
@@ -900,8 +987,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         float* my_acc = acc_s + (size_t)wg * a.n_g * NS * kTileM;
         float* w10_s = acc_s + (size_t)2 * a.n_g * NS * kTileM;  // W1_0 per path
         float* wq0_s = w10_s + kTileM;                          // Wperp_0 per path (plain Monte Carlo)
+        // pass mode 3: per group and path, sqrt(v) of the previous chunk's last column, whose
+        // dW (W1 at the next chunk's first step) is added with the next chunk
+        float* pend_s = acc_s + (size_t)2 * a.n_g * NS * kTileM + (NS - 1) * kTileM;
         int s = 0;
         uint32_t ph = 0;
+        int gpass = 0;  // pass mode 3: passes so far (all tiles); pass g uses TMEM buffer g & 1
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
             const int64_t m = tile * kTileM + p;
             const bool valid = m < a.B;
@@ -910,11 +1001,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 for (int t = 0; t < NS; ++t) my_acc[(NS * g + t) * kTileM + p] = 0.f;
             for (int q = 0; q < pp.np; ++q) {
               const int cb = pp.begin(q), ce = pp.end(q);
-              for (int c = 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+              for (int c = PM == 3 ? cb : 0; c < ce; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
                 // the producers' FP32 tiles of this stage (the upper half also pairs
                 // its last column with the next chunk's first W1), then the MMA results
                 if (!mbar_wait_warp(smem_u32(full + s), ph, a.err, 7, a.prof)) goto done;
-                if (PM > 0 && c < cb) {
+                if ((PM == 1 || PM == 2) && c < cb) {
                     // redrawn chunk: no column becomes final.  Its MMA completion is still
                     // awaited, so that every accf phase is observed in order.
                     if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
@@ -922,12 +1013,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     if (lane == 0) mbar_arrive(smem_u32(empty + s));
                     continue;
                 }
-                const uint32_t tcol0 = PM > 0 ? (uint32_t)(kChunk * cb) : 0u;  // TMEM column of output 0 of this pass
+                // output column - TMEM column (mod 2^32); pass mode 3 alternates two 256-column buffers
+                const uint32_t tcol0 = PM == 3   ? (uint32_t)(kChunk * cb) - (uint32_t)((gpass & 1) * kHalfCols)
+                                       : PM > 0 ? (uint32_t)(kChunk * cb)
+                                                : 0u;
                 const bool pass_end = c == ce - 1;
                 const bool has_next = c + 1 < nc;
-                const bool bnd = PM > 0 && pass_end && q + 1 < pp.np;  // successor W1 in this stage's boundary row
+                // successor W1 in this stage's boundary row (pass mode 3: the next stage holds chunk c + 1)
+                const bool bnd = (PM == 1 || PM == 2) && pass_end && q + 1 < pp.np;
                 const int sn = (s + 1 == S) ? 0 : s + 1;
-                if ((kEpiWGs == 1 || wg == 1) && has_next && !bnd &&
+                if (PM != 3 && (kEpiWGs == 1 || wg == 1) && has_next && !bnd &&
                     !mbar_wait_warp(smem_u32(full + sn), sn == 0 ? ph ^ 1u : ph, a.err, 8, a.prof))
                     goto done;
                 if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
@@ -949,10 +1044,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                         w1pv[jj] = v.x; w1pv[jj + 1] = v.y; w1pv[jj + 2] = v.z; w1pv[jj + 3] = v.w;
                     }
                     const float* nexts = (const float*)(base + L.f0 + sn * FB);
+                    // pass mode 3: the last column's dW waits for the next chunk (its stage may not be
+                    // drawn yet with two stages); W1 at this chunk's first step completes the previous one's
                     const float w_after = (hh == 0) ? w1s[ftile_at(p, 16)]
-                                                    : (!has_next ? 0.f
-                                                       : bnd     ? w1s[kFBnd + p]
-                                                                 : nexts[ftile_at(p, 0)]);
+                                                    : (PM == 3 || !has_next ? 0.f
+                                                       : bnd                ? w1s[kFBnd + p]
+                                                                            : nexts[ftile_at(p, 0)]);
+                    const float w_first = (PM == 3 && hh == 1 && c > 0) ? w1s[ftile_at(p, 0)] : 0.f;
                     float wqv[MC ? 16 : 1], wq_after = 0.f;
                     if (MC) {
 #pragma unroll
@@ -971,7 +1069,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                         // this warp's accumulator columns of the pass are read
                         tc_fence_before();
                         __syncwarp();
-                        if (lane == 0) mbar_arrive(smem_u32(tmem_empty));
+                        if (lane == 0) mbar_arrive(smem_u32((PM == 3 && (gpass & 1)) ? tmem_empty1 : tmem_empty));
                     }
                     float wn[16];
 #pragma unroll
@@ -1007,7 +1105,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                             bt[jj] = u.x; bt[jj + 1] = u.y; bt[jj + 2] = u.z; bt[jj + 3] = u.w;
                         }
                         const int lim = a.nsteps[g] - 1 - kChunk * c - j0;
-                        float sv = 0.f, swv = 0.f, swq = 0.f;
+                        float sv = 0.f, swv = 0.f, swq = 0.f, su_last = 0.f;
                         if (lim >= 16) {
 #pragma unroll
                             for (int jj = 0; jj < 16; ++jj) {
@@ -1015,6 +1113,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                                 sv = fmaf(su, su, sv);
                                 swv = fmaf(su, wn[jj], swv);
                                 if (MC) swq = fmaf(su, wqn[jj], swq);
+                                if (PM == 3 && jj == 15) su_last = su;
                             }
                         } else {
 #pragma unroll
@@ -1027,6 +1126,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                                 }
                             }
                         }
+                        if (PM == 3 && hh == 1) {
+                            float* pg = pend_s + g * kTileM + p;
+                            if (c > 0) swv = fmaf(*pg, w_first, swv);
+                            *pg = su_last;
+                        }
                         my_acc[(NS * g) * kTileM + p] += sv;
                         my_acc[(NS * g + 1) * kTileM + p] += swv;
                         if (MC) my_acc[(NS * g + 2) * kTileM + p] += swq;
@@ -1035,6 +1139,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(empty + s));
               }
+              if (PM == 3) ++gpass;
             }
             // both warpgroups' column sums of this tile are in shared memory
             asm volatile("bar.sync 1, %0;" ::"r"(kEpiWarps * 32) : "memory");
@@ -1098,7 +1203,116 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         const uint32_t strip_hi = smem_u32(strip);
         const uint32_t strip_lo = strip_hi + (uint32_t)((T32 ? strip_smem_bytes_t32(Np) : strip_smem_bytes(Np)) / 2);
         constexpr bool wide = PM == 0 && !T32;  // the wide 16-bit strip exactly when one pass covers Np
-        if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
+        if constexpr (PM == 3) {
+            // Pass mode 3 (PassPlan), per tile and pass q: each own chunk c into its pass's
+            // columns [32 c, Pn) of buffer X, and before the last pass into all 256 columns of
+            // pass q + 1 in buffer Y; its A tile into the cache when a later pass reads it;
+            // then its share of the cached chunks 0 .. cb - 1 into Y, streamed through
+            // kCSlots shared-memory slots two items ahead.  (Loading a pass's first cached
+            // tiles during the pass before measured slower: 4.19 against 4.09 ms at N = 1024,
+            // 2^20 paths, from the wait for the stores at the end of the pass.)
+            unsigned char* cache = a.acache + (size_t)blockIdx.x * a.ncache * kStageA;
+            const uint32_t cs0 = smem_u32(base + L.cs);
+            int64_t G = 0;   // passes so far (all tiles): pass G accumulates in buffer G & 1
+            int64_t cl = 0;  // cached tiles loaded
+            int64_t cj = 0;  // cached tiles consumed (cl == cj at every pass end)
+            int s = 0;
+            uint32_t ph = 0;
+            bool ok = mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof);
+            // cached chunk `chunk` into the next slot, once that slot's previous tile's MMAs are done
+            auto load = [&](int chunk) -> bool {
+                const int slot = (int)(cl % kCSlots);
+                if (cl >= kCSlots &&
+                    !mbar_wait(smem_u32(cempty + slot), (uint32_t)((cl / kCSlots - 1) & 1), a.err, 9, a.prof))
+                    return false;
+                const uint32_t bar = smem_u32(cfull + slot);
+                mbar_expect_tx(bar, (uint32_t)kStageA);
+                bulk_g2s(cs0 + (uint32_t)(slot * kStageA), cache + (size_t)chunk * kStageA, (uint32_t)kStageA, bar);
+                ++cl;
+                return true;
+            };
+            for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                for (int q = 0; q < pp.np && ok; ++q, ++G) {
+                    const int cb = pp.begin(q), ce = pp.end(q);
+                    const int P = kChunk * cb, Pn = kChunk * ce;  // columns: this pass [P, Pn), the next [Pn, Pn + 256)
+                    const bool has_y = q + 1 < pp.np;
+                    const int k = ce - cb, mC = has_y ? cb : 0;  // own chunks; cached chunks into Y
+                    const uint32_t xb = tmem + (uint32_t)((G & 1) * kHalfCols);
+                    const uint32_t yb = tmem + (uint32_t)(((G + 1) & 1) * kHalfCols);
+                    int u = 0;  // cached chunks of this pass done
+                    for (int c = cb; c < ce && ok; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
+                        if (c == 0 && G >= 2) {
+                            // a tile's first pass starts a fresh buffer: pass G - 2 there is read
+                            if (!mbar_wait(smem_u32((G & 1) ? tmem_empty1 : tmem_empty), (uint32_t)(((G - 2) >> 1) & 1),
+                                           a.err, 4, a.prof)) {
+                                ok = false;
+                                break;
+                            }
+                            tc_fence_after();
+                        }
+                        if (!mbar_wait(smem_u32(full + s), ph, a.err, 5, a.prof)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
+                        mma_chunk_narrow<SK>(xb + (uint32_t)(kChunk * c - P), ahi, strip_hi, strip_lo, 0u,
+                                             Pn - kChunk * c, q == 0 && c == 0);
+                        umma_commit(smem_u32(accf + s));
+                        if (has_y) {
+                            if (c == cb && G >= 1) {
+                                // Y held pass G - 1: its columns are read
+                                if (!mbar_wait(smem_u32(((G + 1) & 1) ? tmem_empty1 : tmem_empty),
+                                               (uint32_t)(((G - 1) >> 1) & 1), a.err, 4, a.prof)) {
+                                    ok = false;
+                                    break;
+                                }
+                                tc_fence_after();
+                            }
+                            mma_chunk_narrow<SK>(yb, ahi, strip_hi, strip_lo, (uint32_t)(Pn - kChunk * c), kHalfCols,
+                                                 c == cb);
+                        }
+                        umma_commit(smem_u32(empty + s));
+                        if (c < a.ncache) {
+                            // this chunk's A tile into the cache; the stage may be refilled once the
+                            // copy has read it
+                            bulk_s2g(cache + (size_t)c * kStageA, ahi, (uint32_t)kStageA);
+                            const long long t0 = a.prof ? clock64() : 0;
+                            bulk_wait_read0();
+                            if (a.prof) atomicAdd(a.prof + 11, (unsigned long long)(clock64() - t0));
+                        }
+                        mbar_arrive(smem_u32(empty + s));
+                        if (c == cb && mC > 0) {
+                            // the cached tiles of chunks < cb are in global memory (the most recent
+                            // store, when there is one, is this chunk's own), then the first loads
+                            const long long t0 = a.prof ? clock64() : 0;
+                            if (c < a.ncache)
+                                bulk_wait_done1();
+                            else
+                                bulk_wait_done0();
+                            if (a.prof) atomicAdd(a.prof + 12, (unsigned long long)(clock64() - t0));
+                            for (int t = 0; t < kCSlots - 1 && t < mC && ok; ++t) ok = load(t);
+                        }
+                        const int u_end = (int)((int64_t)mC * (c - cb + 1) / k);
+                        for (; u < u_end && ok; ++u, ++cj) {
+                            const int slot = (int)(cj % kCSlots);
+                            if (!mbar_wait(smem_u32(cfull + slot), (uint32_t)((cj / kCSlots) & 1), a.err, 10, a.prof)) {
+                                ok = false;
+                                break;
+                            }
+                            tc_fence_after();
+                            mma_chunk_narrow<SK>(yb, cs0 + (uint32_t)(slot * kStageA), strip_hi, strip_lo,
+                                                 (uint32_t)(Pn - kChunk * u), kHalfCols, false);
+                            umma_commit(smem_u32(cempty + slot));
+                            if (u + kCSlots - 1 < mC) ok = load(u + kCSlots - 1);
+                        }
+                    }
+                }
+            }
+            // after an error: the loads in flight land and the stores finish before the CTA exits
+            for (; cj < cl; ++cj) mbar_drain(smem_u32(cfull + (int)(cj % kCSlots)), (uint32_t)((cj / kCSlots) & 1));
+            bulk_wait_done0();
+        } else if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
             int64_t pass = 0;
             int s = 0;
             uint32_t ph = 0;
@@ -1996,7 +2210,7 @@ static cudaError_t allow_max_smem(void (*kern)(MixedArgs))
 }
 
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
-                  int64_t max_batch, bool mc)
+                  int64_t max_batch, bool mc, bool tile_cache)
 {
     DevInfo dv;
     if (!device_info(&dv)) {
@@ -2124,6 +2338,16 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
     for (const MixedLaunch& r : job.launches)
         if (r.args.n_o > kMixedMaxFused || smem_layout(Np, 2, r.args.n_g, r.args.n_o, 2, tf32).total > optin)
             job.fused = false;
+    // Pass mode 3 replaces the redrawing two-pass schedule for the 16-bit splits
+    // and the RT estimator where two stages and the cached-tile slots fit.
+    job.pmode = backend == RBG_CONV_GEMM ? pass_mode(Np) : 0;
+    if (RBG_PASS3 && tile_cache && job.pmode == 1 && !tf32 && !mc) {
+        bool fits = true;
+        for (const MixedLaunch& r : job.launches)
+            fits = fits &&
+                   smem_layout(Np, 2, r.args.n_g, job.fused ? r.args.n_o : 0, ns, false, kCSlots).total <= optin;
+        if (fits) job.pmode = 3;
+    }
     for (MixedLaunch& r : job.launches) {
         MixedArgs& A = r.args;
         const int no = job.fused ? A.n_o : 0;
@@ -2131,6 +2355,13 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         if (backend == RBG_CONV_GEMM && smem_layout(Np, A.stages, A.n_g, no, ns, tf32).total > optin) {
             err = "mixed kernel shared memory does not fit";
             return RBG_ERR_UNSUPPORTED;
+        }
+        r.stages_pm1 = A.stages;
+        if (job.pmode == 3) {
+            A.np = (Np + kHalfCols - 1) / kHalfCols;
+            A.n0 = (Np - kHalfCols * (A.np - 1)) / kChunk;
+            A.ncache = A.np >= 3 ? A.n0 + kHalfCols / kChunk * (A.np - 3) : 0;
+            A.stages = 2;
         }
     }
     if (backend == RBG_CONV_FFT) {
@@ -2174,6 +2405,11 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         }
     }
     job.workspace_bytes = off;
+    if (job.pmode == 3) {
+        // the A-tile cache: ncache tiles per CTA, not part of the uploaded image
+        job.off_acache = (off + 1023) / 1024 * 1024;
+        job.workspace_bytes = job.off_acache + (size_t)job.sms * job.launches[0].args.ncache * kStageA;
+    }
     // batch: float2 per (variance group, path) within 1 GiB
     int64_t cap = ((int64_t)1 << 30) / (8 * (int64_t)std::max(1, job.n_vg));
     cap = std::max<int64_t>(kTileM, cap / kTileM * kTileM);
@@ -2205,6 +2441,8 @@ int mixed_part_rows(const MixedJob& job, int64_t B)
 template <int SK, bool MC, int SRC>
 static void (*gemm_kernel_pm(int pm))(MixedArgs)
 {
+    if constexpr (SK != 2 && !MC && SRC == 0)
+        if (pm == 3) return k_mixed_gemm<SK, 3, false, 0>;
     if constexpr (SRC == 1)
         return pm == 0 ? k_mixed_gemm<SK, 0, MC, SRC> : k_mixed_gemm<SK, 1, MC, SRC>;
     else
@@ -2260,15 +2498,28 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
         mixed_set_seed(A, seed);
         A.path0 = path0;
         A.B = B;
-        const int smem =
-            smem_layout(A.Np, A.stages, A.n_g, A.n_o, job.mc ? 3 : 2, job.split == RBG_SPLIT_TF32X2).total;
+        int pm = job.backend == RBG_CONV_GEMM ? pass_mode(A.Np) : 0;
+        if (job.pmode == 3) {
+            if (!ext && !job.sob) {
+                pm = 3;
+                A.acache = base + job.off_acache;
+            } else {
+                // Sobol' or caller normals: the two-pass kernel
+                A.np = 2;
+                A.n0 = (A.Np - kPassCols) / kChunk;
+                A.stages = r.stages_pm1;
+            }
+        }
+        const int smem = smem_layout(A.Np, A.stages, A.n_g, A.n_o, job.mc ? 3 : 2, job.split == RBG_SPLIT_TF32X2,
+                                     pm == 3 ? kCSlots : 0)
+                             .total;
         const int64_t ntiles = (B + kTileM - 1) / kTileM;
         const int grid = (int)std::min<int64_t>(ntiles, job.sms);
         cudaError_t e;
         if (job.backend == RBG_CONV_FFT) {
             e = launch_mixed_fft(A, job.sms, st);
         } else {
-            const int pm = pass_mode(A.Np), sk = split_kind(job.split);
+            const int sk = split_kind(job.split);
             void (*kern)(MixedArgs);
             if (job.sob)
                 kern = gemm_kernel<false, 1>(sk, pm);

@@ -60,6 +60,11 @@ struct MixedArgs {
     // each round's key is an operand of its XOR instead of one of 20 registers
     // held across the whole kernel.
     uint32_t pk[20];
+    // Pass mode 3 (GEMM backend, 512 < Np <= 1024, 16-bit splits, RT, Philox):
+    // per-CTA global cache of the A tiles later passes read back, ncache
+    // chunks of 16 KB per CTA (CTA b's at acache + b * ncache * 16 KB).
+    unsigned char* acache;
+    int ncache;
 };
 
 // Sets a.seed and its Philox round keys a.pk.
@@ -78,6 +83,7 @@ inline void mixed_set_seed(MixedArgs& a, uint64_t seed)
 struct MixedLaunch {
     MixedArgs args;  // device pointers filled at launch time
     size_t off_strip = 0, off_beta = 0, off_spec = 0, off_otab = 0, off_oidx = 0;
+    int stages_pm1 = 0;  // pass mode 3 jobs: pipeline stages of the two-pass kernel that takes other normal sources
 };
 
 struct MixedJob {
@@ -90,14 +96,21 @@ struct MixedJob {
     bool mc = false;              // plain Monte Carlo: third normal stream Wperp and IsvdWp per (group, path)
     const unsigned int* sob = nullptr;  // Sobol' table on the device (set by the caller): QMC normals, not Philox
     size_t off_tw = 0;
+    // GEMM kernel pass mode: 0 one TMEM pass, 1 two, 2 up to eight, 3 two
+    // 256-column buffers with the A-tile cache at off_acache (workspace bytes
+    // past the uploaded image)
+    int pmode = 0;
+    size_t off_acache = 0;
     std::vector<MixedLaunch> launches;   // one per (Volterra pass, <= 16 groups)
     std::vector<const void*> table_dev;  // optional device copies of each launch's strip / spectrum
     std::vector<unsigned char> host_ws;  // image uploaded by mixed_upload
 };
 
 // mc: the plain Monte Carlo estimator (a third normal stream; both backends, every pass mode).
+// tile_cache: pass mode 3 may be chosen (its A-tile cache, sms x up to 16 x
+// 16 KB of device memory, is part of workspace_bytes).
 int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& job, std::string& err,
-                  int64_t max_batch = 0, bool mc = false);
+                  int64_t max_batch = 0, bool mc = false, bool tile_cache = true);
 // Byte range of launch i's strip (GEMM) or spectrum (FFT) inside host_ws, and
 // of the shared FFT twiddle table (empty for the GEMM backend).
 void mixed_table_range(const MixedJob& job, int i, size_t* off, size_t* bytes);

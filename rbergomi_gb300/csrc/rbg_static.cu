@@ -102,7 +102,8 @@ int rbg_price_rt_static(const rbg_params* p, const rbg_options* o, double* price
     if (n_out > kStaticMaxOutputs)
         return static_fail(RBG_ERR_ARG, "par_size * op_size exceeds 4096 outputs of the static scratch");
     MixedJob job;
-    int rc = mixed_prepare(plan, *o, p->M, job, err);
+    // the two-pass kernel without the A-tile cache, which would not fit the static scratch
+    int rc = mixed_prepare(plan, *o, p->M, job, err, 0, false, false);
     if (rc) return static_fail(rc, err);
 
     // carve the scratch: workspace image, output tables, sums, results,

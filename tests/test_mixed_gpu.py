@@ -63,10 +63,11 @@ def test_fused_normals_are_the_exported_stream(R, N, M):
 @pytest.mark.parametrize("split,tol", [(0, 4e-5), (1, 1e-6), (2, 5e-4)])
 @pytest.mark.parametrize("N", [64, 100, 512, 513, 700, 1024, 1025, 1500, 2048, 3001, 4096])
 def test_toeplitz_gemm_columns(R, split, tol, N):
-    """Columns of one TMEM pass (N <= 512), of two (512 < N <= 1024, the
-    second pass fed by redrawn A tiles over the resident strip) and of up to
-    eight (N > 1024: redrawn chunks read their strip window, copied into the
-    stage, every later pass) against the FP64 convolution."""
+    """Columns of one TMEM pass (N <= 512); for 512 < N <= 1024, of 256-column
+    passes in two TMEM buffers whose far-field comes from cached A tiles (the
+    16-bit splits) or of two 512-column passes fed by redrawn A tiles (TF32);
+    and of up to eight (N > 1024: redrawn chunks read their strip window,
+    copied into the stage, every later pass) against the FP64 convolution."""
     H = 0.1
     M = 256
     w, x, _ = R.debug_mixed_paths(0.04, [H], [1.5], [-0.7], [1.0], [1.0], N, M, seed=3, split=split)
@@ -143,6 +144,26 @@ def test_multi_pass_gemm_prices_vs_fp64_identical_normals(R, N):
     err = np.abs(mp - fp)
     assert np.all(err <= 1e-4 * fp)
     assert np.all(err < 0.2 * fs)
+
+
+@pytest.mark.parametrize("N,split", [(544, 1), (768, 0), (1024, 1)])
+def test_cached_tile_passes_many_tiles_per_cta(R, N, split):
+    """512 < N <= 1024 with the 16-bit splits: 256-column passes alternate two
+    TMEM buffers across the tiles of a CTA (three passes at N <= 768, so a
+    tile's first pass lands in either buffer) and the per-CTA A-tile cache is
+    rewritten by every tile.  M = three waves of 128-path tiles over every SM
+    plus a ragged tail; error vs the FP64 form on the same FP32 normals
+    <= 1e-4 relative and < 0.2 standard errors."""
+    H, eta, rho, xi, T = [0.1], [1.5], [-0.7], 0.04, 2.0
+    K = list(np.linspace(0.5, 1.5, 11))
+    M = 3 * 160 * 128 + 77
+    mp, ms, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=5, precision=R.MIXED, split=split,
+                           conv=R.CONV_GEMM)
+    fp, fs, _ = R.price_rt(xi, H, eta, rho, [T] * 11, K, N, M, seed=5, normals=R.NORMALS_F32)
+    err = np.abs(mp - fp)
+    assert np.all(err <= 1e-4 * fp)
+    assert np.all(err < 0.2 * fs)
+    assert np.all(np.abs(ms / fs - 1) < 1e-3)
 
 
 @pytest.mark.parametrize("N,split", [(800, 1), (2500, 1), (700, 2), (2500, 2)])

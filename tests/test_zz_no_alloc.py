@@ -18,6 +18,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-12  # same kernels, same batching of the Philox stream: roundoff only
+# 512 < N <= 1024 (16-bit splits): rbg_price_rt runs 256-column TMEM passes
+# whose far-field reads A tiles back from a per-CTA device cache (tens of MB),
+# which does not fit the static scratch, so the static entry runs the two-pass
+# kernel that draws those tiles again.  Same products, another FP32
+# accumulation order in TMEM: prices agree to roundoff of that order.
+RTOL_TWO_PASS = (2e-6, 2e-5)  # prices; standard errors and implied vols
 
 
 @pytest.fixture(scope="module")
@@ -48,7 +54,7 @@ CASES = [
     # workload-2 shape, reduced M
     dict(xi=0.235 ** 2, H=[0.1], eta=[1.9], rho=[-0.9], T=[1.0] * 21, K=list(np.linspace(0.6, 1.4, 21)), N=512,
          M=(1 << 18) + 77, seed=11),
-    # two Volterra passes, several variance groups, N = 1024 (two TMEM passes of the tensor-core GEMM)
+    # two Volterra passes, several variance groups, N = 1024 (the two-pass kernel in the static entry)
     dict(xi=0.04, H=[0.07, 0.3], eta=[1.5, 2.0], rho=[-0.7, -0.5], T=[0.5, 2.0], K=[0.9, 1.2], N=1024, M=5000,
          seed=3),
     # longer horizon: three TMEM passes with streamed strip windows, and the batched-FFT backend
@@ -69,11 +75,12 @@ def test_static_entry_point_matches_regular(R, case):
     conv = c.pop("conv", 0)
     args = (c["xi"], c["H"], c["eta"], c["rho"], c["T"], c["K"], c["N"], c["M"])
     want_p, want_s, want_iv = R.price_rt(*args, seed=seed, precision=R.MIXED, conv=conv)
+    rp, rs = (RTOL, 1e-9) if not (512 < c["N"] <= 1024 and conv == 0) else RTOL_TWO_PASS
     for _ in range(2):  # second call runs on the contents the first call left behind
         p, s, iv = static_price(R, *args, seed=seed, conv=conv)
-        np.testing.assert_allclose(p, want_p, rtol=RTOL, atol=0)
-        np.testing.assert_allclose(s, want_s, rtol=1e-9, atol=0)
-        np.testing.assert_allclose(iv, want_iv, rtol=1e-9, atol=0)
+        np.testing.assert_allclose(p, want_p, rtol=rp, atol=0)
+        np.testing.assert_allclose(s, want_s, rtol=rs, atol=0)
+        np.testing.assert_allclose(iv, want_iv, rtol=rs, atol=0)
 
 
 def test_static_entry_point_rejects_oversize(R):
