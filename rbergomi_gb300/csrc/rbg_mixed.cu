@@ -391,17 +391,30 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
 // 8 KB above) against the narrow strip (hi / lo halves at bhi / blo) into n
 // TMEM columns from d, the first of which reads strip row jrow (K half ks
 // from row jrow + 16 - 16 ks).  overwrite: the first product replaces D.
+//
+// One thread issues every MMA of the CTA while sixteen warps of Philox and
+// epilogue arithmetic compete for its issue slots (in isolation the MMA pipe
+// takes 144 cycles per N = 256 MMA in this pattern, 183 beside eight such
+// warps), so the descriptors are formed with one 32-bit add each: a chunk's
+// descriptors differ only in the start-address field, address >> 4 in bits
+// 0-13 of the low word, and shared addresses stay below 2^18, so adding an
+// offset / 16 never carries out of it.
+__device__ __forceinline__ uint64_t sdesc_words(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
+
 template <int SK>
 __device__ __forceinline__ void mma_chunk_narrow(uint32_t d, uint32_t ahi, uint32_t bhi, uint32_t blo, uint32_t jrow,
                                                  int n, bool overwrite)
 {
     const uint32_t id = idesc_f16(n, SK);
-    const uint32_t alo = ahi + kTileBytes;
+    const uint64_t a0 = sdesc_sw64(ahi), b0 = sdesc_sw32(bhi + jrow * (kStripK * 2));
+    const uint32_t alo = (uint32_t)a0, ahw = (uint32_t)(a0 >> 32), blo0 = (uint32_t)b0, bhw = (uint32_t)(b0 >> 32);
+    const uint32_t dl = (blo - bhi) >> 4;  // hi half -> lo half of the strip (or window)
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks) {
-        const uint64_t dah = sdesc_sw64(ahi + 32 * ks), dal = sdesc_sw64(alo + 32 * ks);
-        const uint32_t boff = (jrow + (uint32_t)(kStripK * (1 - ks))) * (kStripK * 2);
-        const uint64_t dbh = sdesc_sw32(bhi + boff), dbl = sdesc_sw32(blo + boff);
+        // A: K half ks 32 B into the row, lo tile kTileBytes above; B: rows from jrow + 16 - 16 ks
+        const uint64_t dah = sdesc_words(alo + 2u * ks, ahw), dal = sdesc_words(alo + kTileBytes / 16 + 2u * ks, ahw);
+        const uint32_t bro = (uint32_t)(kStripK * (1 - ks) * kStripK * 2 / 16);
+        const uint64_t dbh = sdesc_words(blo0 + bro, bhw), dbl = sdesc_words(blo0 + dl + bro, bhw);
         umma_f16(d, dah, dbh, id, (overwrite && ks == 0) ? 0u : 1u);
         umma_f16(d, dah, dbl, id, 1u);
         umma_f16(d, dal, dbh, id, 1u);
@@ -1368,6 +1381,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                                 const uint32_t id = idesc_f16(n, SK);
                                 const uint32_t jrow = (uint32_t)(col0 - rbase);
                                 const uint32_t d = tmem + (uint32_t)(col0 - toff);
+                                if constexpr (!wide) {
+                                    mma_chunk_narrow<SK>(d, ahi, bhi, blo, jrow, n, first);
+                                } else {
 #pragma unroll
                                 for (int ks = 0; ks < 2; ++ks) {
                                     // K half ks: A columns [16 ks, 16 ks + 16); wide strip: row jrow, bytes
@@ -1385,6 +1401,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                                     umma_f16(d, dah, dbh, id, (first && ks == 0) ? 0u : 1u);
                                     umma_f16(d, dah, dbl, id, 1u);
                                     umma_f16(d, dal, dbh, id, 1u);
+                                }
                                 }
                             }
                         }
