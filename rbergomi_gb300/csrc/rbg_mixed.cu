@@ -36,7 +36,8 @@
 // 1024 runs pass mode 3 instead (PassPlan): 256-column passes alternating
 // between two TMEM buffers, each chunk drawn once, the far-field of the next
 // pass accumulated in the other buffer from the chunks' A tiles that the MMA
-// thread keeps in a per-CTA global cache.
+// thread keeps in a per-CTA global cache; its epilogue reads W1 back from the
+// A tile (hi + lo), so a stage holds no FP32 W1 tile and three stages fit.
 // Up to Np = 1024 the whole narrow strip stays in shared memory.  Above that
 // (up to 4096, eight passes) only its first 528 rows do -- all that a chunk
 // drawn for real reads -- and each redrawn chunk brings the 528-row window it
@@ -180,7 +181,8 @@ __host__ __device__ inline SmemLayout smem_layout(int Np, int stages, int n_g, i
     L.a0 = ((tf32 ? strip_smem_bytes_t32(Np) : strip_smem_bytes(Np)) + 1023) / 1024 * 1024;
     L.stages = stages;
     L.f0 = L.a0 + stages * kStageA;
-    L.fstride = stage_f_bytes(ns);
+    // pass mode 3 (cslots > 0) keeps only the W1perp tile: W1 is read back from the stage's A tile
+    L.fstride = cslots > 0 ? kChunk * kTileM * 4 : stage_f_bytes(ns);
     const int win2 = tf32 ? 2 * kWindowBytesT : 2 * kWindowBytes;
     if (pass_mode(Np) == 2 && L.fstride < win2) L.fstride = win2;
     L.cs = L.f0 + stages * L.fstride;
@@ -492,6 +494,46 @@ __device__ __forceinline__ void a_tile_store1(unsigned char* st, int p, int k, f
     }
 }
 
+// W1 of path row p read back from a 16-bit A tile as hi + lo (the operand
+// the tensor cores multiply; within 2^-18 |W1| of the FP32 draw for BF16,
+// 2^-22 for FP16): steps [16 hh, 16 hh + 16) of the chunk, or step k.
+template <int SK>
+__device__ __forceinline__ float2 split_pair_f32(uint32_t w)
+{
+    if constexpr (SK == 1) {
+        return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xFFFF0000u));
+    } else {
+        __half2 h;
+        *reinterpret_cast<uint32_t*>(&h) = w;
+        return __half22float2(h);
+    }
+}
+template <int SK>
+__device__ __forceinline__ void a_tile_w1_16(const unsigned char* st, int p, int hh, float (&w)[16])
+{
+    const int sw = (p >> 1) & 3;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const int off = p * 64 + (((2 * hh + e) ^ sw) << 4);
+        const uint4 h = *(const uint4*)(st + off), l = *(const uint4*)(st + kTileBytes + off);
+        const uint32_t hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 a = split_pair_f32<SK>(hv[i]), b = split_pair_f32<SK>(lv[i]);
+            w[8 * e + 2 * i] = a.x + b.x;
+            w[8 * e + 2 * i + 1] = a.y + b.y;
+        }
+    }
+}
+template <int SK>
+__device__ __forceinline__ float a_tile_w1_at(const unsigned char* st, int p, int k)
+{
+    const int off = p * 64 + ((((k >> 3)) ^ ((p >> 1) & 3)) << 4) + (((k & 7) >> 1) << 2);
+    const float2 a = split_pair_f32<SK>(*(const uint32_t*)(st + off)),
+                 b = split_pair_f32<SK>(*(const uint32_t*)(st + kTileBytes + off));
+    return (k & 1) ? a.y + b.y : a.x + b.x;
+}
+
 // --------------------------------------------------------------- the kernel
 // Conditional BS call (tau = 1, r = 0) from (Ivdt, IsvdW) in FP32
 // (rBergLib/rBergomiMT.cpp:598-602 with BlackScholes.cpp:16-21).  ITM strikes
@@ -548,7 +590,9 @@ __device__ __forceinline__ float rt_payoff_f32(float Ivdt, float IsvdW, float rh
 // REDRAW (a first-pass chunk drawn again for the second pass), the FP32 W1 /
 // W1perp tiles the epilogue reads.  Compiled per REDRAW so that the W1 and
 // W1perp Philox streams stay interleaved in the common case.
-template <int SK, bool REDRAW, bool MC>
+// FW1 = false (pass mode 3): no FP32 W1 tile, W1perp at the start of the
+// stage's FP32 region (the epilogue reads W1 back from the A tile).
+template <int SK, bool REDRAW, bool MC, bool FW1 = true>
 __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKeys& keys, uint64_t gpath, bool valid,
                                               int64_t m, int p, int h, int c, bool bnd, unsigned char* st,
                                               float* w1s)
@@ -611,8 +655,12 @@ __device__ __forceinline__ void produce_chunk(const MixedArgs& a, const PhiloxKe
 #pragma unroll
         for (int q = 0; q < SPT; q += 4) {
             const int at = ftile_at(p, SPT * h + q);
-            *(float4*)(w1s + at) = make_float4(w[q], w[q + 1], w[q + 2], w[q + 3]);
-            *(float4*)(w1ps + at) = make_float4(wp[q], wp[q + 1], wp[q + 2], wp[q + 3]);
+            if (FW1) {
+                *(float4*)(w1s + at) = make_float4(w[q], w[q + 1], w[q + 2], w[q + 3]);
+                *(float4*)(w1ps + at) = make_float4(wp[q], wp[q + 1], wp[q + 2], wp[q + 3]);
+            } else {
+                *(float4*)(w1s + at) = make_float4(wp[q], wp[q + 1], wp[q + 2], wp[q + 3]);
+            }
             if (MC) *(float4*)(w1s + kFWq + at) = make_float4(wq[q], wq[q + 1], wq[q + 2], wq[q + 3]);
         }
         // last real chunk of a pass that is not the last: its successor (chunk
@@ -885,7 +933,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int Np = a.Np, nc = a.nc;
     const PassPlan<PM> pp(a);
-    const int FB = (PM == 2) ? L.fstride : kStageFB;  // bytes per stage of the FP32-tile region
+    const int FB = (PM == 2 || PM == 3) ? L.fstride : kStageFB;  // bytes per stage of the FP32-tile region
     const int64_t ntiles = (a.B + kTileM - 1) / kTileM;
     const uint32_t sbytes = (uint32_t)(T32 ? strip_smem_bytes_t32(Np) : strip_smem_bytes(Np));
     const uint32_t half_g = (uint32_t)((T32 ? strip_bytes_t32(Np) : strip_bytes(Np)) / 2);  // hi -> lo in the global image
@@ -978,6 +1026,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                             produce_chunk_ext<SK, true, MC>(a, tile, c, bnd, st, w1s);
                         else
                             produce_chunk_ext<SK, false, MC>(a, tile, c, bnd, st, w1s);
+                    } else if (PM == 3) {
+                        produce_chunk<SK, false, MC, false>(a, keys, gpath, valid, m, p, h, c, bnd, st, w1s);
                     } else if (PM > 0 && redraw) {
                         produce_chunk<SK, true, MC>(a, keys, gpath, valid, m, p, h, c, bnd, st, w1s);
                     } else {
@@ -1041,14 +1091,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                 if (!mbar_wait_warp(smem_u32(accf + s), ph, a.err, 2, a.prof)) goto done;
                 tc_fence_after();
                 const float* w1s = (const float*)(base + L.f0 + s * FB);
-                const float* w1ps = w1s + kFW1p;
+                const float* w1ps = PM == 3 ? w1s : w1s + kFW1p;
                 const float* wqs = w1s + kFWq;  // plain Monte Carlo only
+                const unsigned char* ast = base + L.a0 + s * kStageA;  // pass mode 3: W1 = hi + lo of the A tile
 #pragma unroll 1
                 for (int hh = wg; hh < 2; hh += kEpiWGs) {
                     const int j0 = 16 * hh;
                     // the producers' FP32 operands first: these shared-memory loads are
                     // issued ahead of the TMEM load, so their latencies overlap
                     float w1v[16], w1pv[16];
+                    if constexpr (PM == 3) {
+                        a_tile_w1_16<SK>(ast, p, hh, w1v);
+#pragma unroll
+                        for (int jj = 0; jj < 16; jj += 4) {
+                            const float4 v = *(const float4*)(w1ps + ftile_at(p, j0 + jj));
+                            w1pv[jj] = v.x; w1pv[jj + 1] = v.y; w1pv[jj + 2] = v.z; w1pv[jj + 3] = v.w;
+                        }
+                    } else {
 #pragma unroll
                     for (int jj = 0; jj < 16; jj += 4) {
                         const int at = ftile_at(p, j0 + jj);
@@ -1056,14 +1115,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                         w1v[jj] = u.x; w1v[jj + 1] = u.y; w1v[jj + 2] = u.z; w1v[jj + 3] = u.w;
                         w1pv[jj] = v.x; w1pv[jj + 1] = v.y; w1pv[jj + 2] = v.z; w1pv[jj + 3] = v.w;
                     }
+                    }
                     const float* nexts = (const float*)(base + L.f0 + sn * FB);
-                    // pass mode 3: the last column's dW waits for the next chunk (its stage may not be
-                    // drawn yet with two stages); W1 at this chunk's first step completes the previous one's
-                    const float w_after = (hh == 0) ? w1s[ftile_at(p, 16)]
+                    // pass mode 3: the last column's dW is added with the next chunk, when W1 at its
+                    // first step (w_first) is at hand; the epilogue never waits for a later stage
+                    const float w_after = (hh == 0) ? (PM == 3 ? a_tile_w1_at<SK>(ast, p, 16) : w1s[ftile_at(p, 16)])
                                                     : (PM == 3 || !has_next ? 0.f
                                                        : bnd                ? w1s[kFBnd + p]
                                                                             : nexts[ftile_at(p, 0)]);
-                    const float w_first = (PM == 3 && hh == 1 && c > 0) ? w1s[ftile_at(p, 0)] : 0.f;
+                    const float w_first = (PM == 3 && hh == 1 && c > 0) ? a_tile_w1_at<SK>(ast, p, 0) : 0.f;
                     float wqv[MC ? 16 : 1], wq_after = 0.f;
                     if (MC) {
 #pragma unroll
@@ -2378,7 +2438,7 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
             A.np = (Np + kHalfCols - 1) / kHalfCols;
             A.n0 = (Np - kHalfCols * (A.np - 1)) / kChunk;
             A.ncache = A.np >= 3 ? A.n0 + kHalfCols / kChunk * (A.np - 3) : 0;
-            A.stages = 2;
+            A.stages = smem_layout(Np, 3, A.n_g, no, ns, false, kCSlots).total <= optin ? 3 : 2;
         }
     }
     if (backend == RBG_CONV_FFT) {
