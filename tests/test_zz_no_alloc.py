@@ -22,7 +22,8 @@ RTOL = 1e-12  # same kernels, same batching of the Philox stream: roundoff only
 # whose far-field reads A tiles back from a per-CTA device cache (tens of MB),
 # which does not fit the static scratch, so the static entry runs the two-pass
 # kernel that draws those tiles again.  Same products, another FP32
-# accumulation order in TMEM: prices agree to roundoff of that order.
+# accumulation order in TMEM, and W1 in the epilogue as drawn in FP32 instead
+# of read back as the 16-bit hi + lo pair: prices agree to about 1e-6.
 RTOL_TWO_PASS = (2e-6, 2e-5)  # prices; standard errors and implied vols
 
 
