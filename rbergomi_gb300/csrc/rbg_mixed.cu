@@ -265,6 +265,18 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 
+// Non-blocking test of a phase.
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Bounded wait for the phase of the given parity; false on timeout or when
 // another role already failed (then the caller winds down).  The error word
 // and the clock are polled every 64 tries only (at most 64 x 20 us apart).  With `prof` set (diagnostic
@@ -898,7 +910,7 @@ struct PassPlan {
 // RT only), 2 the caller's FP64 normals (a.ext, quadrature layout).
 // SK: split kind (0 FP16x3, 1 BF16x3, 2 TF32 with one compensation term).
 template <int SK, int PM, bool MC, int SRC = 0>
-__global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
+__global__ void __launch_bounds__(PM == 3 ? kThreads + 32 : kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
     constexpr int NS = MC ? 3 : 2;  // normal streams per path = sums per variance group
     constexpr int kStageFB = stage_f_bytes(NS);
@@ -929,6 +941,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     uint64_t* tmem_empty1 = bars + 13;
     uint64_t* cfull = bars + 14;   // [kCSlots]
     uint64_t* cempty = bars + 17;  // [kCSlots]
+    uint64_t* ydone = bars + 20;   // thread 1's far-field of a pass complete
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int Np = a.Np, nc = a.nc;
@@ -941,20 +954,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
     if (threadIdx.x == kMmaWarp * 32) {
         for (int s = 0; s < S; ++s) {
             mbar_init(smem_u32(full + s), kProdWarps);
-            // pass mode 3: the MMA thread also arrives once the stage's A tile is in the cache
-            mbar_init(smem_u32(empty + s), 1 + kEpiWarps + (PM == 3 ? 1 : 0));
+            // pass mode 3: both MMA threads commit, and thread 0 arrives once the A tile is in the cache
+            mbar_init(smem_u32(empty + s), 1 + kEpiWarps + (PM == 3 ? 2 : 0));
             mbar_init(smem_u32(accf + s), 1);
         }
         mbar_init(smem_u32(tmem_empty), kEpiWarps);
         if (PM == 3) {
             mbar_init(smem_u32(tmem_empty1), kEpiWarps);
+            mbar_init(smem_u32(ydone), 1);
             for (int s = 0; s < kCSlots; ++s) {
                 mbar_init(smem_u32(cfull + s), 1);
                 mbar_init(smem_u32(cempty + s), 1);
             }
         }
         mbar_init(smem_u32(strip_bar), 1);
-        mbar_init(smem_u32(final_bar), 1);
+        mbar_init(smem_u32(final_bar), PM == 3 ? 2 : 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         mbar_expect_tx(smem_u32(strip_bar), sbytes);
         if (PM == 2) {
@@ -1277,32 +1291,41 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
         const uint32_t strip_lo = strip_hi + (uint32_t)((T32 ? strip_smem_bytes_t32(Np) : strip_smem_bytes(Np)) / 2);
         constexpr bool wide = PM == 0 && !T32;  // the wide 16-bit strip exactly when one pass covers Np
         if constexpr (PM == 3) {
-            // Pass mode 3 (PassPlan), per tile and pass q: each own chunk c into its pass's
-            // columns [32 c, Pn) of buffer X, and before the last pass into all 256 columns of
-            // pass q + 1 in buffer Y; its A tile into the cache when a later pass reads it;
-            // then its share of the cached chunks 0 .. cb - 1 into Y, streamed through
-            // kCSlots shared-memory slots two items ahead.  (Loading a pass's first cached
-            // tiles during the pass before measured slower: 4.19 against 4.09 ms at N = 1024,
-            // 2^20 paths, from the wait for the stores at the end of the pass.)
+            // Pass mode 3 (PassPlan) issues its MMAs from two threads on two schedulers: one
+            // thread, issuing in order, competes for issue slots with sixteen warps of
+            // arithmetic, and one would hold the pipeline.  Each TMEM buffer is accumulated by
+            // one thread at a time:
+            //   thread 0 (warp 16): each own chunk c of pass q into its columns [32 c, Pn) of
+            //     buffer X, after the far-field of X (thread 1, pass q - 1) is complete; the A
+            //     tiles that later passes read into the cache, and the cached tiles back into
+            //     the slots, two items ahead of thread 1;
+            //   thread 1 (warp 17): before the last pass, each own chunk into all 256 columns
+            //     of pass q + 1 in buffer Y, then its share of the cached chunks 0 .. cb - 1;
+            //     one commit on `ydone` per pass marks buffer Y complete.
+            const int me = warp - kMmaWarp;
             unsigned char* cache = a.acache + (size_t)blockIdx.x * a.ncache * kStageA;
             const uint32_t cs0 = smem_u32(base + L.cs);
             int64_t G = 0;   // passes so far (all tiles): pass G accumulates in buffer G & 1
-            int64_t cl = 0;  // cached tiles loaded
-            int64_t cj = 0;  // cached tiles consumed (cl == cj at every pass end)
+            int64_t ny = 0;  // passes so far with a far-field (phases of ydone)
+            int64_t cl = 0;  // thread 0: cached tiles loaded
+            int64_t cj = 0;  // thread 1: cached tiles consumed
             int s = 0;
             uint32_t ph = 0;
             bool ok = mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof);
-            // cached chunk `chunk` into the next slot, once that slot's previous tile's MMAs are done
-            auto load = [&](int chunk) -> bool {
+            // thread 0: cached chunk `chunk` into the next slot, once thread 1 is done with the
+            // slot's previous tile (block: wait for it; otherwise only if it already is)
+            auto load = [&](int chunk, bool block) -> int {
                 const int slot = (int)(cl % kCSlots);
-                if (cl >= kCSlots &&
-                    !mbar_wait(smem_u32(cempty + slot), (uint32_t)((cl / kCSlots - 1) & 1), a.err, 9, a.prof))
-                    return false;
+                const uint32_t ce_bar = smem_u32(cempty + slot), ce_par = (uint32_t)((cl / kCSlots - 1) & 1);
+                if (cl >= kCSlots) {
+                    if (!block && !mbar_test(ce_bar, ce_par)) return 0;
+                    if (block && !mbar_wait(ce_bar, ce_par, a.err, 9, a.prof)) return -1;
+                }
                 const uint32_t bar = smem_u32(cfull + slot);
                 mbar_expect_tx(bar, (uint32_t)kStageA);
                 bulk_g2s(cs0 + (uint32_t)(slot * kStageA), cache + (size_t)chunk * kStageA, (uint32_t)kStageA, bar);
                 ++cl;
-                return true;
+                return 1;
             };
             for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
                 for (int q = 0; q < pp.np && ok; ++q, ++G) {
@@ -1312,27 +1335,72 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                     const int k = ce - cb, mC = has_y ? cb : 0;  // own chunks; cached chunks into Y
                     const uint32_t xb = tmem + (uint32_t)((G & 1) * kHalfCols);
                     const uint32_t yb = tmem + (uint32_t)(((G + 1) & 1) * kHalfCols);
-                    int u = 0;  // cached chunks of this pass done
+                    int u = 0;  // cached chunks of this pass loaded (thread 0) or consumed (thread 1)
                     for (int c = cb; c < ce && ok; ++c, s = (s + 1 == S) ? 0 : s + 1, ph ^= (s == 0)) {
-                        if (c == 0 && G >= 2) {
-                            // a tile's first pass starts a fresh buffer: pass G - 2 there is read
-                            if (!mbar_wait(smem_u32((G & 1) ? tmem_empty1 : tmem_empty), (uint32_t)(((G - 2) >> 1) & 1),
-                                           a.err, 4, a.prof)) {
+                        const int u_end = (int)((int64_t)mC * (c - cb + 1) / k);  // thread 1's items after chunk c
+                        if (me == 0) {
+                            if (c == 0 && G >= 2) {
+                                // a tile's first pass starts a fresh buffer: pass G - 2 there is read
+                                if (!mbar_wait(smem_u32((G & 1) ? tmem_empty1 : tmem_empty),
+                                               (uint32_t)(((G - 2) >> 1) & 1), a.err, 4, a.prof)) {
+                                    ok = false;
+                                    break;
+                                }
+                            }
+                            if (c == cb && q > 0 &&
+                                !mbar_wait(smem_u32(ydone), (uint32_t)((ny - 1) & 1), a.err, 13, a.prof)) {
+                                // thread 1's far-field of this buffer (pass q - 1) is complete
+                                ok = false;
+                                break;
+                            }
+                            if (!mbar_wait(smem_u32(full + s), ph, a.err, 5, a.prof)) {
                                 ok = false;
                                 break;
                             }
                             tc_fence_after();
-                        }
-                        if (!mbar_wait(smem_u32(full + s), ph, a.err, 5, a.prof)) {
-                            ok = false;
-                            break;
-                        }
-                        tc_fence_after();
-                        const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
-                        mma_chunk_narrow<SK>(xb + (uint32_t)(kChunk * c - P), ahi, strip_hi, strip_lo, 0u,
-                                             Pn - kChunk * c, q == 0 && c == 0);
-                        umma_commit(smem_u32(accf + s));
-                        if (has_y) {
+                            const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
+                            mma_chunk_narrow<SK>(xb + (uint32_t)(kChunk * c - P), ahi, strip_hi, strip_lo, 0u,
+                                                 Pn - kChunk * c, q == 0 && c == 0);
+                            umma_commit(smem_u32(accf + s));
+                            umma_commit(smem_u32(empty + s));
+                            if (c < a.ncache) {
+                                // the chunk's A tile into the cache; the stage may be refilled once
+                                // the copy has read it
+                                bulk_s2g(cache + (size_t)c * kStageA, ahi, (uint32_t)kStageA);
+                                const long long t0 = a.prof ? clock64() : 0;
+                                bulk_wait_read0();
+                                if (a.prof) atomicAdd(a.prof + 11, (unsigned long long)(clock64() - t0));
+                            }
+                            mbar_arrive(smem_u32(empty + s));
+                            if (mC > 0) {
+                                if (c == cb) {
+                                    // the cached tiles of chunks < cb are in global memory (the most
+                                    // recent store, when there is one, is this chunk's own)
+                                    if (c < a.ncache)
+                                        bulk_wait_done1();
+                                    else
+                                        bulk_wait_done0();
+                                }
+                                // two items ahead of thread 1, as far as the slots are free; the
+                                // rest of the pass's items without fail at its last chunk
+                                const int want = c + 1 == ce ? mC : (u_end + 2 < mC ? u_end + 2 : mC);
+                                while (ok && u < want) {
+                                    const int r = load(u, c + 1 == ce);
+                                    if (r < 0) ok = false;
+                                    if (r <= 0) break;
+                                    ++u;
+                                }
+                            }
+                        } else {
+                            if (!mbar_wait(smem_u32(full + s), ph, a.err, 5, a.prof)) {
+                                ok = false;
+                                break;
+                            }
+                            if (!has_y) {
+                                // the last pass has no far-field: the stage's arrival all the same
+                                mbar_arrive(smem_u32(empty + s));
+                                continue;
+                            }
                             if (c == cb && G >= 1) {
                                 // Y held pass G - 1: its columns are read
                                 if (!mbar_wait(smem_u32(((G + 1) & 1) ? tmem_empty1 : tmem_empty),
@@ -1340,51 +1408,39 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed_gemm(const __grid_constan
                                     ok = false;
                                     break;
                                 }
-                                tc_fence_after();
-                            }
-                            mma_chunk_narrow<SK>(yb, ahi, strip_hi, strip_lo, (uint32_t)(Pn - kChunk * c), kHalfCols,
-                                                 c == cb);
-                        }
-                        umma_commit(smem_u32(empty + s));
-                        if (c < a.ncache) {
-                            // this chunk's A tile into the cache; the stage may be refilled once the
-                            // copy has read it
-                            bulk_s2g(cache + (size_t)c * kStageA, ahi, (uint32_t)kStageA);
-                            const long long t0 = a.prof ? clock64() : 0;
-                            bulk_wait_read0();
-                            if (a.prof) atomicAdd(a.prof + 11, (unsigned long long)(clock64() - t0));
-                        }
-                        mbar_arrive(smem_u32(empty + s));
-                        if (c == cb && mC > 0) {
-                            // the cached tiles of chunks < cb are in global memory (the most recent
-                            // store, when there is one, is this chunk's own), then the first loads
-                            const long long t0 = a.prof ? clock64() : 0;
-                            if (c < a.ncache)
-                                bulk_wait_done1();
-                            else
-                                bulk_wait_done0();
-                            if (a.prof) atomicAdd(a.prof + 12, (unsigned long long)(clock64() - t0));
-                            for (int t = 0; t < kCSlots - 1 && t < mC && ok; ++t) ok = load(t);
-                        }
-                        const int u_end = (int)((int64_t)mC * (c - cb + 1) / k);
-                        for (; u < u_end && ok; ++u, ++cj) {
-                            const int slot = (int)(cj % kCSlots);
-                            if (!mbar_wait(smem_u32(cfull + slot), (uint32_t)((cj / kCSlots) & 1), a.err, 10, a.prof)) {
-                                ok = false;
-                                break;
                             }
                             tc_fence_after();
-                            mma_chunk_narrow<SK>(yb, cs0 + (uint32_t)(slot * kStageA), strip_hi, strip_lo,
-                                                 (uint32_t)(Pn - kChunk * u), kHalfCols, false);
-                            umma_commit(smem_u32(cempty + slot));
-                            if (u + kCSlots - 1 < mC) ok = load(u + kCSlots - 1);
+                            const uint32_t ahi = smem_u32(base + L.a0 + s * kStageA);
+                            mma_chunk_narrow<SK>(yb, ahi, strip_hi, strip_lo, (uint32_t)(Pn - kChunk * c), kHalfCols,
+                                                 c == cb);
+                            umma_commit(smem_u32(empty + s));
+                            for (; u < u_end && ok; ++u, ++cj) {
+                                const int slot = (int)(cj % kCSlots);
+                                if (!mbar_wait(smem_u32(cfull + slot), (uint32_t)((cj / kCSlots) & 1), a.err, 10,
+                                               a.prof)) {
+                                    ok = false;
+                                    break;
+                                }
+                                tc_fence_after();
+                                mma_chunk_narrow<SK>(yb, cs0 + (uint32_t)(slot * kStageA), strip_hi, strip_lo,
+                                                     (uint32_t)(Pn - kChunk * u), kHalfCols, false);
+                                umma_commit(smem_u32(cempty + slot));
+                            }
                         }
+                    }
+                    if (has_y) {
+                        if (me == 1 && ok) umma_commit(smem_u32(ydone));
+                        ++ny;
                     }
                 }
             }
-            // after an error: the loads in flight land and the stores finish before the CTA exits
-            for (; cj < cl; ++cj) mbar_drain(smem_u32(cfull + (int)(cj % kCSlots)), (uint32_t)((cj / kCSlots) & 1));
-            bulk_wait_done0();
+            if (me == 0) {
+                // after an error: the loads in flight land and the stores finish before the CTA exits;
+                // every load issued is of a slot whose fill thread 1 waits for, or the error word is set
+                for (int64_t i = cl - kCSlots < 0 ? 0 : cl - kCSlots; i < cl; ++i)
+                    mbar_drain(smem_u32(cfull + (int)(i % kCSlots)), (uint32_t)((i / kCSlots) & 1));
+                bulk_wait_done0();
+            }
         } else if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
             int64_t pass = 0;
             int s = 0;
@@ -2605,7 +2661,8 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
             else
                 kern = job.mc ? gemm_kernel<true, 0>(sk, pm) : gemm_kernel<false, 0>(sk, pm);
             e = allow_max_smem(kern);
-            if (e == cudaSuccess) kern<<<grid, kThreads, smem, st>>>(A);
+            // pass mode 3 adds a second MMA-issuing warp
+            if (e == cudaSuccess) kern<<<grid, pm == 3 ? kThreads + 32 : kThreads, smem, st>>>(A);
         }
         if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) {
