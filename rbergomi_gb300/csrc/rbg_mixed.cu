@@ -910,7 +910,7 @@ struct PassPlan {
 // RT only), 2 the caller's FP64 normals (a.ext, quadrature layout).
 // SK: split kind (0 FP16x3, 1 BF16x3, 2 TF32 with one compensation term).
 template <int SK, int PM, bool MC, int SRC = 0>
-__global__ void __launch_bounds__(PM == 3 ? kThreads + 32 : kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
+__global__ void __launch_bounds__(PM > 0 ? kThreads + 32 : kThreads, 1) k_mixed_gemm(const __grid_constant__ MixedArgs a)
 {
     constexpr int NS = MC ? 3 : 2;  // normal streams per path = sums per variance group
     constexpr int kStageFB = stage_f_bytes(NS);
@@ -954,8 +954,9 @@ __global__ void __launch_bounds__(PM == 3 ? kThreads + 32 : kThreads, 1) k_mixed
     if (threadIdx.x == kMmaWarp * 32) {
         for (int s = 0; s < S; ++s) {
             mbar_init(smem_u32(full + s), kProdWarps);
-            // pass mode 3: both MMA threads commit, and thread 0 arrives once the A tile is in the cache
-            mbar_init(smem_u32(empty + s), 1 + kEpiWarps + (PM == 3 ? 2 : 0));
+            // multi-pass modes: both MMA threads commit; pass mode 3's thread 0 also arrives once the
+            // A tile is in the cache
+            mbar_init(smem_u32(empty + s), 1 + kEpiWarps + (PM == 3 ? 2 : (PM > 0 ? 1 : 0)));
             mbar_init(smem_u32(accf + s), 1);
         }
         mbar_init(smem_u32(tmem_empty), kEpiWarps);
@@ -968,7 +969,7 @@ __global__ void __launch_bounds__(PM == 3 ? kThreads + 32 : kThreads, 1) k_mixed
             }
         }
         mbar_init(smem_u32(strip_bar), 1);
-        mbar_init(smem_u32(final_bar), PM == 3 ? 2 : 1);
+        mbar_init(smem_u32(final_bar), PM > 0 ? 2 : 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         mbar_expect_tx(smem_u32(strip_bar), sbytes);
         if (PM == 2) {
@@ -1442,6 +1443,10 @@ __global__ void __launch_bounds__(PM == 3 ? kThreads + 32 : kThreads, 1) k_mixed
                 bulk_wait_done0();
             }
         } else if (mbar_wait(smem_u32(strip_bar), 0, a.err, 3, a.prof)) {
+            // Pass modes 1 and 2 issue from two threads (warps 16 and 17), thread h the MMAs
+            // into TMEM columns [256 h, 256 h + 256) of the pass, so each half is accumulated
+            // by one thread; pass mode 0 from one.
+            const int me = warp - kMmaWarp;
             int64_t pass = 0;
             int s = 0;
             uint32_t ph = 0;
@@ -1475,11 +1480,19 @@ __global__ void __launch_bounds__(PM == 3 ? kThreads + 32 : kThreads, 1) k_mixed
                         const uint32_t bhi = win ? smem_u32(base + L.f0 + s * FB) : strip_hi;
                         const uint32_t blo = win ? bhi + (uint32_t)WB : strip_lo;
                         const int rbase = win ? lo : kChunk * c;
+                        int plo = lo, phi = hi;  // this thread's output columns of the chunk
+                        if constexpr (PM > 0) {
+                            const int mid = toff + kHalfCols;
+                            if (me == 0)
+                                phi = phi < mid ? phi : mid;
+                            else
+                                plo = plo > mid ? plo : mid;
+                        }
                         if constexpr (T32) {
                             // TF32: four K = 8 steps per chunk, A in TF32 (SW128) against the
                             // narrow strip's hi and lo halves at row offsets 8 apart
-                            for (int col0 = lo; col0 < hi; col0 += 256) {
-                                const int n = (hi - col0 < 256) ? (hi - col0) : 256;
+                            for (int col0 = plo; col0 < phi; col0 += 256) {
+                                const int n = (phi - col0 < 256) ? (phi - col0) : 256;
                                 const uint32_t id = idesc_tf32(n);
                                 const uint32_t jrow = (uint32_t)(col0 - rbase);
                                 const uint32_t d = tmem + (uint32_t)(col0 - toff);
@@ -1492,8 +1505,8 @@ __global__ void __launch_bounds__(PM == 3 ? kThreads + 32 : kThreads, 1) k_mixed
                                 }
                             }
                         } else {
-                            for (int col0 = lo; col0 < hi; col0 += 256) {
-                                const int n = (hi - col0 < 256) ? (hi - col0) : 256;
+                            for (int col0 = plo; col0 < phi; col0 += 256) {
+                                const int n = (phi - col0 < 256) ? (phi - col0) : 256;
                                 const uint32_t id = idesc_f16(n, SK);
                                 const uint32_t jrow = (uint32_t)(col0 - rbase);
                                 const uint32_t d = tmem + (uint32_t)(col0 - toff);
@@ -1522,7 +1535,10 @@ __global__ void __launch_bounds__(PM == 3 ? kThreads + 32 : kThreads, 1) k_mixed
                             }
                         }
                         umma_commit(smem_u32(empty + s));
-                        umma_commit(smem_u32(accf + s));
+                        // the epilogue reads this chunk's columns from one half: its thread signals
+                        // them (thread 0 for a redrawn chunk, which the epilogue only counts)
+                        if (PM == 0 || me == ((!redraw && kChunk * c - toff >= kHalfCols) ? 1 : 0))
+                            umma_commit(smem_u32(accf + s));
                     }
                 }
             }
@@ -2661,8 +2677,8 @@ int mixed_launch(const MixedJob& job, void* ws, uint64_t seed, int64_t path0, in
             else
                 kern = job.mc ? gemm_kernel<true, 0>(sk, pm) : gemm_kernel<false, 0>(sk, pm);
             e = allow_max_smem(kern);
-            // pass mode 3 adds a second MMA-issuing warp
-            if (e == cudaSuccess) kern<<<grid, pm == 3 ? kThreads + 32 : kThreads, smem, st>>>(A);
+            // the multi-pass modes add a second MMA-issuing warp
+            if (e == cudaSuccess) kern<<<grid, pm > 0 ? kThreads + 32 : kThreads, smem, st>>>(A);
         }
         if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) {
