@@ -43,7 +43,8 @@
 // drawn for real reads -- and each redrawn chunk brings the 528-row window it
 // reads into its stage's FP32-tile region by a bulk copy (33 KB, from L2).
 //
-// Warp roles (544 threads, one CTA per SM, persistent over 128-path tiles):
+// Warp roles (544 threads, 576 in the multi-pass modes; one CTA per SM,
+// persistent over 128-path tiles):
 //   warps 0-7   producers, two threads per path, 16 steps each per chunk:
 //               Philox -> FP32 normals; W1 split into hi/lo 16-bit A tiles
 //               (SW64 K-major layout); FP32 W1, W1perp kept for the epilogue
@@ -51,6 +52,10 @@
 //               chunk), one TMEM lane quadrant per warp: tcgen05.ld,
 //               X = Y2 + a1 W1 + a2 W1perp, v and the two integrals
 //   warp 16     TMEM allocation and the single-thread tcgen05.mma issuer
+//   warp 17     multi-pass modes only: a second issuing thread on another
+//               scheduler (one 256-column TMEM half, or pass mode 3's
+//               far-field), as one thread competing for issue slots with
+//               sixteen arithmetic warps held the multi-pass pipeline
 // Every mbarrier wait is bounded (%globaltimer); on expiry the kernel records
 // an error word, drains its MMAs, frees TMEM and returns.
 #include <cuda_bf16.h>
@@ -2488,7 +2493,8 @@ int mixed_prepare(const Plan& plan, const rbg_options& o, int64_t M, MixedJob& j
         if (r.args.n_o > kMixedMaxFused || smem_layout(Np, 2, r.args.n_g, r.args.n_o, 2, tf32).total > optin)
             job.fused = false;
     // Pass mode 3 replaces the redrawing two-pass schedule for the 16-bit splits
-    // and the RT estimator where two stages and the cached-tile slots fit.
+    // and the RT estimator where two stages (three where they fit) and the
+    // cached-tile slots fit.
     job.pmode = backend == RBG_CONV_GEMM ? pass_mode(Np) : 0;
     if (RBG_PASS3 && tile_cache && job.pmode == 1 && !tf32 && !mc) {
         bool fits = true;
