@@ -16,6 +16,11 @@ checks the invariants the kernel relies on: strip rows below Np + 16, TMEM
 columns below 512, cached chunk indices below ncache, a buffer handed from
 thread 1 (far-field) to thread 0 (own chunks) only after thread 0's wait for
 thread 1's pass, and a release wait before every buffer reuse.
+
+The second model does the same for pass modes 1 and 2 (512-column passes that
+draw the earlier chunks again), issued from two threads, one per 256-column
+TMEM half: one accumulating thread per column, the chunk's signal from the
+thread that owns its columns, and redrawn chunks within their strip window.
 """
 import numpy as np
 import pytest
@@ -136,3 +141,70 @@ def test_pass_mode_3_plan_sizes():
     assert plan(1024)[:3] == (4, 8, 32) and plan(1024)[5] == 16
     # the cache of a CTA holds ncache A tiles of 16 KB: 256 KB per CTA at N = 1024
     assert plan(1024)[5] * 2 * 128 * 32 * 2 == 256 * 1024
+
+
+def run_redraw_schedule(Np, W, gamma, windowed):
+    """Pass modes 1 (Np <= 1024) and 2 (windowed: the strip's first 528 rows
+    resident, redrawn chunks read a 528-row window): 512-column passes, pass 0
+    n0 = (Np - 512 (np - 1)) / 32 chunks, each later pass first redraws every
+    earlier chunk over all its columns, then takes its own 16.  Two issuing
+    threads, thread h the MMAs into TMEM columns [256 h, 256 h + 256) of the
+    pass; the thread whose half holds a chunk's columns signals them."""
+    PASS, WIN = 512, 528
+    npass = (Np + PASS - 1) // PASS
+    n0 = (Np - PASS * (npass - 1)) // KCH
+    nc = Np // KCH
+    gpad = np.concatenate([np.zeros(KCH), gamma, np.zeros(2 * Np)])
+    N = len(gamma)
+
+    def G(d):
+        d = np.asarray(d)
+        return np.where((d >= 0) & (d < N), gpad[np.clip(d, -KCH, 2 * Np - 1) + KCH], 0.0)
+
+    tmem = np.zeros(PASS)
+    cols = np.zeros(Np)
+    for q in range(npass):
+        cb = 0 if q == 0 else n0 + 16 * (q - 1)
+        ce = nc if q + 1 >= npass else n0 + 16 * q
+        toff = KCH * cb
+        writer = {}  # TMEM column -> the one thread that accumulates into it this pass
+        for c in range(ce):
+            redraw = c < cb
+            lo, hi = (KCH * cb if redraw else KCH * c), KCH * ce
+            tile = W[KCH * c:KCH * c + KCH]
+            for me in (0, 1):
+                mid = toff + HALF
+                plo, phi = (lo, min(hi, mid)) if me == 0 else (max(lo, mid), hi)
+                for col0 in range(plo, phi, HALF):
+                    n = min(HALF, phi - col0)
+                    d = col0 - toff
+                    assert 0 <= d and d + n <= PASS and (d < HALF) == (me == 0) and (d + n - 1 < HALF) == (me == 0)
+                    if windowed and redraw:
+                        # rows of the window copied for this chunk: strip rows lo - 32 c + [0, 528)
+                        jrow = col0 - lo
+                        assert jrow + 16 + n - 1 < WIN
+                    elif windowed:
+                        assert col0 - KCH * c + 16 + n - 1 < WIN  # the resident first 528 rows
+                    for t in range(d, d + n):
+                        assert writer.setdefault(t, me) == me, "two threads accumulate into one column"
+                    i = np.arange(n)[:, None]
+                    kp = np.arange(KCH)[None, :]
+                    val = (G(col0 - KCH * c + i - kp) * tile[None, :]).sum(axis=1)
+                    tmem[d:d + n] = val if c == 0 else tmem[d:d + n] + val
+            if not redraw:
+                owner = 1 if KCH * c - toff >= HALF else 0
+                d = KCH * c - toff
+                assert all(writer[t] == owner for t in range(d, d + KCH)), "accf from a thread that does not own the columns"
+                cols[KCH * c:KCH * c + KCH] = tmem[d:d + KCH]
+    return cols
+
+
+@pytest.mark.parametrize("Np", [544, 800, 1024, 1056, 1536, 2048, 3072, 4096])
+def test_redraw_passes_two_thread_split_is_the_causal_convolution(Np):
+    rng = np.random.default_rng(Np + 1)
+    N = Np - (Np // KCH) % 3
+    gamma = rng.standard_normal(N) / np.sqrt(1.0 + np.arange(N))
+    W = np.concatenate([rng.standard_normal(N), np.zeros(Np - N)])
+    cols = run_redraw_schedule(Np, W, gamma, windowed=Np > 1024)
+    ref = np.convolve(W, np.concatenate([gamma, np.zeros(Np - N)]))[:Np]
+    np.testing.assert_allclose(cols, ref, rtol=1e-11, atol=1e-11)
